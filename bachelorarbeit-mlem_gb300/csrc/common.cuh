@@ -1,0 +1,121 @@
+// common.cuh — error handling, launch accounting and small device helpers
+// shared by every translation unit of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <atomic>
+#include <string>
+
+#include "../../include/mlem.h"
+
+namespace mlem {
+
+// ------------------------------------------------------------ error state
+void set_error(const std::string& msg);
+const char* get_error();
+
+struct Error {
+    mlem_status code;
+    std::string msg;
+};
+
+// Throwing helpers used inside the C++ runtime; every extern "C" entry point
+// catches and converts to an mlem_status.
+[[noreturn]] void fail(mlem_status code, const std::string& msg);
+
+#define MLEM_CUDA(expr)                                                              \
+    do {                                                                             \
+        cudaError_t e_ = (expr);                                                     \
+        if (e_ != cudaSuccess)                                                       \
+            ::mlem::fail(e_ == cudaErrorMemoryAllocation ? MLEM_ENOMEM : MLEM_ECUDA, \
+                         std::string(#expr) + ": " + cudaGetErrorString(e_));        \
+    } while (0)
+
+#define MLEM_REQUIRE(cond, code, msg)          \
+    do {                                       \
+        if (!(cond)) ::mlem::fail(code, msg);  \
+    } while (0)
+
+// Kernel launch accounting (reported as gpu_launches by the benchmark).
+extern std::atomic<uint64_t> g_launches;
+inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Checks the launch that was just issued.
+#define MLEM_LAUNCHED()                       \
+    do {                                      \
+        ::mlem::count_launch();               \
+        MLEM_CUDA(cudaGetLastError());        \
+    } while (0)
+
+inline unsigned int ceil_div_u(uint64_t a, uint64_t b) { return (unsigned int)((a + b - 1) / b); }
+
+// ------------------------------------------------------------ device helpers
+// Streaming loads of the matrix: evict-first so the gathered vector stays in L2.
+__device__ __forceinline__ uint4 ld_stream_u4(const uint4* p) { return __ldcs(p); }
+__device__ __forceinline__ uint2 ld_stream_u2(const uint2* p) { return __ldcs(p); }
+__device__ __forceinline__ float4 ld_stream_f4(const float4* p) { return __ldcs(p); }
+
+// Value storage types: load 4 consecutive values (element index 4*v .. 4*v+3).
+template <typename V>
+struct Val4;
+
+template <>
+struct Val4<float> {
+    static __device__ __forceinline__ void load(const float* p, uint64_t v, float out[4]) {
+        float4 t = ld_stream_f4(reinterpret_cast<const float4*>(p) + v);
+        out[0] = t.x; out[1] = t.y; out[2] = t.z; out[3] = t.w;
+    }
+    static __device__ __forceinline__ float one(const float* p, uint64_t e) { return __ldcs(p + e); }
+};
+
+template <>
+struct Val4<__half> {
+    static __device__ __forceinline__ void load(const __half* p, uint64_t v, float out[4]) {
+        uint2 t = ld_stream_u2(reinterpret_cast<const uint2*>(p) + v);
+        __half2 a = *reinterpret_cast<__half2*>(&t.x);
+        __half2 b = *reinterpret_cast<__half2*>(&t.y);
+        float2 fa = __half22float2(a), fb = __half22float2(b);
+        out[0] = fa.x; out[1] = fa.y; out[2] = fb.x; out[3] = fb.y;
+    }
+    static __device__ __forceinline__ float one(const __half* p, uint64_t e) {
+        return __half2float(p[e]);
+    }
+};
+
+template <>
+struct Val4<__nv_bfloat16> {
+    static __device__ __forceinline__ void load(const __nv_bfloat16* p, uint64_t v, float out[4]) {
+        uint2 t = ld_stream_u2(reinterpret_cast<const uint2*>(p) + v);
+        __nv_bfloat162 a = *reinterpret_cast<__nv_bfloat162*>(&t.x);
+        __nv_bfloat162 b = *reinterpret_cast<__nv_bfloat162*>(&t.y);
+        float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
+        out[0] = fa.x; out[1] = fa.y; out[2] = fb.x; out[3] = fb.y;
+    }
+    static __device__ __forceinline__ float one(const __nv_bfloat16* p, uint64_t e) {
+        return __bfloat162float(p[e]);
+    }
+};
+
+// Elements of the col/val arrays are padded on the device to a multiple of
+// this count (zeros), so vector loads never leave the allocation.
+constexpr uint64_t kPad = 8;
+inline uint64_t padded(uint64_t n) { return (n + kPad - 1) / kPad * kPad; }
+
+inline size_t val_bytes(mlem_value_type t) { return t == MLEM_VAL_F32 ? 4 : 2; }
+
+// Device CSR view (rows of A, or rows of Aᵀ = columns of A).
+struct DevCsr {
+    uint32_t nrows = 0;       // number of rows of this operand
+    uint32_t ncols = 0;       // length of the vector it multiplies
+    uint64_t nnz = 0;
+    uint64_t* rowptr = nullptr;  // u64[nrows+1]
+    uint32_t* idx = nullptr;     // u32[padded(nnz)]
+    void* val = nullptr;         // f32/f16/bf16 [padded(nnz)]
+    mlem_value_type vt = MLEM_VAL_F32;
+    uint32_t max_row = 0;        // longest row
+};
+
+}  // namespace mlem

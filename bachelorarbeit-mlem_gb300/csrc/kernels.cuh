@@ -1,0 +1,155 @@
+// kernels.cuh — launchers of the device kernels (one declaration per kernel
+// family; definitions in spmv.cu, merge.cu, transpose.cu, siddon.cu, batch.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace mlem {
+
+// L2 persisting window for the gathered vector of one launch (0 bytes = none).
+struct L2Window {
+    const void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+// ------------------------------------------------------------- spmv.cu
+// Epilogue selection for the row-wise products.
+enum class Epi : int {
+    Correl = 0,   // out[r] = sum != 0 ? g[r] / sum : 0   (calcCorrel, kernel.cu:11-19)
+    Update = 1,   // f[c] = f[c]*sum/norm[c] (or f*sum if norm==0) (calcUpdate, kernel.cu:28-39)
+    Raw = 2       // out[r] = sum
+};
+
+struct EpiArgs {
+    Epi kind = Epi::Raw;
+    const int32_t* g = nullptr;   // Correl
+    float* out = nullptr;         // Correl: ratio; Raw: result
+    float* fwproj = nullptr;      // Correl: optional copy of the projection
+    float* f = nullptr;           // Update: image, updated in place
+    const float* norm = nullptr;  // Update
+};
+
+// Rows of `op` times x, one group of `lanes` (8/16/32) threads per row,
+// 128-bit loads of indices and values, deterministic reduction order.
+void launch_csrvec(const DevCsr& op, const float* x, const EpiArgs& epi, int lanes,
+                   L2Window win, cudaStream_t s);
+// bp[idx] += val * ratio[row] over the rows of A (calcBwProj_none_trans, kernel.cu:165-177).
+void launch_scatter(const DevCsr& A, const float* ratio, float* bp, int lanes, L2Window win,
+                    cudaStream_t s);
+// One pass over A: sum = A[r,:]·x, ratio = g[r]/sum, bp[idx] += val*ratio.
+void launch_fused_fp_scatter(const DevCsr& A, const float* x, const int32_t* g, float* bp,
+                             float* fwproj, L2Window win, cudaStream_t s);
+// f = f*bp/norm (or f*bp), then bp = 0 — update of the scatter forms.
+void launch_update_zero(float* f, float* bp, const float* norm, uint32_t n, cudaStream_t s);
+// Σ_r g_r log(fp_r) - fp_r over rows with fp_r > 0, FP64, fixed reduction order.
+void launch_loglik(const int32_t* g, const float* fwproj, uint32_t rows, double* part,
+                   double* out, cudaStream_t s);
+constexpr int kLoglikParts = 1024;
+int pick_lanes(uint64_t nnz, uint32_t rows);
+
+// ------------------------------------------------------------- merge.cu
+// Reference partition search for thread starts t*secsize (kernel.cu:190-241).
+void launch_merge_search_ref(const uint64_t* rowptr, uint32_t rows, uint64_t nnz,
+                             uint32_t secsize, uint64_t nthreads, int64_t* i_out,
+                             int64_t* j_out, cudaStream_t s);
+
+struct MergePlan {
+    uint32_t secsize = 0;
+    uint32_t threads = 0;   // threads per CTA
+    uint64_t ntiles = 0;
+    uint32_t* tile_i = nullptr;   // [ntiles+1]
+    uint64_t* tile_j = nullptr;   // [ntiles+1]
+    float* carry = nullptr;       // [ntiles]
+    uint32_t* carry_row = nullptr;// [ntiles]
+    float* head = nullptr;        // [ntiles]
+    size_t smem = 0;
+    void release();
+};
+// Builds the tile partition of `op` for a section size (device allocations).
+void merge_plan_build(const DevCsr& op, uint32_t secsize, MergePlan& plan, cudaStream_t s);
+// Merge-path product with deterministic carry fix-up (2 launches).
+void launch_merge_spmv(const DevCsr& op, const MergePlan& plan, const float* x,
+                       const EpiArgs& epi, L2Window win, cudaStream_t s);
+
+// ------------------------------------------------------------- transpose.cu
+// Stable counting sort by column of A (f32 values) -> Aᵀ with u32 row ids.
+void transpose_device(const DevCsr& A, DevCsr& AT, cudaStream_t s);
+// norm[c] = (float) Σ (double) val over column c.
+void colsum_from_transpose(const DevCsr& AT, float* norm, cudaStream_t s);
+void colsum_scatter(const DevCsr& A, float* norm, cudaStream_t s);
+// Value conversion f32 -> f16/bf16 (n elements, padded tail included).
+void convert_values(const float* src, void* dst, mlem_value_type vt, uint64_t n, cudaStream_t s);
+void convert_values_back(const void* src, float* dst, mlem_value_type vt, uint64_t n,
+                         cudaStream_t s);
+uint32_t max_row_length(const uint64_t* rowptr, uint32_t rows, cudaStream_t s);
+// Exclusive scan of u32 counts into u64 offsets; out[n] = total.
+void scan_counts_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t s);
+// rowptr u64[rows+1] with leading zero; device copy sanity check (monotone, last == nnz,
+// indices < cols).  Returns false when the CSR is malformed.
+bool validate_csr(const DevCsr& A, cudaStream_t s);
+
+// ------------------------------------------------------------- siddon.cu
+uint64_t siddon_rows(const mlem_geometry& geo);
+void siddon_count_host(const mlem_geometry& geo, uint64_t* rowptr);
+void siddon_fill_host(const mlem_geometry& geo, const uint64_t* rowptr, uint32_t* col, float* val);
+void siddon_generate_device(const mlem_geometry& geo, DevCsr& A, cudaStream_t s);
+
+// ------------------------------------------------------------- batch.cu
+// Interleaved batch state: slot b of voxel c is f[c*tile + b]; g and ratio
+// are [rows][tile]; remaining[b] counts the iterations slot b still runs.
+struct BatchArgs {
+    uint32_t tile = 16;          // instances per tile (8/16/32)
+    const int32_t* g = nullptr;
+    float* f = nullptr;
+    float* ratio = nullptr;
+    uint32_t* remaining = nullptr;
+};
+// ratio[r][b] = g[r][b] / (A f_b)[r] for all slots.
+void launch_batch_fp(const DevCsr& A, const BatchArgs& b, L2Window win, cudaStream_t s);
+// f_b = f_b * (Aᵀ ratio_b) / norm for slots with remaining > 0.
+void launch_batch_bp_update(const DevCsr& AT, const float* norm, const BatchArgs& b,
+                            L2Window win, cudaStream_t s);
+// remaining[b] -= 1 where positive.
+void launch_batch_tick(const BatchArgs& b, cudaStream_t s);
+// Scatter form (no Aᵀ): bp[c][b] += A[r,c] * ratio[r][b], then update + zero.
+void launch_batch_scatter(const DevCsr& A, const BatchArgs& b, float* bp, cudaStream_t s);
+void launch_batch_update_zero(const float* norm, uint32_t cols, const BatchArgs& b, float* bp,
+                              cudaStream_t s);
+// Slot b <- sinogram g (contiguous), image f0 (contiguous) or the constant init,
+// and its iteration count; slot b -> contiguous image.
+void launch_slot_put(int32_t* G, float* F, uint32_t rows, uint32_t cols, uint32_t BT, uint32_t b,
+                     const int32_t* g, float init, const float* f0, uint32_t* remaining,
+                     uint32_t iters, cudaStream_t s);
+void launch_slot_get(const float* F, uint32_t cols, uint32_t BT, uint32_t b, float* out,
+                     cudaStream_t s);
+
+}  // namespace mlem
+
+namespace mlem {
+// Launch through cudaLaunchKernelEx so the L2 access-policy window travels
+// with the launch (and into a CUDA graph node when captured).
+template <typename... KArgs, typename... Args>
+inline void launch_ex(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                      cudaStream_t s, L2Window win, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    unsigned n = 0;
+    if (win.bytes) {
+        attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+        attr[0].val.accessPolicyWindow.base_ptr = const_cast<void*>(win.ptr);
+        attr[0].val.accessPolicyWindow.num_bytes = win.bytes;
+        attr[0].val.accessPolicyWindow.hitRatio = 1.0f;
+        attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+        n = 1;
+    }
+    cfg.attrs = attr;
+    cfg.numAttrs = n;
+    MLEM_CUDA(cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...));
+    count_launch();
+}
+}  // namespace mlem

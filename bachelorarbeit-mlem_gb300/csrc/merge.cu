@@ -1,0 +1,332 @@
+// merge.cu — merge-path SpMV (Merrill & Garland) for the merge-based switch
+// (argv[8] = 0) of the reference: calcFwProj_merge_based / calcBwProj_merge_based
+// (kernel.cu:52-105), merge_based_start (kernel.cu:190-241) and
+// merge_based_work (kernel.cu:257-286).
+//
+// Work decomposition is the reference's: global thread t consumes secsize
+// items of the merged list (row ends ∪ nonzeros) starting at diagonal
+// t*secsize, with the coordinates the reference search finds.  What differs
+// is how the row fragments are combined: the reference adds every fragment
+// with a global atomicAdd (order nondeterministic); here a CTA of T threads
+// stages its tile of values and gathered x in shared memory, combines the
+// per-thread carries with a segmented scan in a fixed order, applies the
+// fused epilogue (correlation or update) to rows that end inside the tile,
+// and leaves the first row of every tile to a small fix-up kernel that adds
+// the carries of earlier tiles in tile order.  Results are deterministic.
+#include "kernels.cuh"
+
+#include <algorithm>
+
+namespace mlem {
+
+namespace {
+
+// Restatement of the reference search loop (kernel.cu:202-229).  The
+// reference can read csr_Rows[rows+1] (one past the end) when i reaches rows;
+// either outcome of that comparison ends the loop at i = rows, so the probe
+// is answered without the read.
+__host__ __device__ __forceinline__ void search_ref(const uint64_t* rowptr, int64_t rows,
+                                                    int64_t start, int64_t& oi, int64_t& oj) {
+    int64_t lefti = 0, righti = rows;
+    int64_t nexti = righti / 2;
+    int64_t nextj = start - nexti;
+    int64_t i = 0, j = start;
+    while (i != nexti) {
+        i = nexti;
+        j = nextj;
+        const bool right = (i + 1 > rows) ? true : ((int64_t)rowptr[i + 1] > j - 1);
+        if (right) righti = i;
+        else lefti = i + 1;
+        nexti = (lefti + righti) / 2;
+        nextj = start - nexti;
+    }
+    oi = i;
+    oj = j;
+}
+
+__global__ void k_search_ref(const uint64_t* __restrict__ rowptr, uint32_t rows, uint32_t secsize,
+                             uint64_t nthreads, int64_t* __restrict__ oi, int64_t* __restrict__ oj) {
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < nthreads;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        int64_t i, j;
+        search_ref(rowptr, rows, (int64_t)(t * secsize), i, j);
+        oi[t] = i;
+        oj[t] = j;
+    }
+}
+
+// Tile start coordinates at diagonals k*T*S; the end of the path is (rows, nnz).
+__global__ void k_tile_coords(const uint64_t* __restrict__ rowptr, uint32_t rows, uint64_t nnz,
+                              uint64_t tile_items, uint64_t ntiles, uint32_t* __restrict__ ti,
+                              uint64_t* __restrict__ tj) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k <= ntiles;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t d = k * tile_items;
+        if (d >= (uint64_t)rows + nnz) {
+            ti[k] = rows;
+            tj[k] = nnz;
+        } else {
+            int64_t i, j;
+            search_ref(rowptr, rows, (int64_t)d, i, j);
+            ti[k] = (uint32_t)i;
+            tj[k] = (uint64_t)j;
+        }
+    }
+}
+
+struct EpiDev {
+    int kind;
+    const int32_t* g;
+    float* out;
+    float* fwproj;
+    float* f;
+    const float* norm;
+    __device__ __forceinline__ void operator()(uint32_t r, float sum) const {
+        if (kind == (int)Epi::Correl) {
+            out[r] = (sum != 0.0f) ? __fdiv_rn((float)g[r], sum) : 0.0f;
+            if (fwproj) fwproj[r] = sum;
+        } else if (kind == (int)Epi::Update) {
+            const float t = __fmul_rn(f[r], sum);
+            const float n = norm[r];
+            f[r] = (n == 0.0f) ? t : __fdiv_rn(t, n);
+        } else {
+            out[r] = sum;
+        }
+    }
+};
+
+template <typename V>
+__device__ __forceinline__ float load_val(const V* p, uint64_t e) { return Val4<V>::one(p, e); }
+
+// One CTA per tile.  Dynamic shared memory: s_end[T*S+1] (u32, row ends
+// relative to the tile's first nonzero), s_val[T*S], s_x[T*S].
+template <typename V>
+__global__ void __launch_bounds__(256)
+k_merge_tile(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
+             const V* __restrict__ val, const float* __restrict__ x, uint32_t rows,
+             uint32_t S, const uint32_t* __restrict__ ti, const uint64_t* __restrict__ tj,
+             float* __restrict__ carry, uint32_t* __restrict__ carry_row, float* __restrict__ head,
+             EpiDev epi) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t T = blockDim.x;
+    const uint32_t TS = T * S;
+    uint32_t* s_end = reinterpret_cast<uint32_t*>(smem);
+    float* s_val = reinterpret_cast<float*>(smem + sizeof(uint32_t) * (TS + 4));
+    float* s_x = s_val + TS;
+    __shared__ float s_wv[32], s_inv[32];
+    __shared__ int s_wk[32], s_ink[32];
+
+    const uint64_t k = blockIdx.x;
+    const uint32_t I0 = ti[k], I1 = ti[k + 1];
+    const uint64_t J0 = tj[k], J1 = tj[k + 1];
+    const uint32_t nrow_l = I1 - I0;            // row ends inside the tile
+    const uint32_t nj = (uint32_t)(J1 - J0);    // nonzeros inside the tile
+    const uint32_t total = nrow_l + nj;         // items of this tile (< TS only in the last)
+
+    // Stage row ends (relative, clamped to nj+1) and the tile's nonzeros.
+    for (uint32_t u = threadIdx.x; u <= nrow_l; u += T) {
+        const uint64_t r = (uint64_t)I0 + u + 1;
+        uint64_t e = (r <= rows) ? rowptr[r] : J1 + 1;
+        e = e > J1 + 1 ? J1 + 1 : e;
+        s_end[u] = (uint32_t)(e - J0);
+    }
+    for (uint32_t u = threadIdx.x; u < nj; u += T) {
+        const uint64_t e = J0 + u;
+        s_val[u] = load_val<V>(val, e);
+        s_x[u] = __ldg(x + __ldcs(idx + e));
+    }
+    __syncthreads();
+
+    // Thread start coordinate: the same diagonal t*S as the reference's
+    // global thread (blockIdx*T + threadIdx)*S, located inside the tile.
+    const uint32_t dl = threadIdx.x * S;
+    float acc = 0.f, first = 0.f;
+    bool has_first = false;
+    uint32_t first_row = 0;
+    uint32_t i = nrow_l, j = nj;  // idle threads sit at the tile end
+    if (dl < total) {
+        uint32_t lo = dl > nj ? dl - nj : 0;
+        uint32_t hi = dl < nrow_l ? dl : nrow_l;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_end[mid] + mid >= dl) hi = mid;
+            else lo = mid + 1;
+        }
+        i = lo;
+        j = dl - lo;
+        first_row = i;
+        const uint32_t steps = min(S, total - dl);
+        for (uint32_t st = 0; st < steps; ++st) {
+            if (s_end[i] > j) {
+                acc = fmaf(s_val[j], s_x[j], acc);
+                ++j;
+            } else {
+                if (!has_first) {
+                    first = acc;
+                    has_first = true;
+                } else {
+                    epi(I0 + i, acc);  // row started and ended in this thread
+                }
+                acc = 0.f;
+                ++i;
+            }
+        }
+    }
+
+    // Inclusive segmented scan of the carries (key = local row at the end
+    // coordinate; keys are nondecreasing over threads).
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = T >> 5;
+    float v = acc;
+    const int key = (int)i;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float vv = __shfl_up_sync(0xffffffffu, v, o);
+        const int kk = __shfl_up_sync(0xffffffffu, key, o);
+        if (lane >= o && kk == key) v = vv + v;
+    }
+    if (lane == 31) {
+        s_wv[w] = v;
+        s_wk[w] = key;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float inv = 0.f;
+        int ink = -1;
+        for (int q = 0; q < nw; ++q) {
+            s_inv[q] = inv;
+            s_ink[q] = ink;
+            float lv = s_wv[q];
+            const int lk = s_wk[q];
+            if (lk == ink) lv = inv + lv;
+            inv = lv;
+            ink = lk;
+        }
+    }
+    __syncthreads();
+    if (key == s_ink[w]) v = s_inv[w] + v;
+    // carry into this thread = inclusive value of the previous thread
+    float cin = __shfl_up_sync(0xffffffffu, v, 1);
+    if (lane == 0) cin = (w == 0) ? 0.f : s_inv[w];
+    if (threadIdx.x == 0) cin = 0.f;
+
+    if (has_first) {
+        const float tot = cin + first;
+        if (first_row == 0) head[k] = tot;   // tile's first row: earlier tiles may add to it
+        else epi(I0 + first_row, tot);
+    }
+    if (threadIdx.x == T - 1) {
+        carry[k] = v;
+        carry_row[k] = I0 + (uint32_t)key;
+    }
+}
+
+// Rows that end in tile k but started earlier: sum of carries of the earlier
+// tiles that ended inside the row (in tile order), plus the tile's head.
+__global__ void k_merge_fixup(const uint32_t* __restrict__ ti, const float* __restrict__ carry,
+                              const uint32_t* __restrict__ carry_row,
+                              const float* __restrict__ head, uint64_t ntiles, EpiDev epi) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < ntiles;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t I0 = ti[k], I1 = ti[k + 1];
+        if (I1 == I0) continue;  // the tile's first row does not end here
+        int64_t q = (int64_t)k - 1;
+        while (q >= 0 && carry_row[q] == I0) --q;
+        float tot = 0.f;
+        bool any = false;
+        for (uint64_t p = (uint64_t)(q + 1); p < k; ++p) {
+            tot = any ? tot + carry[p] : carry[p];
+            any = true;
+        }
+        tot = any ? tot + head[k] : head[k];
+        epi(I0, tot);
+    }
+}
+
+template <typename V>
+void merge_launch_t(const DevCsr& op, const MergePlan& p, const float* x, const EpiDev& e,
+                    L2Window win, cudaStream_t s) {
+    launch_ex(k_merge_tile<V>, dim3((unsigned)p.ntiles), dim3(p.threads), p.smem, s, win,
+              op.rowptr, op.idx, static_cast<const V*>(op.val), x, op.nrows, p.secsize,
+              p.tile_i, p.tile_j, p.carry, p.carry_row, p.head, e);
+    const unsigned fg = std::max(1u, std::min<unsigned>(ceil_div_u(p.ntiles, 256), 152u * 8u));
+    launch_ex(k_merge_fixup, dim3(fg), dim3(256), 0, s, L2Window{}, p.tile_i, p.carry,
+              p.carry_row, p.head, p.ntiles, e);
+}
+
+}  // namespace
+
+void MergePlan::release() {
+    cudaFree(tile_i);
+    cudaFree(tile_j);
+    cudaFree(carry);
+    cudaFree(carry_row);
+    cudaFree(head);
+    tile_i = nullptr;
+    tile_j = nullptr;
+    carry = nullptr;
+    carry_row = nullptr;
+    head = nullptr;
+    ntiles = 0;
+}
+
+void launch_merge_search_ref(const uint64_t* rowptr, uint32_t rows, uint64_t nnz,
+                             uint32_t secsize, uint64_t nthreads, int64_t* i_out,
+                             int64_t* j_out, cudaStream_t s) {
+    (void)nnz;
+    if (nthreads == 0) return;
+    const unsigned grid = std::min<unsigned>(ceil_div_u(nthreads, 256), 152u * 32u);
+    k_search_ref<<<grid, 256, 0, s>>>(rowptr, rows, secsize, nthreads, i_out, j_out);
+    MLEM_LAUNCHED();
+}
+
+void merge_plan_build(const DevCsr& op, uint32_t secsize, MergePlan& plan, cudaStream_t s) {
+    MLEM_REQUIRE(secsize >= 1 && secsize <= 512, MLEM_EINVAL,
+                 "merge section size must be in 1..512");
+    plan.release();
+    plan.secsize = secsize;
+    uint32_t T = 4096 / secsize;
+    T = std::max(32u, std::min(256u, T & ~31u));
+    plan.threads = T;
+    const uint64_t TS = (uint64_t)T * secsize;
+    const uint64_t items = (uint64_t)op.nrows + op.nnz;
+    plan.ntiles = (items + TS - 1) / TS;
+    MLEM_REQUIRE(plan.ntiles < (1ull << 31), MLEM_EUNSUPPORTED, "merge path: too many tiles");
+    plan.smem = sizeof(uint32_t) * (TS + 4) + 2 * sizeof(float) * TS;
+    const uint64_t nt = std::max<uint64_t>(plan.ntiles, 1);
+    MLEM_CUDA(cudaMalloc(&plan.tile_i, sizeof(uint32_t) * (nt + 1)));
+    MLEM_CUDA(cudaMalloc(&plan.tile_j, sizeof(uint64_t) * (nt + 1)));
+    MLEM_CUDA(cudaMalloc(&plan.carry, sizeof(float) * nt));
+    MLEM_CUDA(cudaMalloc(&plan.carry_row, sizeof(uint32_t) * nt));
+    MLEM_CUDA(cudaMalloc(&plan.head, sizeof(float) * nt));
+    // opt in to the tile's shared memory once, outside any stream capture
+    switch (op.vt) {
+        case MLEM_VAL_F32:
+            MLEM_CUDA(cudaFuncSetAttribute(k_merge_tile<float>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem));
+            break;
+        case MLEM_VAL_F16:
+            MLEM_CUDA(cudaFuncSetAttribute(k_merge_tile<__half>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem));
+            break;
+        default:
+            MLEM_CUDA(cudaFuncSetAttribute(k_merge_tile<__nv_bfloat16>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem));
+    }
+    const unsigned grid = std::max(1u, std::min<unsigned>(ceil_div_u(plan.ntiles + 1, 256), 152u * 16u));
+    k_tile_coords<<<grid, 256, 0, s>>>(op.rowptr, op.nrows, op.nnz, TS, plan.ntiles, plan.tile_i,
+                                       plan.tile_j);
+    MLEM_LAUNCHED();
+}
+
+void launch_merge_spmv(const DevCsr& op, const MergePlan& plan, const float* x, const EpiArgs& epi,
+                       L2Window win, cudaStream_t s) {
+    if (plan.ntiles == 0) return;
+    EpiDev e{(int)epi.kind, epi.g, epi.out, epi.fwproj, epi.f, epi.norm};
+    switch (op.vt) {
+        case MLEM_VAL_F32: merge_launch_t<float>(op, plan, x, e, win, s); break;
+        case MLEM_VAL_F16: merge_launch_t<__half>(op, plan, x, e, win, s); break;
+        default: merge_launch_t<__nv_bfloat16>(op, plan, x, e, win, s);
+    }
+}
+
+}  // namespace mlem

@@ -1,0 +1,782 @@
+// runtime.cu — matrix handles, the MLEM iteration loop and the C ABI entry
+// points of the single-reconstruction path.
+//
+// The reference mlem() (main.cu:167-514) allocates, uploads, runs
+//   FP -> correl -> [AllReduce] -> BP -> update -> AllReduce(bp->f) -> 2x memset
+// per iteration with host synchronisation after each collective, and frees
+// everything at the end.  Here the matrix (A, the device-built Aᵀ and the
+// sensitivity image) is a resident handle; one iteration is two kernels (FP
+// with fused correlation, BP with fused update) or three in the scatter
+// forms, enqueued on one stream and replayed as a CUDA graph; there is no
+// memset, no collective and no host synchronisation inside the loop.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <thread>
+
+#include "runtime.h"
+
+namespace mlem {
+
+std::atomic<uint64_t> g_launches{0};
+
+namespace {
+thread_local std::string t_error;
+}
+
+void set_error(const std::string& msg) { t_error = msg; }
+const char* get_error() { return t_error.c_str(); }
+
+[[noreturn]] void fail(mlem_status code, const std::string& msg) { throw Error{code, msg}; }
+
+void Workspace::release() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    cudaFree(g);
+    cudaFree(f);
+    cudaFree(ratio);
+    cudaFree(bp);
+    cudaFree(fwproj);
+    cudaFree(ll_part);
+    cudaFree(ll_vals);
+    *this = Workspace();
+}
+
+void BatchState::alloc(uint32_t rows, uint32_t cols, uint32_t t, bool scatter) {
+    tile = t;
+    const uint64_t R = std::max<uint32_t>(rows, 1), C = std::max<uint32_t>(cols, 1);
+    MLEM_CUDA(cudaMalloc(&g, sizeof(int32_t) * R * t));
+    MLEM_CUDA(cudaMalloc(&f, sizeof(float) * C * t));
+    MLEM_CUDA(cudaMalloc(&ratio, sizeof(float) * R * t));
+    MLEM_CUDA(cudaMalloc(&remaining, sizeof(uint32_t) * 32));
+    MLEM_CUDA(cudaMalloc(&stage_g, sizeof(int32_t) * R));
+    MLEM_CUDA(cudaMalloc(&stage_f, sizeof(float) * C));
+    MLEM_CUDA(cudaMemset(g, 0, sizeof(int32_t) * R * t));
+    MLEM_CUDA(cudaMemset(f, 0, sizeof(float) * C * t));
+    MLEM_CUDA(cudaMemset(remaining, 0, sizeof(uint32_t) * 32));
+    bytes = (sizeof(int32_t) + sizeof(float)) * R * t + sizeof(float) * C * t + 4 * R + 4 * C + 128;
+    if (scatter) {
+        MLEM_CUDA(cudaMalloc(&bp, sizeof(float) * C * t));
+        MLEM_CUDA(cudaMemset(bp, 0, sizeof(float) * C * t));
+        bytes += sizeof(float) * C * t;
+    }
+}
+
+void BatchState::release() {
+    if (graph) cudaGraphExecDestroy(graph);
+    cudaFree(g);
+    cudaFree(f);
+    cudaFree(ratio);
+    cudaFree(bp);
+    cudaFree(remaining);
+    cudaFree(stage_g);
+    cudaFree(stage_f);
+    *this = BatchState();
+}
+
+static void free_csr(DevCsr& c) {
+    cudaFree(c.rowptr);
+    cudaFree(c.idx);
+    cudaFree(c.val);
+    c = DevCsr();
+}
+
+static uint64_t csr_bytes(const DevCsr& c) {
+    if (!c.rowptr) return 0;
+    return sizeof(uint64_t) * ((uint64_t)c.nrows + 1) + sizeof(uint32_t) * padded(c.nnz) +
+           val_bytes(c.vt) * padded(c.nnz);
+}
+
+void ensure_workspace(mlem_matrix* m) {
+    Workspace& w = m->ws;
+    if (w.ready) return;
+    const uint64_t R = std::max<uint32_t>(m->A.nrows, 1), C = std::max<uint32_t>(m->A.ncols, 1);
+    MLEM_CUDA(cudaMalloc(&w.g, sizeof(int32_t) * R));
+    MLEM_CUDA(cudaMalloc(&w.f, sizeof(float) * C));
+    MLEM_CUDA(cudaMalloc(&w.ratio, sizeof(float) * R));
+    MLEM_CUDA(cudaMalloc(&w.bp, sizeof(float) * C));
+    MLEM_CUDA(cudaMalloc(&w.fwproj, sizeof(float) * R));
+    MLEM_CUDA(cudaMalloc(&w.ll_part, sizeof(double) * kLoglikParts));
+    MLEM_CUDA(cudaMemsetAsync(w.bp, 0, sizeof(float) * C, m->stream));
+    MLEM_CUDA(cudaMemsetAsync(w.ratio, 0, sizeof(float) * R, m->stream));
+    w.ready = true;
+}
+
+const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
+    auto& plans = transposed ? m->plan_AT : m->plan_A;
+    auto it = plans.find(secsize);
+    if (it != plans.end()) return it->second;
+    MergePlan p;
+    merge_plan_build(transposed ? m->AT : m->A, secsize, p, m->stream);
+    MLEM_CUDA(cudaStreamSynchronize(m->stream));
+    return plans.emplace(secsize, p).first->second;
+}
+
+void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o) {
+    MLEM_REQUIRE(o.spmv == MLEM_SPMV_MERGE || o.spmv == MLEM_SPMV_CSR_VECTOR, MLEM_EINVAL,
+                 "spmv must be 0 (merge-based) or 1 (csr-vector)");
+    MLEM_REQUIRE(o.bp_mode == MLEM_BP_TRANS || o.bp_mode == MLEM_BP_SCATTER || o.bp_mode == MLEM_BP_FUSED,
+                 MLEM_EINVAL, "bp_mode must be 0 (transposed), 1 (scatter) or 2 (fused)");
+    MLEM_REQUIRE(o.secsize_fp >= 1 && o.secsize_fp <= 512 && o.secsize_bp >= 1 && o.secsize_bp <= 512,
+                 MLEM_EINVAL, "section sizes must be in 1..512");
+    MLEM_REQUIRE(o.bp_mode != MLEM_BP_TRANS || m->has_t, MLEM_EINVAL,
+                 "transposed back projection needs a matrix created with build_transpose = 1");
+}
+
+// One MLEM iteration on stream s using the matrix workspace.
+void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, double* ll_slot) {
+    Workspace& w = m->ws;
+    const DevCsr& A = m->A;
+    const bool want_ll = ll_slot != nullptr;
+    L2Window wf, wr;
+    if (o.l2_window) {
+        wf = {w.f, sizeof(float) * (size_t)A.ncols};
+        wr = {w.ratio, sizeof(float) * (size_t)A.nrows};
+    }
+    if (o.bp_mode == MLEM_BP_FUSED) {
+        launch_fused_fp_scatter(A, w.f, w.g, w.bp, want_ll ? w.fwproj : nullptr, wf, s);
+        launch_update_zero(w.f, w.bp, m->norm, A.ncols, s);
+    } else {
+        EpiArgs fe;
+        fe.kind = Epi::Correl;
+        fe.g = w.g;
+        fe.out = w.ratio;
+        fe.fwproj = want_ll ? w.fwproj : nullptr;
+        if (o.spmv == MLEM_SPMV_MERGE) launch_merge_spmv(A, merge_plan(m, false, o.secsize_fp), w.f, fe, wf, s);
+        else launch_csrvec(A, w.f, fe, pick_lanes(A.nnz, A.nrows), wf, s);
+        if (o.bp_mode == MLEM_BP_TRANS) {
+            EpiArgs be;
+            be.kind = Epi::Update;
+            be.f = w.f;
+            be.norm = m->norm;
+            if (o.spmv == MLEM_SPMV_MERGE)
+                launch_merge_spmv(m->AT, merge_plan(m, true, o.secsize_bp), w.ratio, be, wr, s);
+            else launch_csrvec(m->AT, w.ratio, be, pick_lanes(m->AT.nnz, m->AT.nrows), wr, s);
+        } else {
+            launch_scatter(A, w.ratio, w.bp, pick_lanes(A.nnz, A.nrows), wr, s);
+            launch_update_zero(w.f, w.bp, m->norm, A.ncols, s);
+        }
+    }
+    if (want_ll) launch_loglik(w.g, w.fwproj, A.nrows, w.ll_part, ll_slot, s);
+}
+
+float reference_initial_value(const mlem_matrix* m, const int32_t* g) {
+    // main.cu:83-97: FP32 running sum of norm in column order, integer sum of g
+    float sum_norm = 0.0f;
+    for (float v : m->norm_host) sum_norm += v;
+    int64_t sum_g = 0;
+    for (uint32_t i = 0; i < m->A.nrows; ++i) sum_g += g[i];
+    return (float)sum_g / sum_norm;
+}
+
+static void enable_l2_persisting(int dev) {
+    static std::mutex mu;
+    static std::map<int, bool> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done[dev]) return;
+    done[dev] = true;
+    int maxp = 0;
+    if (cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev) == cudaSuccess && maxp > 0) {
+        const size_t want = std::min<size_t>((size_t)maxp, 64ull << 20);
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want);  // context-scoped limit
+        cudaGetLastError();
+    }
+}
+
+// Runs `iters` iterations on the workspace (g and f already in place).
+static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
+                     double* ll_dev) {
+    if (o.loglik_every > 0 || !o.use_graph) {
+        for (uint32_t it = 0; it < iters; ++it) {
+            double* slot = (o.loglik_every > 0 && it % o.loglik_every == 0) ? ll_dev + it : nullptr;
+            enqueue_iteration(m, o, s, slot);
+        }
+        return;
+    }
+    constexpr uint32_t kChunk = 8;
+    auto get_graph = [&](uint32_t chunk) -> cudaGraphExec_t {
+        RunKey key{(int)o.spmv, (int)o.bp_mode, (int)o.secsize_fp, (int)o.secsize_bp, (int)o.l2_window,
+                   (int)chunk};
+        auto it = m->ws.graphs.find(key);
+        if (it != m->ws.graphs.end()) return it->second;
+        // plans must exist before capture (their build synchronises)
+        if (o.spmv == MLEM_SPMV_MERGE && o.bp_mode != MLEM_BP_FUSED) {
+            merge_plan(m, false, o.secsize_fp);
+            if (o.bp_mode == MLEM_BP_TRANS) merge_plan(m, true, o.secsize_bp);
+        }
+        cudaStream_t cs = m->stream;
+        cudaGraph_t graph = nullptr;
+        const uint64_t l0 = g_launches.load();
+        MLEM_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        try {
+            for (uint32_t q = 0; q < chunk; ++q) enqueue_iteration(m, o, cs, nullptr);
+        } catch (...) {
+            cudaStreamEndCapture(cs, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        MLEM_CUDA(cudaStreamEndCapture(cs, &graph));
+        // captured launches are counted when the graph is replayed, not here
+        const uint64_t nodes = g_launches.load() - l0;
+        g_launches.fetch_sub(nodes);
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        MLEM_CUDA(e);
+        m->ws.graphs[key] = exec;
+        m->ws.graph_nodes[key] = nodes;
+        return exec;
+    };
+    const uint32_t full = iters / kChunk, rest = iters % kChunk;
+    auto replay = [&](uint32_t chunk, uint32_t times) {
+        cudaGraphExec_t ge = get_graph(chunk);
+        const RunKey key{(int)o.spmv, (int)o.bp_mode, (int)o.secsize_fp, (int)o.secsize_bp,
+                         (int)o.l2_window, (int)chunk};
+        const uint64_t nodes = m->ws.graph_nodes[key];
+        for (uint32_t q = 0; q < times; ++q) {
+            MLEM_CUDA(cudaGraphLaunch(ge, s));
+            count_launch(nodes);
+        }
+    };
+    if (full) replay(kChunk, full);
+    if (rest) replay(1, rest);
+}
+
+static void postprocess_matrix(mlem_matrix* m, const mlem_matrix_opts& o) {
+    cudaStream_t s = m->stream;
+    DevCsr& A = m->A;
+    A.max_row = max_row_length(A.rowptr, A.nrows, s);
+    if (o.build_transpose) {
+        transpose_device(A, m->AT, s);
+        m->has_t = true;
+    }
+    // low-precision storage first, so the sensitivity image is Aᵀ1 of the
+    // matrix the projections actually use
+    if (o.value_type != MLEM_VAL_F32) {
+        auto lower = [&](DevCsr& c) {
+            void* nv = nullptr;
+            MLEM_CUDA(cudaMalloc(&nv, 2 * padded(c.nnz)));
+            convert_values(static_cast<const float*>(c.val), nv, o.value_type, padded(c.nnz), s);
+            MLEM_CUDA(cudaStreamSynchronize(s));
+            cudaFree(c.val);
+            c.val = nv;
+            c.vt = o.value_type;
+        };
+        lower(A);
+        if (m->has_t) lower(m->AT);
+    }
+    m->vt = o.value_type;
+    MLEM_CUDA(cudaMalloc(&m->norm, sizeof(float) * std::max<uint32_t>(A.ncols, 1)));
+    if (o.norm) {
+        MLEM_CUDA(cudaMemcpyAsync(m->norm, o.norm, sizeof(float) * A.ncols, cudaMemcpyHostToDevice, s));
+    } else if (m->has_t) {
+        colsum_from_transpose(m->AT, m->norm, s);
+    } else {
+        colsum_scatter(A, m->norm, s);
+    }
+    m->norm_host.resize(A.ncols);
+    if (A.ncols)
+        MLEM_CUDA(cudaMemcpyAsync(m->norm_host.data(), m->norm, sizeof(float) * A.ncols,
+                                  cudaMemcpyDeviceToHost, s));
+    MLEM_CUDA(cudaStreamSynchronize(s));
+}
+
+static mlem_matrix* new_matrix(const mlem_matrix_opts& o) {
+    MLEM_REQUIRE(o.value_type == MLEM_VAL_F32 || o.value_type == MLEM_VAL_F16 ||
+                     o.value_type == MLEM_VAL_BF16,
+                 MLEM_EINVAL, "value_type must be F32, F16 or BF16");
+    int ndev = 0;
+    MLEM_CUDA(cudaGetDeviceCount(&ndev));
+    MLEM_REQUIRE(o.device >= 0 && o.device < ndev, MLEM_EINVAL, "device ordinal out of range");
+    auto* m = new mlem_matrix();
+    m->device = o.device;
+    MLEM_CUDA(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+    enable_l2_persisting(o.device);
+    return m;
+}
+
+static void destroy_matrix(mlem_matrix* m) {
+    if (!m) return;
+    DeviceGuard dg(m->device);
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    m->ws.release();
+    for (auto& kv : m->plan_A) kv.second.release();
+    for (auto& kv : m->plan_AT) kv.second.release();
+    free_csr(m->A);
+    free_csr(m->AT);
+    cudaFree(m->norm);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+}
+
+static void check_host_csr(const mlem_csr_host* c) {
+    MLEM_REQUIRE(c != nullptr, MLEM_EINVAL, "csr is NULL");
+    MLEM_REQUIRE(c->rowptr != nullptr, MLEM_EINVAL, "csr rowptr is NULL");
+    MLEM_REQUIRE(c->nnz == 0 || (c->col && c->val), MLEM_EINVAL, "csr col/val is NULL");
+    MLEM_REQUIRE(c->rows >= 1 && c->cols >= 1, MLEM_EINVAL, "matrix must have rows and columns");
+    MLEM_REQUIRE(c->rowptr[0] == 0, MLEM_EINVAL, "rowptr[0] must be 0");
+    for (uint32_t r = 0; r < c->rows; ++r)
+        MLEM_REQUIRE(c->rowptr[r + 1] >= c->rowptr[r], MLEM_EINVAL, "rowptr must be nondecreasing");
+    MLEM_REQUIRE(c->rowptr[c->rows] == c->nnz, MLEM_EINVAL, "rowptr[rows] must equal nnz");
+}
+
+static void upload_csr(const mlem_csr_host* c, DevCsr& A, cudaStream_t s) {
+    A.nrows = c->rows;
+    A.ncols = c->cols;
+    A.nnz = c->nnz;
+    A.vt = MLEM_VAL_F32;
+    MLEM_CUDA(cudaMalloc(&A.rowptr, sizeof(uint64_t) * ((uint64_t)c->rows + 1)));
+    MLEM_CUDA(cudaMalloc(&A.idx, sizeof(uint32_t) * padded(c->nnz)));
+    MLEM_CUDA(cudaMalloc(&A.val, sizeof(float) * padded(c->nnz)));
+    MLEM_CUDA(cudaMemsetAsync(A.idx, 0, sizeof(uint32_t) * padded(c->nnz), s));
+    MLEM_CUDA(cudaMemsetAsync(A.val, 0, sizeof(float) * padded(c->nnz), s));
+    MLEM_CUDA(cudaMemcpyAsync(A.rowptr, c->rowptr, sizeof(uint64_t) * ((uint64_t)c->rows + 1),
+                              cudaMemcpyHostToDevice, s));
+    if (c->nnz) {
+        MLEM_CUDA(cudaMemcpyAsync(A.idx, c->col, sizeof(uint32_t) * c->nnz, cudaMemcpyHostToDevice, s));
+        MLEM_CUDA(cudaMemcpyAsync(A.val, c->val, sizeof(float) * c->nnz, cudaMemcpyHostToDevice, s));
+    }
+    MLEM_CUDA(cudaStreamSynchronize(s));
+    MLEM_REQUIRE(validate_csr(A, s), MLEM_EINVAL, "csr column index >= cols or malformed row pointers");
+}
+
+}  // namespace mlem
+
+using namespace mlem;
+
+uint64_t mlem_matrix::bytes() const {
+    uint64_t b = csr_bytes(A) + csr_bytes(AT) + sizeof(float) * (uint64_t)A.ncols;
+    for (auto& kv : plan_A) b += kv.second.ntiles * 24;
+    for (auto& kv : plan_AT) b += kv.second.ntiles * 24;
+    if (ws.ready) b += (uint64_t)A.nrows * 12 + (uint64_t)A.ncols * 8;
+    return b;
+}
+
+extern "C" {
+
+const char* mlem_last_error(void) { return get_error(); }
+const char* mlem_version(void) { return "mlem-gb300 1.0 (sm_103a)"; }
+uint64_t mlem_kernel_launch_count(void) { return g_launches.load(); }
+
+void mlem_matrix_opts_default(mlem_matrix_opts* o) {
+    if (!o) return;
+    o->value_type = MLEM_VAL_F32;
+    o->build_transpose = 1;
+    o->norm = nullptr;
+    o->device = 0;
+}
+
+void mlem_run_opts_default(mlem_run_opts* o) {
+    if (!o) return;
+    o->spmv = MLEM_SPMV_CSR_VECTOR;
+    o->bp_mode = MLEM_BP_TRANS;
+    o->secsize_fp = 5;
+    o->secsize_bp = 5;
+    o->use_graph = 1;
+    o->loglik_every = 0;
+    o->l2_window = 1;
+}
+
+mlem_status mlem_matrix_create(const mlem_csr_host* csr, const mlem_matrix_opts* opts, mlem_matrix** out) {
+    return guarded([&] {
+        MLEM_REQUIRE(out != nullptr, MLEM_EINVAL, "out is NULL");
+        *out = nullptr;
+        mlem_matrix_opts o;
+        mlem_matrix_opts_default(&o);
+        if (opts) o = *opts;
+        check_host_csr(csr);
+        DeviceGuard dg(o.device);
+        mlem_matrix* m = new_matrix(o);
+        try {
+            upload_csr(csr, m->A, m->stream);
+            postprocess_matrix(m, o);
+        } catch (...) {
+            destroy_matrix(m);
+            throw;
+        }
+        *out = m;
+    });
+}
+
+mlem_status mlem_matrix_generate(const mlem_geometry* geo, const mlem_matrix_opts* opts, mlem_matrix** out) {
+    return guarded([&] {
+        MLEM_REQUIRE(out != nullptr && geo != nullptr, MLEM_EINVAL, "NULL argument");
+        *out = nullptr;
+        mlem_matrix_opts o;
+        mlem_matrix_opts_default(&o);
+        if (opts) o = *opts;
+        DeviceGuard dg(o.device);
+        mlem_matrix* m = new_matrix(o);
+        try {
+            siddon_generate_device(*geo, m->A, m->stream);
+            MLEM_REQUIRE(m->A.nrows >= 1, MLEM_EINVAL, "geometry produced no rows");
+            postprocess_matrix(m, o);
+        } catch (...) {
+            destroy_matrix(m);
+            throw;
+        }
+        *out = m;
+    });
+}
+
+mlem_status mlem_matrix_destroy(mlem_matrix* m) {
+    return guarded([&] { destroy_matrix(m); });
+}
+
+mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info) {
+    return guarded([&] {
+        MLEM_REQUIRE(m && info, MLEM_EINVAL, "NULL argument");
+        info->rows = m->A.nrows;
+        info->cols = m->A.ncols;
+        info->nnz = m->A.nnz;
+        info->value_type = m->vt;
+        info->has_transpose = m->has_t ? 1 : 0;
+        info->device_bytes = m->bytes();
+        info->max_row_nnz = m->A.max_row;
+        info->max_col_nnz = m->has_t ? m->AT.max_row : 0;
+    });
+}
+
+mlem_status mlem_matrix_get_norm(const mlem_matrix* m, float* norm_out) {
+    return guarded([&] {
+        MLEM_REQUIRE(m && norm_out, MLEM_EINVAL, "NULL argument");
+        std::memcpy(norm_out, m->norm_host.data(), sizeof(float) * m->A.ncols);
+    });
+}
+
+mlem_status mlem_matrix_get_transpose(const mlem_matrix* m, uint64_t* colptr, uint32_t* rowidx, float* val) {
+    return guarded([&] {
+        MLEM_REQUIRE(m && colptr && rowidx && val, MLEM_EINVAL, "NULL argument");
+        MLEM_REQUIRE(m->has_t, MLEM_EINVAL, "matrix has no transpose");
+        DeviceGuard dg(m->device);
+        const DevCsr& T = m->AT;
+        MLEM_CUDA(cudaMemcpy(colptr, T.rowptr, sizeof(uint64_t) * ((uint64_t)T.nrows + 1), cudaMemcpyDeviceToHost));
+        if (T.nnz) {
+            MLEM_CUDA(cudaMemcpy(rowidx, T.idx, sizeof(uint32_t) * T.nnz, cudaMemcpyDeviceToHost));
+            float* tmp = nullptr;
+            MLEM_CUDA(cudaMalloc(&tmp, sizeof(float) * T.nnz));
+            convert_values_back(T.val, tmp, T.vt, T.nnz, m->stream);
+            MLEM_CUDA(cudaStreamSynchronize(m->stream));
+            const cudaError_t e = cudaMemcpy(val, tmp, sizeof(float) * T.nnz, cudaMemcpyDeviceToHost);
+            cudaFree(tmp);
+            MLEM_CUDA(e);
+        }
+    });
+}
+
+mlem_status mlem_matrix_get_csr(const mlem_matrix* m, uint64_t* rowptr, uint32_t* col, float* val) {
+    return guarded([&] {
+        MLEM_REQUIRE(m && rowptr && col && val, MLEM_EINVAL, "NULL argument");
+        DeviceGuard dg(m->device);
+        const DevCsr& A = m->A;
+        MLEM_CUDA(cudaMemcpy(rowptr, A.rowptr, sizeof(uint64_t) * ((uint64_t)A.nrows + 1), cudaMemcpyDeviceToHost));
+        if (A.nnz) {
+            MLEM_CUDA(cudaMemcpy(col, A.idx, sizeof(uint32_t) * A.nnz, cudaMemcpyDeviceToHost));
+            float* tmp = nullptr;
+            MLEM_CUDA(cudaMalloc(&tmp, sizeof(float) * A.nnz));
+            convert_values_back(A.val, tmp, A.vt, A.nnz, m->stream);
+            MLEM_CUDA(cudaStreamSynchronize(m->stream));
+            const cudaError_t e = cudaMemcpy(val, tmp, sizeof(float) * A.nnz, cudaMemcpyDeviceToHost);
+            cudaFree(tmp);
+            MLEM_CUDA(e);
+        }
+    });
+}
+
+mlem_status mlem_initial_value(const mlem_matrix* m, const int32_t* g, float* init_out) {
+    return guarded([&] {
+        MLEM_REQUIRE(m && g && init_out, MLEM_EINVAL, "NULL argument");
+        *init_out = reference_initial_value(m, g);
+    });
+}
+
+mlem_status mlem_run(mlem_matrix* m, const int32_t* g, const float* f0, uint32_t iterations,
+                     const mlem_run_opts* opts, float* f_out, double* loglik_out, mlem_stats* stats) {
+    return guarded([&] {
+        const auto t0 = std::chrono::steady_clock::now();
+        MLEM_REQUIRE(m && g && f_out, MLEM_EINVAL, "NULL argument");
+        MLEM_REQUIRE(iterations > 0, MLEM_EINVAL, "iterations must be > 0");
+        mlem_run_opts o;
+        mlem_run_opts_default(&o);
+        if (opts) o = *opts;
+        check_run_opts(m, o);
+        std::lock_guard<std::mutex> lk(m->mu);
+        DeviceGuard dg(m->device);
+        ensure_workspace(m);
+        cudaStream_t s = m->stream;
+        const uint32_t rows = m->A.nrows, cols = m->A.ncols;
+        Workspace& w = m->ws;
+        MLEM_CUDA(cudaMemcpyAsync(w.g, g, sizeof(int32_t) * rows, cudaMemcpyHostToDevice, s));
+        uint64_t h2d = sizeof(int32_t) * (uint64_t)rows;
+        if (f0) {
+            MLEM_CUDA(cudaMemcpyAsync(w.f, f0, sizeof(float) * cols, cudaMemcpyHostToDevice, s));
+            h2d += sizeof(float) * (uint64_t)cols;
+        } else {
+            std::vector<float> init(cols, reference_initial_value(m, g));
+            MLEM_CUDA(cudaMemcpyAsync(w.f, init.data(), sizeof(float) * cols, cudaMemcpyHostToDevice, s));
+            MLEM_CUDA(cudaStreamSynchronize(s));
+            h2d += sizeof(float) * (uint64_t)cols;
+        }
+        if (o.loglik_every > 0 && w.ll_cap < iterations) {
+            cudaFree(w.ll_vals);
+            w.ll_vals = nullptr;
+            MLEM_CUDA(cudaMalloc(&w.ll_vals, sizeof(double) * iterations));
+            w.ll_cap = iterations;
+        }
+        if (o.loglik_every > 0) {
+            std::vector<double> nan(iterations, std::numeric_limits<double>::quiet_NaN());
+            MLEM_CUDA(cudaMemcpyAsync(w.ll_vals, nan.data(), sizeof(double) * iterations, cudaMemcpyHostToDevice, s));
+            MLEM_CUDA(cudaStreamSynchronize(s));
+        }
+        cudaEvent_t e0, e1;
+        MLEM_CUDA(cudaEventCreate(&e0));
+        MLEM_CUDA(cudaEventCreate(&e1));
+        const uint64_t l0 = g_launches.load();
+        MLEM_CUDA(cudaEventRecord(e0, s));
+        run_loop(m, o, iterations, s, w.ll_vals);
+        MLEM_CUDA(cudaEventRecord(e1, s));
+        const uint64_t l1 = g_launches.load();
+        MLEM_CUDA(cudaMemcpyAsync(f_out, w.f, sizeof(float) * cols, cudaMemcpyDeviceToHost, s));
+        std::vector<double> ll;
+        if (o.loglik_every > 0) {
+            ll.resize(iterations);
+            MLEM_CUDA(cudaMemcpyAsync(ll.data(), w.ll_vals, sizeof(double) * iterations, cudaMemcpyDeviceToHost, s));
+        }
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (loglik_out) {
+            for (uint32_t i = 0; i < iterations; ++i)
+                loglik_out[i] = ll.empty() ? std::numeric_limits<double>::quiet_NaN() : ll[i];
+        }
+        if (stats) {
+            stats->seconds_total =
+                std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            stats->seconds_iterations = ms * 1e-3;
+            stats->iterations = iterations;
+            stats->kernel_launches = (uint32_t)(l1 - l0);
+            stats->bytes_h2d = h2d;
+            stats->bytes_d2h = sizeof(float) * (uint64_t)cols;
+            stats->loglik_last = std::numeric_limits<double>::quiet_NaN();
+            for (uint32_t i = iterations; i-- > 0;)
+                if (!ll.empty() && !std::isnan(ll[i])) {
+                    stats->loglik_last = ll[i];
+                    break;
+                }
+        }
+    });
+}
+
+mlem_status mlem_run_device(mlem_matrix* m, const int32_t* g_dev, float* f_dev, uint32_t iterations,
+                            const mlem_run_opts* opts, void* stream) {
+    return guarded([&] {
+        MLEM_REQUIRE(m && g_dev && f_dev, MLEM_EINVAL, "NULL argument");
+        MLEM_REQUIRE(iterations > 0, MLEM_EINVAL, "iterations must be > 0");
+        mlem_run_opts o;
+        mlem_run_opts_default(&o);
+        if (opts) o = *opts;
+        MLEM_REQUIRE(o.loglik_every == 0, MLEM_EINVAL, "log-likelihood output needs mlem_run");
+        check_run_opts(m, o);
+        std::lock_guard<std::mutex> lk(m->mu);
+        DeviceGuard dg(m->device);
+        ensure_workspace(m);
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        const uint32_t rows = m->A.nrows, cols = m->A.ncols;
+        Workspace& w = m->ws;
+        MLEM_CUDA(cudaMemcpyAsync(w.g, g_dev, sizeof(int32_t) * rows, cudaMemcpyDeviceToDevice, s));
+        MLEM_CUDA(cudaMemcpyAsync(w.f, f_dev, sizeof(float) * cols, cudaMemcpyDeviceToDevice, s));
+        run_loop(m, o, iterations, s, nullptr);
+        MLEM_CUDA(cudaMemcpyAsync(f_dev, w.f, sizeof(float) * cols, cudaMemcpyDeviceToDevice, s));
+    });
+}
+
+mlem_status mlem_forward_project(mlem_matrix* m, const float* f_dev, const int32_t* g_dev, float* ratio_dev,
+                                 float* fwproj_out_dev, const mlem_run_opts* opts, void* stream) {
+    return guarded([&] {
+        MLEM_REQUIRE(m && f_dev && g_dev && ratio_dev, MLEM_EINVAL, "NULL argument");
+        mlem_run_opts o;
+        mlem_run_opts_default(&o);
+        if (opts) o = *opts;
+        check_run_opts(m, o);
+        std::lock_guard<std::mutex> lk(m->mu);
+        DeviceGuard dg(m->device);
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        EpiArgs fe;
+        fe.kind = Epi::Correl;
+        fe.g = g_dev;
+        fe.out = ratio_dev;
+        fe.fwproj = fwproj_out_dev;
+        if (o.spmv == MLEM_SPMV_MERGE) launch_merge_spmv(m->A, merge_plan(m, false, o.secsize_fp), f_dev, fe, {}, s);
+        else launch_csrvec(m->A, f_dev, fe, pick_lanes(m->A.nnz, m->A.nrows), {}, s);
+    });
+}
+
+mlem_status mlem_back_project(mlem_matrix* m, const float* ratio_dev, float* bp_dev, const mlem_run_opts* opts,
+                              void* stream) {
+    return guarded([&] {
+        MLEM_REQUIRE(m && ratio_dev && bp_dev, MLEM_EINVAL, "NULL argument");
+        mlem_run_opts o;
+        mlem_run_opts_default(&o);
+        if (opts) o = *opts;
+        check_run_opts(m, o);
+        std::lock_guard<std::mutex> lk(m->mu);
+        DeviceGuard dg(m->device);
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (o.bp_mode == MLEM_BP_TRANS) {
+            EpiArgs be;
+            be.kind = Epi::Raw;
+            be.out = bp_dev;
+            if (o.spmv == MLEM_SPMV_MERGE) launch_merge_spmv(m->AT, merge_plan(m, true, o.secsize_bp), ratio_dev, be, {}, s);
+            else launch_csrvec(m->AT, ratio_dev, be, pick_lanes(m->AT.nnz, m->AT.nrows), {}, s);
+        } else {
+            MLEM_CUDA(cudaMemsetAsync(bp_dev, 0, sizeof(float) * m->A.ncols, s));
+            launch_scatter(m->A, ratio_dev, bp_dev, pick_lanes(m->A.nnz, m->A.nrows), {}, s);
+        }
+    });
+}
+
+mlem_status mlem_merge_path_search(const uint64_t* rowptr_dev, uint32_t rows, uint64_t nnz, uint32_t secsize,
+                                   uint64_t nthreads, int64_t* i_out_dev, int64_t* j_out_dev, void* stream) {
+    return guarded([&] {
+        MLEM_REQUIRE(rowptr_dev && i_out_dev && j_out_dev, MLEM_EINVAL, "NULL argument");
+        MLEM_REQUIRE(secsize >= 1, MLEM_EINVAL, "secsize must be > 0");
+        launch_merge_search_ref(rowptr_dev, rows, nnz, secsize, nthreads, i_out_dev, j_out_dev,
+                                static_cast<cudaStream_t>(stream));
+    });
+}
+
+mlem_status mlem_transpose_host(const mlem_csr_host* csr, uint64_t* colptr, uint32_t* rowidx, float* val) {
+    return guarded([&] {
+        MLEM_REQUIRE(colptr && (csr == nullptr || csr->nnz == 0 || (rowidx && val)), MLEM_EINVAL, "NULL argument");
+        check_host_csr(csr);
+        DeviceGuard dg(0);
+        cudaStream_t s = nullptr;
+        MLEM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        DevCsr A, T;
+        try {
+            upload_csr(csr, A, s);
+            transpose_device(A, T, s);
+            MLEM_CUDA(cudaStreamSynchronize(s));
+            MLEM_CUDA(cudaMemcpy(colptr, T.rowptr, sizeof(uint64_t) * ((uint64_t)T.nrows + 1), cudaMemcpyDeviceToHost));
+            if (T.nnz) {
+                MLEM_CUDA(cudaMemcpy(rowidx, T.idx, sizeof(uint32_t) * T.nnz, cudaMemcpyDeviceToHost));
+                MLEM_CUDA(cudaMemcpy(val, T.val, sizeof(float) * T.nnz, cudaMemcpyDeviceToHost));
+            }
+        } catch (...) {
+            free_csr(A);
+            free_csr(T);
+            cudaStreamDestroy(s);
+            throw;
+        }
+        free_csr(A);
+        free_csr(T);
+        cudaStreamDestroy(s);
+    });
+}
+
+mlem_status mlem_column_sums_host(const mlem_csr_host* csr, float* norm_out) {
+    return guarded([&] {
+        MLEM_REQUIRE(norm_out, MLEM_EINVAL, "NULL argument");
+        check_host_csr(csr);
+        DeviceGuard dg(0);
+        cudaStream_t s = nullptr;
+        MLEM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        DevCsr A, T;
+        float* n = nullptr;
+        try {
+            upload_csr(csr, A, s);
+            transpose_device(A, T, s);
+            MLEM_CUDA(cudaMalloc(&n, sizeof(float) * csr->cols));
+            colsum_from_transpose(T, n, s);
+            MLEM_CUDA(cudaStreamSynchronize(s));
+            MLEM_CUDA(cudaMemcpy(norm_out, n, sizeof(float) * csr->cols, cudaMemcpyDeviceToHost));
+        } catch (...) {
+            cudaFree(n);
+            free_csr(A);
+            free_csr(T);
+            cudaStreamDestroy(s);
+            throw;
+        }
+        cudaFree(n);
+        free_csr(A);
+        free_csr(T);
+        cudaStreamDestroy(s);
+    });
+}
+
+mlem_status mlem_partition_rows(const uint64_t* rowptr, uint64_t nnz, uint32_t rows, uint32_t nseg,
+                                uint32_t* segments, uint32_t* seg_rows, uint32_t* seg_nnz, uint64_t* offsets) {
+    return guarded([&] {
+        MLEM_REQUIRE(rowptr && segments && seg_rows && seg_nnz && offsets, MLEM_EINVAL, "NULL argument");
+        MLEM_REQUIRE(nseg >= 1, MLEM_EINVAL, "nseg must be > 0");
+        // partitionMatrix (main.cu:593-611): segment s starts at the first row
+        // whose start offset reaches s * nnz / nseg
+        segments[0] = 0;
+        segments[nseg] = rows;
+        uint32_t i = 0;
+        const double per = (double)nnz / (double)nseg;
+        for (uint32_t sgm = 0; sgm < nseg; ++sgm) {
+            for (; i <= rows; ++i)
+                if ((double)rowptr[i] >= per * sgm) break;
+            segments[sgm] = i;
+        }
+        for (uint32_t sgm = 0; sgm < nseg; ++sgm) {
+            seg_rows[sgm] = segments[sgm + 1] - segments[sgm];
+            seg_nnz[sgm] = (uint32_t)(rowptr[segments[sgm + 1]] - rowptr[segments[sgm]]);
+            offsets[sgm] = rowptr[segments[sgm]];
+        }
+    });
+}
+
+mlem_status mlem_reconstruct(const uint64_t* csr_rows, const uint32_t* csr_cols, const float* csr_vals,
+                             const uint64_t* csr_rows_trans, const uint32_t* csr_cols_trans,
+                             const float* csr_vals_trans, const int32_t* g, const float* norm, const float* f,
+                             float* result_f, uint32_t rows, uint32_t cols, uint64_t nnzs, uint32_t iterations,
+                             uint32_t device_numbers, uint32_t matrix_vector_mul, uint32_t secsize_fp,
+                             uint32_t secsize_bp, uint32_t using_trans) {
+    return guarded([&] {
+        MLEM_REQUIRE(device_numbers >= 1, MLEM_EINVAL, "device_numbers must be > 0");
+        MLEM_REQUIRE(device_numbers == 1, MLEM_EUNSUPPORTED,
+                     "one GPU per process: run independent replicas instead of device_numbers > 1");
+        MLEM_REQUIRE(using_trans <= 1 && matrix_vector_mul <= 1, MLEM_EINVAL, "switches must be 0 or 1");
+        MLEM_REQUIRE(g && f && result_f && norm, MLEM_EINVAL, "NULL argument");
+        mlem_csr_host c{rows, cols, nnzs, csr_rows, csr_cols, csr_vals};
+        mlem_matrix_opts mo;
+        mlem_matrix_opts_default(&mo);
+        mo.norm = norm;
+        const bool host_t = using_trans == 0 && csr_rows_trans && (nnzs == 0 || (csr_cols_trans && csr_vals_trans));
+        mo.build_transpose = (using_trans == 0 && !host_t) ? 1 : 0;
+        mlem_matrix* m = nullptr;
+        mlem_status st = mlem_matrix_create(&c, &mo, &m);
+        if (st != MLEM_OK) fail(st, get_error());
+        try {
+            if (host_t) {
+                // the caller supplied Aᵀ (as main.cu:100-105 does): upload it as is
+                DeviceGuard dg(m->device);
+                mlem_csr_host t{cols, rows, nnzs, csr_rows_trans, csr_cols_trans, csr_vals_trans};
+                check_host_csr(&t);
+                upload_csr(&t, m->AT, m->stream);
+                m->AT.max_row = max_row_length(m->AT.rowptr, m->AT.nrows, m->stream);
+                m->has_t = true;
+            }
+            mlem_run_opts o;
+            mlem_run_opts_default(&o);
+            o.spmv = matrix_vector_mul ? MLEM_SPMV_CSR_VECTOR : MLEM_SPMV_MERGE;
+            o.bp_mode = using_trans ? MLEM_BP_SCATTER : MLEM_BP_TRANS;
+            o.secsize_fp = secsize_fp;
+            o.secsize_bp = secsize_bp;
+            st = mlem_run(m, g, f, iterations, &o, result_f, nullptr, nullptr);
+            if (st != MLEM_OK) fail(st, get_error());
+        } catch (...) {
+            destroy_matrix(m);
+            throw;
+        }
+        destroy_matrix(m);
+    });
+}
+
+}  // extern "C"

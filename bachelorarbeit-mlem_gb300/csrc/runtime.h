@@ -1,0 +1,126 @@
+// runtime.h — internal host-side objects behind the C ABI.
+#pragma once
+
+#include <condition_variable>
+#include <new>
+#include <stdexcept>
+#include <tuple>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace mlem {
+
+// Runs fn and converts exceptions into a status plus the thread's error text.
+template <class F>
+mlem_status guarded(F&& fn) {
+    try {
+        fn();
+        return MLEM_OK;
+    } catch (const Error& e) {
+        set_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_error("host allocation failed");
+        return MLEM_ENOMEM;
+    } catch (const std::exception& e) {
+        set_error(e.what());
+        return MLEM_EINVAL;
+    }
+}
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) MLEM_CUDA(cudaSetDevice(dev));
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+struct RunKey {
+    int spmv, bp, ss_fp, ss_bp, l2, chunk;
+    bool operator<(const RunKey& o) const {
+        return std::tie(spmv, bp, ss_fp, ss_bp, l2, chunk) <
+               std::tie(o.spmv, o.bp, o.ss_fp, o.ss_bp, o.l2, o.chunk);
+    }
+};
+
+// Per-matrix run state reused across calls (buffers and captured graphs).
+struct Workspace {
+    bool ready = false;
+    int32_t* g = nullptr;      // [rows]
+    float* f = nullptr;        // [cols]
+    float* ratio = nullptr;    // [rows]
+    float* bp = nullptr;       // [cols] accumulator of the scatter forms (kept zero)
+    float* fwproj = nullptr;   // [rows] projection kept for the log-likelihood
+    double* ll_part = nullptr; // [kLoglikParts]
+    double* ll_vals = nullptr; // [ll_cap]
+    uint32_t ll_cap = 0;
+    std::map<RunKey, cudaGraphExec_t> graphs;
+    std::map<RunKey, uint64_t> graph_nodes;
+    void release();
+};
+
+// Batched tile state (also the server's per-matrix slot state).
+struct BatchState {
+    uint32_t tile = 0;
+    int32_t* g = nullptr;        // [rows][tile]
+    float* f = nullptr;          // [cols][tile]
+    float* ratio = nullptr;      // [rows][tile]
+    float* bp = nullptr;         // [cols][tile] scatter form only
+    uint32_t* remaining = nullptr;  // [tile]
+    int32_t* stage_g = nullptr;  // [rows] contiguous staging
+    float* stage_f = nullptr;    // [cols] contiguous staging
+    cudaGraphExec_t graph = nullptr;
+    uint64_t bytes = 0;
+    void alloc(uint32_t rows, uint32_t cols, uint32_t tile, bool scatter);
+    void release();
+    BatchArgs args() const {
+        BatchArgs a;
+        a.tile = tile;
+        a.g = g;
+        a.f = f;
+        a.ratio = ratio;
+        a.remaining = remaining;
+        return a;
+    }
+};
+
+}  // namespace mlem
+
+struct mlem_matrix {
+    int device = 0;
+    mlem_value_type vt = MLEM_VAL_F32;
+    mlem::DevCsr A, AT;
+    bool has_t = false;
+    float* norm = nullptr;
+    std::vector<float> norm_host;     // host copy (initial value computation)
+    cudaStream_t stream = nullptr;
+    mlem::Workspace ws;
+    std::map<uint32_t, mlem::MergePlan> plan_A, plan_AT;
+    uint32_t batch_tile = 0;          // autotuned batch tile (0 = not yet)
+    std::mutex mu;
+    uint64_t bytes() const;
+};
+
+namespace mlem {
+// Shared by the single, batched and server paths.
+void ensure_workspace(mlem_matrix* m);
+const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize);
+void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, double* ll_slot);
+void enqueue_batch_iteration(mlem_matrix* m, BatchState& b, cudaStream_t s);
+float reference_initial_value(const mlem_matrix* m, const int32_t* g);
+void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o);
+// Copies slot b of the interleaved batch state to/from contiguous device buffers.
+void batch_put_slot(BatchState& b, uint32_t rows, uint32_t cols, uint32_t slot, const int32_t* g_dev,
+                    float init, const float* f0_dev, uint32_t iters, cudaStream_t s);
+void batch_get_slot(const BatchState& b, uint32_t cols, uint32_t slot, float* f_dev, cudaStream_t s);
+}  // namespace mlem

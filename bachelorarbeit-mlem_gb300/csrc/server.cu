@@ -1,0 +1,540 @@
+// server.cu — batched reconstruction (many sinograms, one resident matrix)
+// and the continuous-batching request server.
+//
+// Batched form: instances are packed into tiles of BT slots (interleaved
+// image/ratio state, per-slot iteration counters on the device).  One
+// iteration of a tile = batched FP, batched BP + update, counter tick; it is
+// captured once as a CUDA graph and replayed until the longest slot of the
+// tile finishes.  BT is picked by timing 8/16/32 on the matrix (autotuner).
+//
+// Server: one worker thread owns per-matrix slot states.  Between iterations
+// it admits queued requests into free slots (a matrix's slot state is
+// allocated on first use if it fits the HBM budget), runs one iteration of
+// every matrix that has active slots, each matrix on its own stream so their
+// kernels overlap on the GPU, and hands finished images back.  A request's
+// arithmetic depends only on its slot's tile size, so its result is the same
+// alone and in a mix.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <numeric>
+#include <thread>
+#include <unordered_map>
+
+#include "runtime.h"
+
+namespace mlem {
+
+void enqueue_batch_iteration(mlem_matrix* m, BatchState& b, cudaStream_t s) {
+    const BatchArgs a = b.args();
+    launch_batch_fp(m->A, a, {}, s);
+    if (m->has_t) {
+        launch_batch_bp_update(m->AT, m->norm, a, {}, s);
+    } else {
+        launch_batch_scatter(m->A, a, b.bp, s);
+        launch_batch_update_zero(m->norm, m->A.ncols, a, b.bp, s);
+    }
+    launch_batch_tick(a, s);
+}
+
+void batch_put_slot(BatchState& b, uint32_t rows, uint32_t cols, uint32_t slot, const int32_t* g_dev,
+                    float init, const float* f0_dev, uint32_t iters, cudaStream_t s) {
+    launch_slot_put(b.g, b.f, rows, cols, b.tile, slot, g_dev, init, f0_dev, b.remaining, iters, s);
+}
+
+void batch_get_slot(const BatchState& b, uint32_t cols, uint32_t slot, float* f_dev, cudaStream_t s) {
+    launch_slot_get(b.f, cols, b.tile, slot, f_dev, s);
+}
+
+static uint64_t batch_state_bytes(uint32_t rows, uint32_t cols, uint32_t tile, bool scatter) {
+    const uint64_t R = std::max<uint32_t>(rows, 1), C = std::max<uint32_t>(cols, 1);
+    return 8ull * R * tile + 4ull * C * tile * (scatter ? 2 : 1) + 4 * R + 4 * C + 128;
+}
+
+// Replays one iteration of the tile as a CUDA graph (captured on first use).
+static void batch_step(mlem_matrix* m, BatchState& b, cudaStream_t s, bool use_graph, uint64_t& nodes) {
+    if (!use_graph) {
+        enqueue_batch_iteration(m, b, s);
+        return;
+    }
+    if (!b.graph) {
+        cudaStream_t cs = nullptr;
+        MLEM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaGraph_t graph = nullptr;
+        const uint64_t l0 = g_launches.load();
+        MLEM_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        try {
+            enqueue_batch_iteration(m, b, cs);
+        } catch (...) {
+            cudaStreamEndCapture(cs, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            cudaStreamDestroy(cs);
+            throw;
+        }
+        MLEM_CUDA(cudaStreamEndCapture(cs, &graph));
+        nodes = g_launches.load() - l0;
+        g_launches.fetch_sub(nodes);
+        const cudaError_t e = cudaGraphInstantiate(&b.graph, graph, 0);
+        cudaGraphDestroy(graph);
+        cudaStreamDestroy(cs);
+        MLEM_CUDA(e);
+    }
+    MLEM_CUDA(cudaGraphLaunch(b.graph, s));
+    count_launch(nodes);
+}
+
+// Picks the batch tile with the highest images*iterations per second.
+static uint32_t autotune_tile(mlem_matrix* m, cudaStream_t s) {
+    if (m->batch_tile) return m->batch_tile;
+    const uint32_t rows = m->A.nrows, cols = m->A.ncols;
+    uint32_t best = 16;
+    double best_rate = -1.0;
+    cudaEvent_t e0, e1;
+    MLEM_CUDA(cudaEventCreate(&e0));
+    MLEM_CUDA(cudaEventCreate(&e1));
+    for (uint32_t bt : {8u, 16u, 32u}) {
+        BatchState b;
+        try {
+            b.alloc(rows, cols, bt, !m->has_t);
+        } catch (const Error&) {
+            b.release();
+            cudaGetLastError();
+            continue;
+        }
+        // all slots idle (remaining = 0): the kernels run in full, f is kept
+        MLEM_CUDA(cudaMemsetAsync(b.f, 0, sizeof(float) * (uint64_t)std::max(cols, 1u) * bt, s));
+        enqueue_batch_iteration(m, b, s);  // warm-up
+        MLEM_CUDA(cudaEventRecord(e0, s));
+        for (int q = 0; q < 2; ++q) enqueue_batch_iteration(m, b, s);
+        MLEM_CUDA(cudaEventRecord(e1, s));
+        MLEM_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double rate = bt / std::max(1e-6, (double)ms);
+        if (rate > best_rate) {
+            best_rate = rate;
+            best = bt;
+        }
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        b.release();
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    m->batch_tile = best;
+    return best;
+}
+
+}  // namespace mlem
+
+using namespace mlem;
+
+// ------------------------------------------------------------------ server
+namespace {
+
+enum class ReqState { Queued, Running, Done, Cancelled };
+
+struct Request {
+    uint64_t id = 0;
+    uint32_t mid = 0;
+    std::vector<int32_t> g;
+    uint32_t iters = 0;
+    std::chrono::steady_clock::time_point t_submit, t_done;
+    ReqState state = ReqState::Queued;
+    std::vector<float> result;
+};
+
+struct MatrixSlots {
+    mlem_matrix* m = nullptr;
+    BatchState bs;
+    bool allocated = false;
+    cudaStream_t stream = nullptr;
+    std::vector<uint64_t> slot_req;   // 0 = free
+    std::vector<uint32_t> slot_left;
+    uint64_t graph_nodes = 0;
+    uint32_t tile = 0;
+};
+
+}  // namespace
+
+struct mlem_server {
+    mlem_server_opts opts{};
+    int device = 0;
+    std::vector<MatrixSlots> mats;
+    std::deque<uint64_t> queue;
+    std::unordered_map<uint64_t, Request> reqs;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::thread worker;
+    bool stop = false;
+    bool started = false;
+    uint64_t next_id = 1;
+    uint64_t budget = 0, in_use = 0;
+    mlem_server_stats st{};
+    std::string worker_error;
+
+    void run();
+    bool admit_locked();
+};
+
+bool mlem_server::admit_locked() {
+    bool any = false;
+    for (auto it = queue.begin(); it != queue.end();) {
+        Request& r = reqs[*it];
+        MatrixSlots& ms = mats[r.mid];
+        const uint32_t rows = ms.m->A.nrows, cols = ms.m->A.ncols;
+        if (!ms.allocated) {
+            const uint64_t need = batch_state_bytes(rows, cols, ms.tile, !ms.m->has_t);
+            if (in_use + need > budget) {
+                // release the state of idle matrices, then retry once
+                for (auto& o : mats)
+                    if (o.allocated && std::all_of(o.slot_req.begin(), o.slot_req.end(),
+                                                   [](uint64_t x) { return x == 0; })) {
+                        cudaStreamSynchronize(o.stream);
+                        in_use -= o.bs.bytes;
+                        o.bs.release();
+                        o.allocated = false;
+                    }
+                if (in_use + need > budget) {
+                    ++it;
+                    continue;
+                }
+            }
+            ms.bs.alloc(rows, cols, ms.tile, !ms.m->has_t);
+            ms.allocated = true;
+            in_use += ms.bs.bytes;
+        }
+        int slot = -1;
+        for (uint32_t b = 0; b < ms.tile; ++b)
+            if (ms.slot_req[b] == 0) {
+                slot = (int)b;
+                break;
+            }
+        if (slot < 0) {
+            ++it;
+            continue;
+        }
+        MLEM_CUDA(cudaMemcpyAsync(ms.bs.stage_g, r.g.data(), sizeof(int32_t) * rows, cudaMemcpyHostToDevice,
+                                  ms.stream));
+        const float init = reference_initial_value(ms.m, r.g.data());
+        batch_put_slot(ms.bs, rows, cols, (uint32_t)slot, ms.bs.stage_g, init, nullptr, r.iters, ms.stream);
+        MLEM_CUDA(cudaStreamSynchronize(ms.stream));  // stage_g is reused by the next admission
+        ms.slot_req[slot] = r.id;
+        ms.slot_left[slot] = r.iters;
+        r.state = ReqState::Running;
+        ++st.active;
+        --st.queued;
+        it = queue.erase(it);
+        any = true;
+    }
+    return any;
+}
+
+void mlem_server::run() {
+    DeviceGuard dg(device);
+    std::vector<float> host_f;
+    while (true) {
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            if (stop) break;
+            admit_locked();
+            bool active = false;
+            for (auto& ms : mats)
+                for (uint64_t x : ms.slot_req) active |= (x != 0);
+            if (!active) {
+                cv_work.wait_for(lk, std::chrono::milliseconds(20));
+                continue;
+            }
+        }
+        // one iteration of every matrix with work, overlapping across streams
+        for (auto& ms : mats) {
+            bool act = false;
+            for (uint64_t x : ms.slot_req) act |= (x != 0);
+            if (act) batch_step(ms.m, ms.bs, ms.stream, true, ms.graph_nodes);
+        }
+        for (auto& ms : mats)
+            if (ms.allocated) MLEM_CUDA(cudaStreamSynchronize(ms.stream));
+        std::unique_lock<std::mutex> lk(mu);
+        for (auto& ms : mats) {
+            const uint32_t cols = ms.m->A.ncols;
+            for (uint32_t b = 0; b < ms.tile; ++b) {
+                if (ms.slot_req[b] == 0) continue;
+                ++st.iterations_done;
+                if (--ms.slot_left[b] > 0) continue;
+                Request& r = reqs[ms.slot_req[b]];
+                batch_get_slot(ms.bs, cols, b, ms.bs.stage_f, ms.stream);
+                r.result.resize(cols);
+                MLEM_CUDA(cudaMemcpyAsync(r.result.data(), ms.bs.stage_f, sizeof(float) * cols,
+                                          cudaMemcpyDeviceToHost, ms.stream));
+                MLEM_CUDA(cudaStreamSynchronize(ms.stream));
+                r.t_done = std::chrono::steady_clock::now();
+                r.state = ReqState::Done;
+                ms.slot_req[b] = 0;
+                --st.active;
+                ++st.completed;
+            }
+        }
+        cv_done.notify_all();
+    }
+}
+
+extern "C" {
+
+void mlem_batch_opts_default(mlem_batch_opts* o) {
+    if (!o) return;
+    o->tile = 0;
+    o->use_graph = 1;
+    o->order_by_iterations = 1;
+}
+
+mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, const uint32_t* iterations,
+                           const float* f0, const mlem_batch_opts* opts, float* f_out, mlem_stats* stats) {
+    return guarded([&] {
+        const auto t0 = std::chrono::steady_clock::now();
+        MLEM_REQUIRE(m && g && iterations && f_out, MLEM_EINVAL, "NULL argument");
+        mlem_batch_opts o;
+        mlem_batch_opts_default(&o);
+        if (opts) o = *opts;
+        MLEM_REQUIRE(o.tile == 0 || o.tile == 8 || o.tile == 16 || o.tile == 32, MLEM_EINVAL,
+                     "batch tile must be 0 (autotune), 8, 16 or 32");
+        std::lock_guard<std::mutex> lk(m->mu);
+        DeviceGuard dg(m->device);
+        cudaStream_t s = m->stream;
+        const uint32_t rows = m->A.nrows, cols = m->A.ncols;
+        const uint32_t tile = o.tile ? o.tile : autotune_tile(m, s);
+        std::vector<uint32_t> order(count);
+        std::iota(order.begin(), order.end(), 0u);
+        if (o.order_by_iterations)
+            std::stable_sort(order.begin(), order.end(),
+                             [&](uint32_t a, uint32_t b) { return iterations[a] > iterations[b]; });
+        BatchState bs;
+        bs.alloc(rows, cols, tile, !m->has_t);
+        uint64_t nodes = 0, h2d = 0, d2h = 0, iters_total = 0;
+        cudaEvent_t e0, e1;
+        MLEM_CUDA(cudaEventCreate(&e0));
+        MLEM_CUDA(cudaEventCreate(&e1));
+        double dev_seconds = 0.0;
+        const uint64_t l0 = g_launches.load();
+        try {
+            for (uint32_t base = 0; base < count; base += tile) {
+                const uint32_t n = std::min(tile, count - base);
+                MLEM_CUDA(cudaMemsetAsync(bs.remaining, 0, sizeof(uint32_t) * 32, s));
+                uint32_t maxit = 0;
+                for (uint32_t b = 0; b < n; ++b) {
+                    const uint32_t i = order[base + b];
+                    const int32_t* gi = g + (uint64_t)i * rows;
+                    MLEM_CUDA(cudaMemcpyAsync(bs.stage_g, gi, sizeof(int32_t) * rows, cudaMemcpyHostToDevice, s));
+                    h2d += sizeof(int32_t) * (uint64_t)rows;
+                    const float* f0d = nullptr;
+                    float init = 0.f;
+                    if (f0) {
+                        MLEM_CUDA(cudaMemcpyAsync(bs.stage_f, f0 + (uint64_t)i * cols, sizeof(float) * cols,
+                                                  cudaMemcpyHostToDevice, s));
+                        h2d += sizeof(float) * (uint64_t)cols;
+                        f0d = bs.stage_f;
+                    } else {
+                        init = reference_initial_value(m, gi);
+                    }
+                    batch_put_slot(bs, rows, cols, b, bs.stage_g, init, f0d, iterations[i], s);
+                    maxit = std::max(maxit, iterations[i]);
+                    iters_total += iterations[i];
+                }
+                MLEM_CUDA(cudaEventRecord(e0, s));
+                for (uint32_t it = 0; it < maxit; ++it) batch_step(m, bs, s, o.use_graph != 0, nodes);
+                MLEM_CUDA(cudaEventRecord(e1, s));
+                for (uint32_t b = 0; b < n; ++b) {
+                    const uint32_t i = order[base + b];
+                    batch_get_slot(bs, cols, b, bs.stage_f, s);
+                    MLEM_CUDA(cudaMemcpyAsync(f_out + (uint64_t)i * cols, bs.stage_f, sizeof(float) * cols,
+                                              cudaMemcpyDeviceToHost, s));
+                    d2h += sizeof(float) * (uint64_t)cols;
+                }
+                MLEM_CUDA(cudaStreamSynchronize(s));
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                dev_seconds += ms * 1e-3;
+            }
+        } catch (...) {
+            cudaStreamSynchronize(s);
+            bs.release();
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+        bs.release();
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (stats) {
+            stats->seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            stats->seconds_iterations = dev_seconds;
+            stats->iterations = (uint32_t)std::min<uint64_t>(iters_total, 0xffffffffu);
+            stats->kernel_launches = (uint32_t)(g_launches.load() - l0);
+            stats->bytes_h2d = h2d;
+            stats->bytes_d2h = d2h;
+            stats->loglik_last = std::nan("");
+        }
+    });
+}
+
+void mlem_server_opts_default(mlem_server_opts* o) {
+    if (!o) return;
+    o->slots_per_matrix = 16;
+    o->hbm_budget_bytes = 0;
+    o->hbm_reserve_bytes = 2ull << 30;
+    o->queue_capacity = 4096;
+}
+
+mlem_status mlem_server_create(const mlem_server_opts* opts, mlem_server** out) {
+    return guarded([&] {
+        MLEM_REQUIRE(out, MLEM_EINVAL, "NULL argument");
+        *out = nullptr;
+        auto* s = new mlem_server();
+        mlem_server_opts_default(&s->opts);
+        if (opts) s->opts = *opts;
+        if (!(s->opts.slots_per_matrix == 8 || s->opts.slots_per_matrix == 16 || s->opts.slots_per_matrix == 32)) {
+            delete s;
+            fail(MLEM_EINVAL, "slots_per_matrix must be 8, 16 or 32");
+        }
+        cudaGetDevice(&s->device);
+        if (s->opts.hbm_budget_bytes) {
+            s->budget = s->opts.hbm_budget_bytes;
+        } else {
+            size_t fr = 0, tot = 0;
+            MLEM_CUDA(cudaMemGetInfo(&fr, &tot));
+            s->budget = fr > s->opts.hbm_reserve_bytes ? fr - s->opts.hbm_reserve_bytes : 0;
+        }
+        *out = s;
+    });
+}
+
+mlem_status mlem_server_add_matrix(mlem_server* s, mlem_matrix* m, uint32_t* matrix_id) {
+    return guarded([&] {
+        MLEM_REQUIRE(s && m && matrix_id, MLEM_EINVAL, "NULL argument");
+        std::lock_guard<std::mutex> lk(s->mu);
+        MLEM_REQUIRE(!s->started, MLEM_EBUSY, "add matrices before the first submit");
+        MLEM_REQUIRE(s->mats.empty() || m->device == s->device, MLEM_EINVAL, "all matrices must share a device");
+        s->device = m->device;
+        MatrixSlots ms;
+        ms.m = m;
+        ms.tile = s->opts.slots_per_matrix;
+        ms.slot_req.assign(ms.tile, 0);
+        ms.slot_left.assign(ms.tile, 0);
+        DeviceGuard dg(m->device);
+        MLEM_CUDA(cudaStreamCreateWithFlags(&ms.stream, cudaStreamNonBlocking));
+        s->mats.push_back(std::move(ms));
+        *matrix_id = (uint32_t)(s->mats.size() - 1);
+    });
+}
+
+mlem_status mlem_server_submit(mlem_server* s, uint32_t matrix_id, const int32_t* g, uint32_t iterations,
+                               uint64_t* request_id) {
+    return guarded([&] {
+        MLEM_REQUIRE(s && g && request_id, MLEM_EINVAL, "NULL argument");
+        MLEM_REQUIRE(iterations > 0, MLEM_EINVAL, "iterations must be > 0");
+        std::lock_guard<std::mutex> lk(s->mu);
+        MLEM_REQUIRE(matrix_id < s->mats.size(), MLEM_EINVAL, "unknown matrix id");
+        if (!s->worker_error.empty()) fail(MLEM_ECUDA, "server worker stopped: " + s->worker_error);
+        if (s->queue.size() >= s->opts.queue_capacity) {
+            ++s->st.rejected;
+            fail(MLEM_EBUSY, "server queue full");
+        }
+        Request r;
+        r.id = s->next_id++;
+        r.mid = matrix_id;
+        const uint32_t rows = s->mats[matrix_id].m->A.nrows;
+        r.g.assign(g, g + rows);
+        r.iters = iterations;
+        r.t_submit = std::chrono::steady_clock::now();
+        *request_id = r.id;
+        s->queue.push_back(r.id);
+        s->reqs.emplace(r.id, std::move(r));
+        ++s->st.submitted;
+        ++s->st.queued;
+        if (!s->started) {
+            s->started = true;
+            s->worker = std::thread([s] {
+                try {
+                    s->run();
+                } catch (const Error& e) {
+                    std::lock_guard<std::mutex> l2(s->mu);
+                    s->worker_error = e.msg;
+                    s->cv_done.notify_all();
+                }
+            });
+        }
+        s->cv_work.notify_one();
+    });
+}
+
+mlem_status mlem_server_wait(mlem_server* s, uint64_t request_id, float* f_out, uint32_t timeout_ms,
+                             double* latency_s) {
+    return guarded([&] {
+        MLEM_REQUIRE(s, MLEM_EINVAL, "NULL argument");
+        std::unique_lock<std::mutex> lk(s->mu);
+        auto it = s->reqs.find(request_id);
+        MLEM_REQUIRE(it != s->reqs.end(), MLEM_EINVAL, "unknown request id");
+        const bool ok = s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] {
+            auto jt = s->reqs.find(request_id);
+            return jt->second.state == ReqState::Done || jt->second.state == ReqState::Cancelled ||
+                   !s->worker_error.empty();
+        });
+        Request& r = s->reqs.find(request_id)->second;
+        if (r.state == ReqState::Cancelled) {
+            s->reqs.erase(request_id);
+            fail(MLEM_EINVAL, "request was cancelled");
+        }
+        if (r.state != ReqState::Done) {
+            if (!s->worker_error.empty()) fail(MLEM_ECUDA, "server worker stopped: " + s->worker_error);
+            MLEM_REQUIRE(ok, MLEM_ETIMEOUT, "request not finished within the timeout");
+        }
+        if (f_out) std::memcpy(f_out, r.result.data(), sizeof(float) * r.result.size());
+        if (latency_s) *latency_s = std::chrono::duration<double>(r.t_done - r.t_submit).count();
+        s->reqs.erase(request_id);
+    });
+}
+
+mlem_status mlem_server_cancel(mlem_server* s, uint64_t request_id) {
+    return guarded([&] {
+        MLEM_REQUIRE(s, MLEM_EINVAL, "NULL argument");
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->reqs.find(request_id);
+        MLEM_REQUIRE(it != s->reqs.end(), MLEM_EINVAL, "unknown request id");
+        MLEM_REQUIRE(it->second.state == ReqState::Queued, MLEM_EINVAL, "request is not queued");
+        s->queue.erase(std::remove(s->queue.begin(), s->queue.end(), request_id), s->queue.end());
+        it->second.state = ReqState::Cancelled;
+        --s->st.queued;
+        ++s->st.cancelled;
+        s->cv_done.notify_all();
+    });
+}
+
+mlem_status mlem_server_get_stats(mlem_server* s, mlem_server_stats* st) {
+    return guarded([&] {
+        MLEM_REQUIRE(s && st, MLEM_EINVAL, "NULL argument");
+        std::lock_guard<std::mutex> lk(s->mu);
+        *st = s->st;
+        st->hbm_in_use = s->in_use;
+    });
+}
+
+mlem_status mlem_server_destroy(mlem_server* s) {
+    return guarded([&] {
+        if (!s) return;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stop = true;
+        }
+        s->cv_work.notify_all();
+        if (s->worker.joinable()) s->worker.join();
+        DeviceGuard dg(s->device);
+        for (auto& ms : s->mats) {
+            if (ms.stream) cudaStreamSynchronize(ms.stream);
+            ms.bs.release();
+            if (ms.stream) cudaStreamDestroy(ms.stream);
+        }
+        delete s;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,370 @@
+// spmv.cu — row-parallel projection kernels of the MLEM iteration.
+//
+//   forward projection + correlation   (calcFwProj_csr_vector + calcCorrel,
+//                                        kernel.cu:118-130, 297-336, 11-19)
+//   back projection over Aᵀ + update   (calcBwProj_csr_vector + calcUpdate,
+//                                        kernel.cu:141-153, 28-39)
+//   scatter back projection over A     (calcBwProj_none_trans, kernel.cu:165-177, 347-370)
+//   fused single pass FP+correl+scatter (no reference counterpart; same arithmetic)
+//
+// Design: a group of LPR lanes owns one row; each lane streams aligned 16-byte
+// vectors of column indices and values (4 elements per vector, the row head
+// and tail are masked), gathers x[col] through the read-only path, accumulates
+// with FMA in FP32 and the group reduces with a fixed xor butterfly, so every
+// row sum has one deterministic order.  The correlation and the multiplicative
+// update are applied by the group leader in the same kernel, so an MLEM
+// iteration is two launches and never needs a memset.
+#include "kernels.cuh"
+
+namespace mlem {
+
+namespace {
+
+__device__ __forceinline__ bool in_row(uint64_t e, uint64_t s, uint64_t t) { return e >= s && e < t; }
+
+template <typename V>
+struct Vec4 {
+    uint4 c;
+    float a[4];
+    __device__ __forceinline__ void load(const uint4* idx4, const V* val, uint64_t v) {
+        c = __ldcs(idx4 + v);
+        Val4<V>::load(val, v, a);
+    }
+};
+
+// Gathers for one 4-element vector (masked), then the FMAs in element order.
+__device__ __forceinline__ void gather4(const uint4& c, uint64_t base, uint64_t s, uint64_t t,
+                                        const float* __restrict__ x, float g[4]) {
+    g[0] = in_row(base + 0, s, t) ? __ldg(x + c.x) : 0.f;
+    g[1] = in_row(base + 1, s, t) ? __ldg(x + c.y) : 0.f;
+    g[2] = in_row(base + 2, s, t) ? __ldg(x + c.z) : 0.f;
+    g[3] = in_row(base + 3, s, t) ? __ldg(x + c.w) : 0.f;
+}
+
+__device__ __forceinline__ float fma4(float acc, const float a[4], const float g[4], uint64_t base,
+                                      uint64_t s, uint64_t t) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (in_row(base + k, s, t)) acc = fmaf(a[k], g[k], acc);
+    return acc;
+}
+
+// Dot product of row [s, t) with x by one lane of an LPR-lane group.
+template <typename V, int LPR>
+__device__ __forceinline__ float lane_dot(const uint32_t* __restrict__ idx, const V* __restrict__ val,
+                                          const float* __restrict__ x, uint64_t s, uint64_t t, int sub) {
+    const uint4* idx4 = reinterpret_cast<const uint4*>(idx);
+    const uint64_t v1 = (t + 3) >> 2;
+    uint64_t v = (s >> 2) + sub;
+    float acc = 0.f;
+    // two vectors in flight per lane before their gathers are consumed
+    for (; v + LPR < v1; v += 2 * LPR) {
+        Vec4<V> p, q;
+        p.load(idx4, val, v);
+        q.load(idx4, val, v + LPR);
+        float gp[4], gq[4];
+        gather4(p.c, v << 2, s, t, x, gp);
+        gather4(q.c, (v + LPR) << 2, s, t, x, gq);
+        acc = fma4(acc, p.a, gp, v << 2, s, t);
+        acc = fma4(acc, q.a, gq, (v + LPR) << 2, s, t);
+    }
+    if (v < v1) {
+        Vec4<V> p;
+        p.load(idx4, val, v);
+        float gp[4];
+        gather4(p.c, v << 2, s, t, x, gp);
+        acc = fma4(acc, p.a, gp, v << 2, s, t);
+    }
+    return acc;
+}
+
+template <int LPR>
+__device__ __forceinline__ float group_sum(float acc) {
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    return acc;
+}
+
+// Epilogues (executed by the group leader only).
+__device__ __forceinline__ void epi_correl(uint32_t r, float sum, const int32_t* __restrict__ g,
+                                           float* __restrict__ ratio, float* __restrict__ fwproj) {
+    // calcCorrel (kernel.cu:17-18): ratio stays 0 where the projection is 0.
+    ratio[r] = (sum != 0.0f) ? __fdiv_rn((float)g[r], sum) : 0.0f;
+    if (fwproj) fwproj[r] = sum;
+}
+
+__device__ __forceinline__ void epi_update(uint32_t c, float sum, float* __restrict__ f,
+                                           const float* __restrict__ norm) {
+    // calcUpdate (kernel.cu:34-37): f * bp / norm, evaluated left to right.
+    const float t = __fmul_rn(f[c], sum);
+    const float n = norm[c];
+    f[c] = (n == 0.0f) ? t : __fdiv_rn(t, n);
+}
+
+template <typename V, int LPR, int EPI>
+__global__ void __launch_bounds__(256)
+k_csrvec(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
+         const V* __restrict__ val, const float* __restrict__ x, uint32_t nrows,
+         const int32_t* __restrict__ g, float* __restrict__ out, float* __restrict__ fwproj,
+         float* __restrict__ f, const float* __restrict__ norm) {
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t row = gt / LPR;
+    const int sub = threadIdx.x & (LPR - 1);
+    float acc = 0.f;
+    if (row < nrows) {
+        const uint64_t s = rowptr[row], t = rowptr[row + 1];
+        acc = lane_dot<V, LPR>(idx, val, x, s, t, sub);
+    }
+    acc = group_sum<LPR>(acc);
+    if (sub == 0 && row < nrows) {
+        if (EPI == (int)Epi::Correl) epi_correl(row, acc, g, out, fwproj);
+        else if (EPI == (int)Epi::Update) epi_update(row, acc, f, norm);
+        else out[row] = acc;
+    }
+}
+
+template <typename V, int LPR>
+__global__ void __launch_bounds__(256)
+k_scatter(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
+          const V* __restrict__ val, const float* __restrict__ ratio, uint32_t nrows,
+          float* __restrict__ bp) {
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t row = gt / LPR;
+    const int sub = threadIdx.x & (LPR - 1);
+    if (row >= nrows) return;
+    const float r = ratio[row];
+    if (r == 0.0f) return;  // adds of val*0 leave bp unchanged
+    const uint64_t s = rowptr[row], t = rowptr[row + 1];
+    const uint4* idx4 = reinterpret_cast<const uint4*>(idx);
+    for (uint64_t v = (s >> 2) + sub; v < ((t + 3) >> 2); v += LPR) {
+        Vec4<V> p;
+        p.load(idx4, val, v);
+        const uint64_t b = v << 2;
+        const uint32_t cs[4] = {p.c.x, p.c.y, p.c.z, p.c.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (in_row(b + k, s, t)) atomicAdd(bp + cs[k], __fmul_rn(p.a[k], r));
+    }
+}
+
+// One warp per row of A: the row's vectors stay in registers between the
+// forward dot product and the scatter (rows longer than 512 elements re-read
+// their tail, which is then L2-resident).
+template <typename V>
+__global__ void __launch_bounds__(256)
+k_fused(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
+        const V* __restrict__ val, const float* __restrict__ x, const int32_t* __restrict__ g,
+        uint32_t nrows, float* __restrict__ bp, float* __restrict__ fwproj) {
+    constexpr int Q = 4;
+    const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= nrows) return;  // whole warp leaves together
+    const uint64_t s = rowptr[row], t = rowptr[row + 1];
+    const uint4* idx4 = reinterpret_cast<const uint4*>(idx);
+    const uint64_t v0 = s >> 2, v1 = (t + 3) >> 2;
+    Vec4<V> keep[Q];
+    float gth[Q][4];
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const uint64_t v = v0 + lane + 32 * q;
+        if (v < v1) {
+            keep[q].load(idx4, val, v);
+            gather4(keep[q].c, v << 2, s, t, x, gth[q]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const uint64_t v = v0 + lane + 32 * q;
+        if (v < v1) acc = fma4(acc, keep[q].a, gth[q], v << 2, s, t);
+    }
+    for (uint64_t v = v0 + lane + 32 * Q; v < v1; v += 32) {
+        Vec4<V> p;
+        p.load(idx4, val, v);
+        float gp[4];
+        gather4(p.c, v << 2, s, t, x, gp);
+        acc = fma4(acc, p.a, gp, v << 2, s, t);
+    }
+    acc = group_sum<32>(acc);
+    if (fwproj && lane == 0) fwproj[row] = acc;
+    if (acc == 0.0f) return;
+    const float r = __fdiv_rn((float)g[row], acc);
+    if (r == 0.0f) return;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const uint64_t v = v0 + lane + 32 * q;
+        if (v < v1) {
+            const uint64_t b = v << 2;
+            const uint32_t cs[4] = {keep[q].c.x, keep[q].c.y, keep[q].c.z, keep[q].c.w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (in_row(b + k, s, t)) atomicAdd(bp + cs[k], __fmul_rn(keep[q].a[k], r));
+        }
+    }
+    for (uint64_t v = v0 + lane + 32 * Q; v < v1; v += 32) {
+        Vec4<V> p;
+        p.load(idx4, val, v);
+        const uint64_t b = v << 2;
+        const uint32_t cs[4] = {p.c.x, p.c.y, p.c.z, p.c.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (in_row(b + k, s, t)) atomicAdd(bp + cs[k], __fmul_rn(p.a[k], r));
+    }
+}
+
+__global__ void k_update_zero(float* __restrict__ f, float* __restrict__ bp,
+                              const float* __restrict__ norm, uint32_t n) {
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const float b = bp[c];
+        bp[c] = 0.0f;
+        const float t = __fmul_rn(f[c], b);
+        const float nn = norm[c];
+        f[c] = (nn == 0.0f) ? t : __fdiv_rn(t, nn);
+    }
+}
+
+__device__ __forceinline__ double block_sum_f64(double v, double* sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double tot = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) tot += sh[i];
+    return tot;
+}
+
+__global__ void __launch_bounds__(256)
+k_loglik_part(const int32_t* __restrict__ g, const float* __restrict__ fp, uint32_t rows,
+              double* __restrict__ part) {
+    __shared__ double sh[8];
+    double acc = 0.0;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        const double p = (double)fp[r];
+        if (p > 0.0) acc += (g[r] > 0 ? (double)g[r] * log(p) : 0.0) - p;
+    }
+    const double tot = block_sum_f64(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_reduce_f64(const double* __restrict__ part, int n,
+                                                     double* __restrict__ out) {
+    __shared__ double sh[32];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += part[i];
+    const double tot = block_sum_f64(v, sh);
+    if (threadIdx.x == 0) *out = tot;
+}
+
+template <typename V, int LPR>
+void csrvec_dispatch_epi(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win,
+                         cudaStream_t s) {
+    const uint64_t threads = (uint64_t)op.nrows * LPR;
+    const dim3 grid(ceil_div_u(threads, 256)), block(256);
+    const V* val = static_cast<const V*>(op.val);
+    switch (e.kind) {
+        case Epi::Correl:
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Correl>, grid, block, 0, s, win, op.rowptr, op.idx,
+                      val, x, op.nrows, e.g, e.out, e.fwproj, (float*)nullptr, (const float*)nullptr);
+            break;
+        case Epi::Update:
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Update>, grid, block, 0, s, win, op.rowptr, op.idx,
+                      val, x, op.nrows, (const int32_t*)nullptr, (float*)nullptr, (float*)nullptr,
+                      e.f, e.norm);
+            break;
+        default:
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Raw>, grid, block, 0, s, win, op.rowptr, op.idx,
+                      val, x, op.nrows, (const int32_t*)nullptr, e.out, (float*)nullptr,
+                      (float*)nullptr, (const float*)nullptr);
+    }
+}
+
+template <typename V>
+void csrvec_dispatch_lanes(const DevCsr& op, const float* x, const EpiArgs& e, int lanes,
+                           L2Window win, cudaStream_t s) {
+    if (lanes >= 32) csrvec_dispatch_epi<V, 32>(op, x, e, win, s);
+    else if (lanes >= 16) csrvec_dispatch_epi<V, 16>(op, x, e, win, s);
+    else if (lanes >= 8) csrvec_dispatch_epi<V, 8>(op, x, e, win, s);
+    else csrvec_dispatch_epi<V, 4>(op, x, e, win, s);
+}
+
+template <typename V>
+void scatter_dispatch(const DevCsr& A, const float* ratio, float* bp, int lanes, L2Window win,
+                      cudaStream_t s) {
+    const V* val = static_cast<const V*>(A.val);
+    auto go = [&](auto kern, int lpr) {
+        const uint64_t threads = (uint64_t)A.nrows * lpr;
+        launch_ex(kern, dim3(ceil_div_u(threads, 256)), dim3(256), 0, s, win, A.rowptr, A.idx, val,
+                  ratio, A.nrows, bp);
+    };
+    if (lanes >= 32) go(k_scatter<V, 32>, 32);
+    else if (lanes >= 16) go(k_scatter<V, 16>, 16);
+    else go(k_scatter<V, 8>, 8);
+}
+
+}  // namespace
+
+int pick_lanes(uint64_t nnz, uint32_t rows) {
+    const double mean = rows ? (double)nnz / rows : 0.0;
+    if (mean >= 96.0) return 32;
+    if (mean >= 40.0) return 16;
+    if (mean >= 12.0) return 8;
+    return 4;
+}
+
+void launch_csrvec(const DevCsr& op, const float* x, const EpiArgs& epi, int lanes, L2Window win,
+                   cudaStream_t s) {
+    if (op.nrows == 0) return;
+    switch (op.vt) {
+        case MLEM_VAL_F32: csrvec_dispatch_lanes<float>(op, x, epi, lanes, win, s); break;
+        case MLEM_VAL_F16: csrvec_dispatch_lanes<__half>(op, x, epi, lanes, win, s); break;
+        default: csrvec_dispatch_lanes<__nv_bfloat16>(op, x, epi, lanes, win, s);
+    }
+}
+
+void launch_scatter(const DevCsr& A, const float* ratio, float* bp, int lanes, L2Window win,
+                    cudaStream_t s) {
+    if (A.nrows == 0) return;
+    switch (A.vt) {
+        case MLEM_VAL_F32: scatter_dispatch<float>(A, ratio, bp, lanes, win, s); break;
+        case MLEM_VAL_F16: scatter_dispatch<__half>(A, ratio, bp, lanes, win, s); break;
+        default: scatter_dispatch<__nv_bfloat16>(A, ratio, bp, lanes, win, s);
+    }
+}
+
+void launch_fused_fp_scatter(const DevCsr& A, const float* x, const int32_t* g, float* bp,
+                             float* fwproj, L2Window win, cudaStream_t s) {
+    if (A.nrows == 0) return;
+    const dim3 grid(ceil_div_u((uint64_t)A.nrows * 32, 256)), block(256);
+    switch (A.vt) {
+        case MLEM_VAL_F32:
+            launch_ex(k_fused<float>, grid, block, 0, s, win, A.rowptr, A.idx,
+                      (const float*)A.val, x, g, A.nrows, bp, fwproj);
+            break;
+        case MLEM_VAL_F16:
+            launch_ex(k_fused<__half>, grid, block, 0, s, win, A.rowptr, A.idx,
+                      (const __half*)A.val, x, g, A.nrows, bp, fwproj);
+            break;
+        default:
+            launch_ex(k_fused<__nv_bfloat16>, grid, block, 0, s, win, A.rowptr, A.idx,
+                      (const __nv_bfloat16*)A.val, x, g, A.nrows, bp, fwproj);
+    }
+}
+
+void launch_update_zero(float* f, float* bp, const float* norm, uint32_t n, cudaStream_t s) {
+    if (n == 0) return;
+    const unsigned grid = std::min<unsigned>(ceil_div_u(n, 256), 152u * 16u);
+    k_update_zero<<<grid, 256, 0, s>>>(f, bp, norm, n);
+    MLEM_LAUNCHED();
+}
+
+void launch_loglik(const int32_t* g, const float* fwproj, uint32_t rows, double* part,
+                   double* out, cudaStream_t s) {
+    k_loglik_part<<<kLoglikParts, 256, 0, s>>>(g, fwproj, rows, part);
+    MLEM_LAUNCHED();
+    k_reduce_f64<<<1, 1024, 0, s>>>(part, kLoglikParts, out);
+    MLEM_LAUNCHED();
+}
+
+}  // namespace mlem

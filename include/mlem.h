@@ -1,0 +1,337 @@
+/*
+ * mlem.h — C ABI of the GB300-native MLEM reconstructor.
+ *
+ * Drop-in for the single-device MLEM loop of wmd0701/Bachelorarbeit-MLEM.
+ * Every entry point returns an mlem_status; mlem_last_error() gives the text
+ * of the last failure on the calling thread.  Host buffers are owned by the
+ * caller and never mutated unless they are documented outputs.  Device memory
+ * is owned by the library through opaque handles.  A handle is used by one
+ * host thread at a time (the server object is internally threaded).
+ *
+ * Reference interfaces replaced (file:line in the reference project):
+ *   - mlem()                       main.cu:19, main.cu:167-514
+ *   - main() argv contract         main.cu:42-62, help() main.cu:614-625
+ *   - csr_format_for_cuda()        main.cu:518-554
+ *   - calcColumnSums()             main.cu:558-580
+ *   - partitionMatrix()            main.cu:593-611
+ *   - sptrans_scanTrans_specialized sptrans.h:397-545
+ *   - merge_based_start()          kernel.cu:190-241 (partition search)
+ *   - Csr4Matrix(path)             helper_files_common/csr4matrix.cpp:36-178
+ *   - Vector<int>(path), writeToFile helper_files_common/vector.hpp:33-87
+ */
+#ifndef MLEM_GB300_H
+#define MLEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef enum {
+    MLEM_OK = 0,
+    MLEM_EINVAL = 1,      /* bad argument (the reference prints help() and exits) */
+    MLEM_EIO = 2,         /* unreadable / malformed file (reference: runtime_error) */
+    MLEM_ENOMEM = 3,      /* device or host allocation failed, or admission refused */
+    MLEM_ECUDA = 4,       /* a CUDA runtime call failed */
+    MLEM_ETIMEOUT = 5,    /* a bounded wait expired (server) */
+    MLEM_EUNSUPPORTED = 6,/* size or mode outside what this build handles */
+    MLEM_EBUSY = 7        /* server queue full / object in use */
+} mlem_status;
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char* mlem_last_error(void);
+/* Library version string. */
+const char* mlem_version(void);
+
+/* --------------------------------------------------------------- switches */
+/* argv[8] of the reference CLI: 0 merge-based SpMV, 1 csr-vector SpMV. */
+typedef enum { MLEM_SPMV_MERGE = 0, MLEM_SPMV_CSR_VECTOR = 1 } mlem_spmv;
+
+/* Storage type of the matrix values on the device (accumulation is FP32). */
+typedef enum { MLEM_VAL_F32 = 0, MLEM_VAL_F16 = 1, MLEM_VAL_BF16 = 2 } mlem_value_type;
+
+/* Back-projection form.  MLEM_BP_TRANS and MLEM_BP_SCATTER are argv[7]=0 and
+ * argv[7]=1 of the reference; MLEM_BP_FUSED is a single pass over A that does
+ * forward projection, correlation and the scatter back projection row by row
+ * (reads the matrix once per iteration; same arithmetic as SCATTER). */
+typedef enum { MLEM_BP_TRANS = 0, MLEM_BP_SCATTER = 1, MLEM_BP_FUSED = 2 } mlem_bp_mode;
+
+/* ------------------------------------------------------------ host CSR */
+/* SoA CSR as produced by csr_format_for_cuda (main.cu:518-554):
+ * rowptr u64[rows+1] with rowptr[0] = 0, col u32[nnz], val f32[nnz]. */
+typedef struct {
+    uint32_t rows;
+    uint32_t cols;
+    uint64_t nnz;
+    const uint64_t* rowptr;
+    const uint32_t* col;
+    const float* val;
+} mlem_csr_host;
+
+/* ------------------------------------------------------------- matrix */
+typedef struct mlem_matrix mlem_matrix;
+
+typedef struct {
+    mlem_value_type value_type; /* device storage of values (F32 = plain method) */
+    uint32_t build_transpose;   /* 1: build Aᵀ on the GPU (stable counting sort) */
+    const float* norm;          /* optional host sensitivity image f32[cols];
+                                   NULL = computed on the GPU as Aᵀ1 in FP64 */
+    int device;                 /* CUDA device ordinal (reference: GPU 0) */
+} mlem_matrix_opts;
+
+/* Fills *o with the defaults: F32 values, transpose built, norm computed, device 0. */
+void mlem_matrix_opts_default(mlem_matrix_opts* o);
+
+/* Uploads A (host CSR), optionally builds Aᵀ and the sensitivity image on the
+ * device.  Replaces the H2D part of mlem() (main.cu:236-299), the host
+ * transpose (main.cu:100-105) and calcColumnSums (main.cu:558-580). */
+mlem_status mlem_matrix_create(const mlem_csr_host* csr, const mlem_matrix_opts* opts,
+                               mlem_matrix** out);
+
+/* Reads a csr4 file (helper_files_common/csr4matrix.cpp:36-178 format) and
+ * creates the device matrix from it. */
+mlem_status mlem_matrix_load_csr4(const char* path, const mlem_matrix_opts* opts,
+                                  mlem_matrix** out);
+
+mlem_status mlem_matrix_destroy(mlem_matrix* m);
+
+typedef struct {
+    uint32_t rows, cols;
+    uint64_t nnz;
+    mlem_value_type value_type;
+    uint32_t has_transpose;
+    uint64_t device_bytes;      /* bytes of device memory held by the handle */
+    uint32_t max_row_nnz, max_col_nnz;
+} mlem_matrix_info;
+
+mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info);
+/* Copies the sensitivity image (f32[cols]) to the host. */
+mlem_status mlem_matrix_get_norm(const mlem_matrix* m, float* norm_out);
+/* Copies the device-built transpose to the host: colptr u64[cols+1],
+ * rowidx u32[nnz], val f32[nnz] (same layout as sptrans_scanTrans_specialized
+ * outputs cscColPtr / cscRowIdx / cscVal, sptrans.h:397-405). */
+mlem_status mlem_matrix_get_transpose(const mlem_matrix* m, uint64_t* colptr,
+                                      uint32_t* rowidx, float* val);
+
+/* ------------------------------------------------------------------ run */
+typedef struct {
+    mlem_spmv spmv;             /* argv[8] */
+    mlem_bp_mode bp_mode;       /* argv[7] (0 trans, 1 scatter) or 2 fused */
+    uint32_t secsize_fp;        /* argv[5]: items per thread, merge FP, 1..512 */
+    uint32_t secsize_bp;        /* argv[6]: items per thread, merge BP, 1..512 */
+    uint32_t use_graph;         /* 1: replay the iteration as a CUDA graph */
+    uint32_t loglik_every;      /* 0: off; k: FP64 log-likelihood every k-th iteration */
+    uint32_t l2_window;         /* 1: keep the image/ratio vector L2-persisting */
+} mlem_run_opts;
+
+/* Defaults: CSR_VECTOR, BP_TRANS, secsize 5/5, graphs on, no log-likelihood, L2 window on. */
+void mlem_run_opts_default(mlem_run_opts* o);
+
+typedef struct {
+    double seconds_total;       /* wall time of the call */
+    double seconds_iterations;  /* device time of the iteration loop (CUDA events) */
+    uint32_t iterations;
+    uint32_t kernel_launches;   /* kernels launched by the iteration loop */
+    uint64_t bytes_h2d, bytes_d2h;
+    double loglik_last;         /* last computed log-likelihood (NaN if none) */
+} mlem_stats;
+
+/* Runs `iterations` MLEM iterations on host buffers: g i32[rows] (sinogram),
+ * f0 f32[cols] (NULL = reference initial value Σg/Σnorm, main.cu:83-97),
+ * f_out f32[cols].  Replaces the loop and teardown of mlem() (main.cu:329-463).
+ * loglik_out: optional f64[iterations] (NaN where not computed). */
+mlem_status mlem_run(mlem_matrix* m, const int32_t* g, const float* f0, uint32_t iterations,
+                     const mlem_run_opts* opts, float* f_out, double* loglik_out,
+                     mlem_stats* stats);
+
+/* Same loop on device buffers already resident in HBM: g_dev i32[rows],
+ * f_dev f32[cols] holds f0 on entry and the image on exit.  Asynchronous on
+ * `stream` (a cudaStream_t, NULL = legacy default stream). */
+mlem_status mlem_run_device(mlem_matrix* m, const int32_t* g_dev, float* f_dev,
+                            uint32_t iterations, const mlem_run_opts* opts, void* stream);
+
+/* Reference initial value: f0 = (float)Σg / Σnorm with Σnorm summed in FP32
+ * in column order (main.cu:83-97). */
+mlem_status mlem_initial_value(const mlem_matrix* m, const int32_t* g, float* init_out);
+
+/* Drop-in with the exact argument list of the reference mlem() (main.cu:19):
+ * host CSR of A (u64 row pointers), optional host CSR of Aᵀ (used when
+ * using_trans == 0; if NULL the transpose is built on the GPU), g, norm,
+ * f (initial image), result_f (output).  device_numbers must be 1.
+ * Unlike the reference, the caller's arrays are never modified. */
+mlem_status mlem_reconstruct(const uint64_t* csr_rows, const uint32_t* csr_cols,
+                             const float* csr_vals, const uint64_t* csr_rows_trans,
+                             const uint32_t* csr_cols_trans, const float* csr_vals_trans,
+                             const int32_t* g, const float* norm, const float* f,
+                             float* result_f, uint32_t rows, uint32_t cols, uint64_t nnzs,
+                             uint32_t iterations, uint32_t device_numbers,
+                             uint32_t matrix_vector_mul, uint32_t secsize_fp,
+                             uint32_t secsize_bp, uint32_t using_trans);
+
+/* ----------------------------------------------------- single operators */
+/* ratio = correl(g, A·f): forward projection with the fused correlation of
+ * calcCorrel (kernel.cu:11-19).  Device pointers, asynchronous on stream.
+ * fwproj_out (optional, f32[rows]) receives A·f before the correlation. */
+mlem_status mlem_forward_project(mlem_matrix* m, const float* f_dev, const int32_t* g_dev,
+                                 float* ratio_dev, float* fwproj_out_dev,
+                                 const mlem_run_opts* opts, void* stream);
+/* bp = Aᵀ·ratio (no update) into bp_dev f32[cols]. */
+mlem_status mlem_back_project(mlem_matrix* m, const float* ratio_dev, float* bp_dev,
+                              const mlem_run_opts* opts, void* stream);
+
+/* Merge-path partition search of merge_based_start (kernel.cu:190-241) for
+ * the thread starts d = t*secsize, t = 0..nthreads-1, over device row
+ * pointers u64[rows+1].  Writes the coordinates (i, j) as int64. */
+mlem_status mlem_merge_path_search(const uint64_t* rowptr_dev, uint32_t rows, uint64_t nnz,
+                                   uint32_t secsize, uint64_t nthreads, int64_t* i_out_dev,
+                                   int64_t* j_out_dev, void* stream);
+
+/* GPU stable counting-sort transpose (CSR -> CSR of Aᵀ), bit-exact with
+ * sptrans_scanTrans_specialized (sptrans.h:397-545).  Host in/out buffers. */
+mlem_status mlem_transpose_host(const mlem_csr_host* csr, uint64_t* colptr, uint32_t* rowidx,
+                                float* val);
+
+/* Column sums Aᵀ1 accumulated in FP64 on the GPU, rounded to f32 (replaces
+ * calcColumnSums, main.cu:558-580).  Host in/out buffers. */
+mlem_status mlem_column_sums_host(const mlem_csr_host* csr, float* norm_out);
+
+/* nnz-balanced row partition of partitionMatrix (main.cu:593-611): segments
+ * u32[nseg+1], seg_rows u32[nseg], seg_nnz u32[nseg], offsets u64[nseg]. */
+mlem_status mlem_partition_rows(const uint64_t* rowptr, uint64_t nnz, uint32_t rows,
+                                uint32_t nseg, uint32_t* segments, uint32_t* seg_rows,
+                                uint32_t* seg_nnz, uint64_t* offsets);
+
+/* ------------------------------------------------------------- file I/O */
+typedef struct {
+    uint32_t rows, cols;
+    uint64_t nnz;
+    uint8_t sym_flags;          /* csr4 header byte 5 (x/y/z symmetry bits) */
+    uint32_t nx, ny, nz;        /* voxel grid from the scanner configuration */
+} mlem_csr4_header;
+
+/* Parses only the header and scanner configuration of a csr4 file. */
+mlem_status mlem_csr4_read_header(const char* path, mlem_csr4_header* hdr);
+/* Reads a whole csr4 file into caller buffers: rowptr u64[rows+1] (with a
+ * leading 0, like csr_format_for_cuda), col u32[nnz], val f32[nnz]. */
+mlem_status mlem_csr4_read(const char* path, uint64_t* rowptr, uint32_t* col, float* val);
+
+/* Scanner description written into a csr4 header. */
+typedef struct {
+    uint32_t n_layers;          /* layers written with {w,h,d,r,mu} below */
+    float crystal_w, crystal_h, crystal_d, radius, mu;
+    uint32_t n_blocks, block_size, n_rings;
+    float block_gap, ring_gap;
+    float voxel_w, voxel_h, voxel_d;
+    uint32_t nx, ny, nz;
+    uint8_t sym_flags;
+} mlem_csr4_scanner;
+
+/* Writes a csr4 file readable by the reference Csr4Matrix. */
+mlem_status mlem_csr4_write(const char* path, const mlem_csr4_scanner* scanner,
+                            const mlem_csr_host* csr);
+/* Raw headerless vectors (vector.hpp:33-87): int32 sinogram in, f32 image out. */
+mlem_status mlem_read_sinogram(const char* path, int32_t* g, uint64_t capacity,
+                               uint64_t* count_out);
+mlem_status mlem_write_image(const char* path, const float* f, uint64_t count);
+
+/* ------------------------------------------------ synthetic system matrix */
+/* Cylindrical ring scanner: n_rings rings of det_per_ring detectors on a
+ * circle of `radius` mm, ring centres at z = (k - (n_rings-1)/2)*ring_pitch;
+ * voxel grid nx*ny*nz of (vx,vy,vz) mm centred on the origin.  Rows are the
+ * unordered detector pairs (a<b) in lexicographic order, columns
+ * x + nx*(y + ny*z), values the exact Siddon ray-voxel intersection lengths
+ * in mm (averaged over the sub-rays of the tube of response), columns
+ * strictly ascending within a row. */
+typedef struct {
+    uint32_t det_per_ring, n_rings;
+    float radius, ring_pitch;
+    uint32_t nx, ny, nz;
+    float vx, vy, vz;
+    uint32_t row_stride;        /* 0 or 1: all rows; k > 1: keep rows r with r % k == row_phase */
+    uint32_t row_phase;
+    /* Tube of response: sub_t x sub_z parallel sub-rays per LOR spread over
+     * width_t (tangential) x width_z (axial) mm of the crystal faces; the
+     * element value is the mean intersection length over the sub-rays.
+     * 0 or 1 sub-rays = the single line between the crystal centres. */
+    uint32_t sub_t, sub_z;
+    float width_t, width_z;
+} mlem_geometry;
+
+/* Number of rows (kept LORs) of the geometry; 0 for an invalid geometry. */
+uint64_t mlem_siddon_rows(const mlem_geometry* geo);
+/* Row pointers u64[rows+1] of the geometry's matrix (host, OpenMP). */
+mlem_status mlem_siddon_count_host(const mlem_geometry* geo, uint64_t* rowptr_out);
+/* Fills col/val for rows with the given rowptr (host, OpenMP). */
+mlem_status mlem_siddon_fill_host(const mlem_geometry* geo, const uint64_t* rowptr,
+                                  uint32_t* col, float* val);
+/* Same generator on the GPU: the matrix is built in HBM and never leaves it.
+ * Bit-identical to the host generator (no FMA contraction, same operation order). */
+mlem_status mlem_matrix_generate(const mlem_geometry* geo, const mlem_matrix_opts* opts,
+                                 mlem_matrix** out);
+/* Copies the device matrix A to host buffers (f32 values converted back). */
+mlem_status mlem_matrix_get_csr(const mlem_matrix* m, uint64_t* rowptr, uint32_t* col,
+                                float* val);
+
+/* ------------------------------------------------------------- batched */
+/* Reconstructs `count` sinograms against one resident matrix as a batched
+ * SpMM (forward and back projection shared by up to 32 instances per tile),
+ * replayed as CUDA graphs.  g: i32[count][rows]; iterations: u32[count]
+ * (uneven counts allowed); f0: NULL (reference initial value per instance) or
+ * f32[count][cols]; f_out: f32[count][cols].  Results of an instance do not
+ * depend on which other instances share its batch. */
+typedef struct {
+    uint32_t tile;              /* instances per batch tile: 0 = autotune, else 8/16/32 */
+    uint32_t use_graph;
+    uint32_t order_by_iterations; /* 1: group instances of similar length */
+} mlem_batch_opts;
+
+void mlem_batch_opts_default(mlem_batch_opts* o);
+mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g,
+                           const uint32_t* iterations, const float* f0,
+                           const mlem_batch_opts* opts, float* f_out, mlem_stats* stats);
+
+/* -------------------------------------------------------------- serving */
+typedef struct mlem_server mlem_server;
+
+typedef struct {
+    uint32_t slots_per_matrix;  /* concurrent reconstructions per matrix (batch tile) */
+    uint64_t hbm_budget_bytes;  /* admission limit for per-request state (0 = free HBM - reserve) */
+    uint64_t hbm_reserve_bytes; /* HBM kept free when hbm_budget_bytes == 0 */
+    uint32_t queue_capacity;    /* max queued requests before submit returns EBUSY */
+} mlem_server_opts;
+
+void mlem_server_opts_default(mlem_server_opts* o);
+mlem_status mlem_server_create(const mlem_server_opts* opts, mlem_server** out);
+/* Registers a resident matrix; returns its index in *matrix_id.  The server
+ * does not take ownership: destroy the matrix after the server. */
+mlem_status mlem_server_add_matrix(mlem_server* s, mlem_matrix* m, uint32_t* matrix_id);
+/* Queues a reconstruction; g (i32[rows]) is copied at submit time.
+ * *request_id identifies it for mlem_server_wait. */
+mlem_status mlem_server_submit(mlem_server* s, uint32_t matrix_id, const int32_t* g,
+                               uint32_t iterations, uint64_t* request_id);
+/* Waits up to timeout_ms for a request; copies its image to f_out
+ * (f32[cols]) and its submit->done latency in seconds. */
+mlem_status mlem_server_wait(mlem_server* s, uint64_t request_id, float* f_out,
+                             uint32_t timeout_ms, double* latency_s);
+/* Cancels a queued request (MLEM_EINVAL if unknown or already running). */
+mlem_status mlem_server_cancel(mlem_server* s, uint64_t request_id);
+typedef struct {
+    uint64_t submitted, completed, cancelled, rejected;
+    uint64_t active, queued;
+    uint64_t hbm_in_use;
+    uint64_t iterations_done;
+} mlem_server_stats;
+mlem_status mlem_server_get_stats(mlem_server* s, mlem_server_stats* st);
+mlem_status mlem_server_destroy(mlem_server* s);
+
+/* ---------------------------------------------------------- diagnostics */
+/* Number of kernels this library launched since load (all entry points). */
+uint64_t mlem_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MLEM_GB300_H */
