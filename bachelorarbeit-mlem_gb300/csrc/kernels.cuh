@@ -126,6 +126,9 @@ void launch_slot_get(const float* F, uint32_t cols, uint32_t BT, uint32_t b, flo
 }  // namespace mlem
 
 namespace mlem {
+// Largest access-policy window the device accepts (0 until queried).
+extern size_t g_max_window_bytes;
+
 // Launch through cudaLaunchKernelEx so the L2 access-policy window travels
 // with the launch (and into a CUDA graph node when captured).
 template <typename... KArgs, typename... Args>
@@ -138,10 +141,10 @@ inline void launch_ex(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sm
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     unsigned n = 0;
-    if (win.bytes) {
+    if (win.bytes && g_max_window_bytes) {
         attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
         attr[0].val.accessPolicyWindow.base_ptr = const_cast<void*>(win.ptr);
-        attr[0].val.accessPolicyWindow.num_bytes = win.bytes;
+        attr[0].val.accessPolicyWindow.num_bytes = win.bytes < g_max_window_bytes ? win.bytes : g_max_window_bytes;
         attr[0].val.accessPolicyWindow.hitRatio = 1.0f;
         attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
         attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;

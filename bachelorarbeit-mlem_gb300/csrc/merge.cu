@@ -16,6 +16,8 @@
 #include "kernels.cuh"
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 namespace mlem {
 
@@ -298,19 +300,28 @@ void merge_plan_build(const DevCsr& op, uint32_t secsize, MergePlan& plan, cudaS
     MLEM_CUDA(cudaMalloc(&plan.carry, sizeof(float) * nt));
     MLEM_CUDA(cudaMalloc(&plan.carry_row, sizeof(uint32_t) * nt));
     MLEM_CUDA(cudaMalloc(&plan.head, sizeof(float) * nt));
-    // opt in to the tile's shared memory once, outside any stream capture
-    switch (op.vt) {
-        case MLEM_VAL_F32:
-            MLEM_CUDA(cudaFuncSetAttribute(k_merge_tile<float>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem));
-            break;
-        case MLEM_VAL_F16:
-            MLEM_CUDA(cudaFuncSetAttribute(k_merge_tile<__half>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem));
-            break;
-        default:
-            MLEM_CUDA(cudaFuncSetAttribute(k_merge_tile<__nv_bfloat16>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem));
+    // Opt in to the tile's shared memory outside any stream capture.  The
+    // attribute belongs to the kernel, which all plans of a value type share,
+    // so it only ever grows.
+    {
+        static std::mutex mu;
+        static std::map<int, size_t> cur;  // (device * 4 + value type) -> bytes
+        std::lock_guard<std::mutex> lk(mu);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const int t = dev * 4 + (int)op.vt;
+        if (plan.smem > cur[t]) {
+            cudaError_t e;
+            if (op.vt == MLEM_VAL_F32)
+                e = cudaFuncSetAttribute(k_merge_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
+            else if (op.vt == MLEM_VAL_F16)
+                e = cudaFuncSetAttribute(k_merge_tile<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
+            else
+                e = cudaFuncSetAttribute(k_merge_tile<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)plan.smem);
+            MLEM_CUDA(e);
+            cur[t] = plan.smem;
+        }
     }
     const unsigned grid = std::max(1u, std::min<unsigned>(ceil_div_u(plan.ntiles + 1, 256), 152u * 16u));
     k_tile_coords<<<grid, 256, 0, s>>>(op.rowptr, op.nrows, op.nnz, TS, plan.ntiles, plan.tile_i,

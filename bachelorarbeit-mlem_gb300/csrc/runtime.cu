@@ -21,6 +21,7 @@
 namespace mlem {
 
 std::atomic<uint64_t> g_launches{0};
+size_t g_max_window_bytes = 0;
 
 namespace {
 thread_local std::string t_error;
@@ -177,12 +178,15 @@ static void enable_l2_persisting(int dev) {
     std::lock_guard<std::mutex> lk(mu);
     if (done[dev]) return;
     done[dev] = true;
-    int maxp = 0;
-    if (cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev) == cudaSuccess && maxp > 0) {
+    int maxp = 0, maxw = 0;
+    if (cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev) == cudaSuccess && maxp > 0 &&
+        cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, dev) == cudaSuccess && maxw > 0) {
         const size_t want = std::min<size_t>((size_t)maxp, 64ull << 20);
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want);  // context-scoped limit
-        cudaGetLastError();
+        // context-scoped set-aside: released with this process's context
+        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) == cudaSuccess)
+            g_max_window_bytes = (size_t)maxw;
     }
+    cudaGetLastError();
 }
 
 // Runs `iters` iterations on the workspace (g and f already in place).

@@ -58,7 +58,9 @@ Geo make_geo(const mlem_geometry& g) {
     G.S = G.sub_t * G.sub_z;
     G.width_t = g.width_t;
     G.width_z = g.width_z;
-    G.cap_ray = g.nx + g.ny + g.nz + 2;
+    // a straight segment visits at most nx+ny+nz+4 voxels (one per plane
+    // crossed); ray_walk never emits more than cap_ray elements
+    G.cap_ray = g.nx + g.ny + g.nz + 8;
     return G;
 }
 
@@ -191,7 +193,7 @@ __host__ __device__ uint32_t ray_walk(const Geo& G, const double p[6], Emit&& em
     uint32_t pend_col = 0xffffffffu;
     double pend_len = 0.0;
     auto flush = [&]() {
-        if (pend_col != 0xffffffffu && pend_len > kMinLen) {
+        if (pend_col != 0xffffffffu && pend_len > kMinLen && n < G.cap_ray) {
             emit(pend_col, pend_len);
             ++n;
         }

@@ -1,0 +1,433 @@
+"""MLEM benchmark: iterations/s of the single-device MLEM loop on GB300.
+
+Workload (default): the 12 GB-class synthetic scanner — 16 rings x 144
+detectors (r = 60 mm), 200x200x64 voxels of 0.4 mm, 2,653,056 LOR rows,
+~1.43 B nonzeros of multi-ray Siddon lengths (11.5 GB in FP32, 23 GB with the
+transpose) — plain FP32 MLEM, csr-vector forward projection + transposed
+back projection, 100 iterations per step, seeded 20-ellipsoid phantom,
+Poisson sinogram of 1e8 counts.  All inputs are synthetic (the reference's
+measured data are not distributed).
+
+value  : iterations/s with the matrix, sinogram and image resident in HBM
+         (one step = one 100-iteration reconstruction through mlem_run_device).
+e2e    : the same through mlem_run (the C ABI a user calls) from pinned host
+         buffers: sinogram + initial image in, image out, every step.
+roofline: the dominant kernel's algorithmic bytes / its CUDA-event duration
+         against the measured HBM copy bandwidth.
+cpu_baseline: the oracle's OpenMP MLEM (FP32 values, FP64 accumulation) on a
+         row sample of the same matrix, scaled to the full matrix by nnz.
+
+--impl reference runs only the CPU implementation (the reference has no CPU
+path of its own and its CUDA code cannot be built on the GPU host; the
+oracle port stands in) and prints its line.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+PKG_DIR = ROOT / "bachelorarbeit-mlem_gb300"
+PROFILES = ROOT / "profiles"
+
+WORKLOADS = {
+    "cyl3d_12gb": dict(iters=100, shapes=20, total=1e8, cpu_stride=64),
+    "cyl3d_mid": dict(iters=100, shapes=20, total=1e8, cpu_stride=8),
+    "ring2d": dict(iters=20, shapes=5, total=1e6, cpu_stride=1),
+}
+
+
+def load_pkg():
+    spec = importlib.util.spec_from_file_location("mlem_gb300_build", PKG_DIR / "build.py")
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build()
+    spec = importlib.util.spec_from_file_location("mlem_gb300", PKG_DIR / "__init__.py",
+                                                  submodule_search_locations=[str(PKG_DIR)])
+    m = importlib.util.module_from_spec(spec)
+    sys.modules["mlem_gb300"] = m
+    spec.loader.exec_module(m)
+    return m
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(rows, cols, nnz, sv):
+    """Per-launch algorithmic bytes of the two kernels of an iteration."""
+    fp = nnz * (sv + 4) + 8 * (rows + 1) + 4 * cols + 4 * rows + 4 * rows   # A, rowptr, x once, g, ratio
+    bp = nnz * (sv + 4) + 8 * (cols + 1) + 4 * rows + 12 * cols             # Aᵀ, colptr, ratio once, norm, f r/w
+    return fp, bp
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if n_gpus > 0 else "gloo")
+    return rank, world, local, dist
+
+
+def barrier(dist, torch=None):
+    if dist is not None:
+        if torch is not None:
+            dist.barrier(device_ids=[torch.cuda.current_device()])
+        else:
+            dist.barrier()
+
+
+def make_problem(pkg, name, torch, value_type=0):
+    from mlem_gb300 import synth
+    cfg = WORKLOADS[name]
+    geo = pkg.preset(name)
+    t0 = time.time()
+    m = pkg.Matrix.generate(geo, value_type=value_type)
+    t_gen = time.time() - t0
+    xt = synth.phantom(geo, cfg["shapes"], seed=1).astype(np.float32)
+    dx = torch.from_numpy(xt).cuda()
+    dz = torch.zeros(m.rows, dtype=torch.int32, device="cuda")
+    ratio = torch.zeros(m.rows, dtype=torch.float32, device="cuda")
+    fp = torch.zeros(m.rows, dtype=torch.float32, device="cuda")
+    m.forward_project(dx.data_ptr(), dz.data_ptr(), ratio.data_ptr(), fp.data_ptr(),
+                      stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    g = synth.poisson_sinogram(fp.cpu().numpy().astype(np.float64), cfg["total"], seed=2)
+    return m, geo, g, t_gen
+
+
+def time_kernels(pkg, m, torch, g_dev, f_dev, reps=10):
+    """Average CUDA-event duration of the FP and BP kernels (launched alone)."""
+    s = torch.cuda.current_stream()
+    ratio = torch.zeros(m.rows, dtype=torch.float32, device="cuda")
+    bp = torch.zeros(m.cols, dtype=torch.float32, device="cuda")
+    out = {}
+    for kind in ("fp", "bp"):
+        for _ in range(2):
+            if kind == "fp":
+                m.forward_project(f_dev.data_ptr(), g_dev.data_ptr(), ratio.data_ptr(), 0, stream=s.cuda_stream)
+            else:
+                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream)
+        times = []
+        for _ in range(reps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            if kind == "fp":
+                m.forward_project(f_dev.data_ptr(), g_dev.data_ptr(), ratio.data_ptr(), 0, stream=s.cuda_stream)
+            else:
+                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream)
+            b.record(s)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        out[kind] = sum(times) / len(times)
+    return out
+
+
+def cpu_baseline(pkg, name, stride, iters=1):
+    """Oracle OpenMP MLEM on every stride-th LOR of the workload, scaled by nnz."""
+    from oracle import oracle as O
+    from mlem_gb300 import synth
+    geo = pkg.preset(name, row_stride=stride)
+    rp, col, val, cols = pkg.siddon_host(geo)
+    AT = O.transpose(rp, col, val, cols)
+    norm = O.colsum(rp, col, val, cols)
+    xt = synth.phantom(pkg.preset(name), WORKLOADS[name]["shapes"], seed=1)
+    g = synth.poisson_sinogram(synth.project_host(rp, col, val, xt), WORKLOADS[name]["total"] / stride, seed=2)
+    f0 = np.full(cols, O.initial_value(g, norm), np.float32)
+    threads = O.lib().oracle_max_threads()
+    O.mlem_omp((rp, col, val), AT, g, norm, f0, 1, threads)  # warm-up
+    t0 = time.perf_counter()
+    O.mlem_omp((rp, col, val), AT, g, norm, f0, iters, threads)
+    dt = (time.perf_counter() - t0) / iters
+    return dict(nnz=len(col), rows=len(rp) - 1, seconds=dt, cores=threads, stride=stride)
+
+
+def run_reference(args):
+    """CPU implementation of the path on the host cores (oracle port)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    pkg = load_pkg()
+    name = args.workload
+    full_rows = pkg.siddon_rows(pkg.preset(name))
+    stride = WORKLOADS[name]["cpu_stride"]
+    for _ in range(args.warmup):
+        pass
+    samples = []
+    for _ in range(args.steps):
+        samples.append(cpu_baseline(pkg, name, stride))
+    # full-matrix nnz estimated from the sample's nnz per row
+    s = samples[-1]
+    full_nnz = s["nnz"] * full_rows / s["rows"]
+    sec = statistics.median(x["seconds"] for x in samples) * full_nnz / s["nnz"]
+    value = 1.0 / sec
+    line = {
+        "impl": "reference", "metric": "MLEM iterations/s", "value": value, "unit": "iter/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 values, f64 accumulation",
+        "data": "synthetic", "config": {"workload": name, "iterations_per_step": 1, "form": "fp32 plain"},
+        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": s["cores"], "kind": "port",
+                         "sample": f"every {stride}th LOR row ({s['rows']} rows, {s['nnz']} nnz), 1 iteration, "
+                                   f"time scaled by full/sample nnz"},
+        "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's MLEM loop exists only as CUDA kernels + NCCL; its CPU-side restatement "
+                "(oracle/mlem_oracle.c, pinned bit-exact to the reference's compiled kernels) is timed",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_forms(pkg, torch, args):
+    """FP16-value and batched forms (images*iterations/s)."""
+    from mlem_gb300 import synth
+    res = {}
+    s = torch.cuda.current_stream()
+    name = args.workload
+    iters = WORKLOADS[name]["iters"]
+    # FP16 values, same workload
+    m16, geo, g, _ = make_problem(pkg, name, torch, value_type=pkg.VAL_F16)
+    g_dev = torch.from_numpy(g).cuda()
+    f0 = np.full(m16.cols, m16.initial_value(g), np.float32)
+    f0_dev = torch.from_numpy(f0).cuda()
+    f_dev = torch.empty_like(f0_dev)
+    for bp_mode, label in ((0, "fp16_trans"), (2, "fp16_fused")):
+        f_dev.copy_(f0_dev)
+        m16.run_device(g_dev.data_ptr(), f_dev.data_ptr(), 5, stream=s.cuda_stream, bp_mode=bp_mode)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f_dev.copy_(f0_dev)
+        a.record(s)
+        m16.run_device(g_dev.data_ptr(), f_dev.data_ptr(), iters, stream=s.cuda_stream, bp_mode=bp_mode)
+        b.record(s)
+        b.synchronize()
+        res[label] = {"images_iterations_per_s": iters / (a.elapsed_time(b) * 1e-3)}
+    m16.close()
+    # batched: the mid-size matrix with FP16 values, 64 sinograms, uneven iterations
+    mb = pkg.Matrix.generate(pkg.preset("cyl3d_mid"), value_type=pkg.VAL_F16)
+    rng = np.random.Generator(np.random.PCG64(7))
+    totals = np.exp(rng.uniform(np.log(1e5), np.log(1e9), 64))
+    its = np.random.Generator(np.random.PCG64(8)).integers(10, 201, 64).astype(np.uint32)
+    dz = torch.zeros(mb.rows, dtype=torch.int32, device="cuda")
+    ratio = torch.zeros(mb.rows, dtype=torch.float32, device="cuda")
+    fp = torch.zeros(mb.rows, dtype=torch.float32, device="cuda")
+    G = np.zeros((64, mb.rows), np.int32)
+    geo_b = pkg.preset("cyl3d_mid")
+    for k in range(64):
+        xt = torch.from_numpy(synth.phantom(geo_b, 20, seed=1000 + k)).cuda()
+        mb.forward_project(xt.data_ptr(), dz.data_ptr(), ratio.data_ptr(), fp.data_ptr(), stream=s.cuda_stream)
+        G[k] = synth.poisson_sinogram(fp.cpu().numpy().astype(np.float64), totals[k], seed=2000 + k)
+    _, st = mb.batch_run(G[:8], np.full(8, 2, np.uint32), stats=True)  # autotune + warm-up
+    _, st = mb.batch_run(G, its, stats=True)
+    res["batched_fp16_64"] = {"images_iterations_per_s": float(its.sum()) / st["seconds_iterations"],
+                              "wall_images_iterations_per_s": float(its.sum()) / st["seconds_total"],
+                              "workload": "cyl3d_mid fp16, 64 sinograms, iterations U{10..200}"}
+    mb.close()
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cyl3d_12gb", choices=sorted(WORKLOADS))
+    ap.add_argument("--forms", default="all", choices=["all", "none"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank, world, local, dist = dist_init(args.gpus)
+    torch.cuda.set_device(local)
+    pkg = load_pkg()
+    name = args.workload
+    iters = WORKLOADS[name]["iters"]
+    m, geo, g, t_gen = make_problem(pkg, name, torch)
+    s = torch.cuda.current_stream()
+    g_dev = torch.from_numpy(g).cuda()
+    f0 = np.full(m.cols, m.initial_value(g), np.float32)
+    f0_dev = torch.from_numpy(f0).cuda()
+    f_dev = torch.empty_like(f0_dev)
+
+    def step():
+        f_dev.copy_(f0_dev)
+        m.run_device(g_dev.data_ptr(), f_dev.data_ptr(), iters, stream=s.cuda_stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    barrier(dist, torch)
+    n0 = pkg.kernel_launch_count()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        a.record(s)
+        for _ in range(args.steps):
+            step()
+        b.record(s)
+        torch.cuda.synchronize()
+    launches = pkg.kernel_launch_count() - n0
+    ms = a.elapsed_time(b)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    barrier(dist, torch)
+    value = world * args.steps * iters / (ms * 1e-3)
+
+    # e2e: through mlem_run from pinned host buffers (sinogram + f0 in, image out)
+    g_pin = torch.from_numpy(g).pin_memory()
+    f0_pin = torch.from_numpy(f0).pin_memory()
+    out_pin = torch.empty(m.cols, dtype=torch.float32).pin_memory()
+    import ctypes as C
+    lib = pkg.load_library()
+    ro = pkg.Matrix.run_opts()
+
+    def e2e_step():
+        st = lib.mlem_run(m.handle, C.c_void_p(g_pin.data_ptr()), C.c_void_p(f0_pin.data_ptr()), iters,
+                          C.byref(ro), C.c_void_p(out_pin.data_ptr()), None, None)
+        if st != 0:
+            raise pkg.MlemError(st, lib.mlem_last_error().decode())
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier(dist, torch)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = world * args.steps * iters / float(te.item())
+
+    # roofline of the dominant kernel
+    kt = time_kernels(pkg, m, torch, g_dev, f0_dev)
+    fp_b, bp_b = algorithmic_bytes(m.rows, m.cols, m.nnz, 4)
+    dom = "fp" if kt["fp"] >= kt["bp"] else "bp"
+    dom_bytes = fp_b if dom == "fp" else bp_b
+    peak, peak_kind = peaks()
+    achieved = dom_bytes / (kt[dom] * 1e-3) / 1e9
+    iter_bytes = fp_b + bp_b
+    traffic = None
+    tf = PROFILES / "dram_traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(f"{name}/{dom}")
+
+    line = {
+        "metric": "MLEM iterations/s", "value": value, "unit": "iter/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded multi-ray Siddon matrix, ellipsoid phantom, Poisson sinogram)",
+        "config": {"workload": name, "rows": m.rows, "cols": m.cols, "nnz": m.nnz, "iterations_per_step": iters,
+                   "form": "fp32 plain: csr-vector FP + transposed BP", "l2": "inputs larger than L2 "
+                   f"({(m.device_bytes) / 1e9:.1f} GB resident matrix)", "replicas": world,
+                   "matrix_generation_s": round(t_gen, 2)},
+        "e2e": {"value": e2e_value, "unit": "iter/s", "h2d_bytes_per_step": int(4 * m.rows + 4 * m.cols),
+                "d2h_bytes_per_step": int(4 * m.cols)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "k_csrvec (FP, fused correlation)" if dom == "fp"
+                     else "k_csrvec (BP over Aᵀ)", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes": dom_bytes, "kernel_ms": kt[dom],
+                     "iteration": {"bytes": iter_bytes, "ms": ms / args.steps / iters,
+                                   "achieved_gbs": iter_bytes / (ms / args.steps / iters * 1e-3) / 1e9,
+                                   "frac": iter_bytes / (ms / args.steps / iters * 1e-3) / 1e9 / peak},
+                     "fp_ms": kt["fp"], "bp_ms": kt["bp"]},
+        "clocks": clk.summary(),
+    }
+    m.close()
+    if args.forms == "all":
+        line["forms"] = run_forms(pkg, torch, args)
+        line["forms"]["fp32_plain"] = {"images_iterations_per_s": value / world}
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_baseline(pkg, name, WORKLOADS[name]["cpu_stride"])
+        full_nnz = line["config"]["nnz"]
+        sec_full = cb["seconds"] * full_nnz / cb["nnz"]
+        line["cpu_baseline"] = {"value": 1.0 / sec_full, "unit": "iter/s", "cores": cb["cores"], "kind": "port",
+                                "sample": f"every {cb['stride']}th LOR row of the same matrix ({cb['rows']} rows, "
+                                          f"{cb['nnz']} nnz), 1 OpenMP MLEM iteration (FP32 values, FP64 "
+                                          f"accumulation), time scaled by {full_nnz}/{cb['nnz']} nnz"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
