@@ -130,6 +130,8 @@ _SIGS = {
     "mlem_forward_project": (C.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "mlem_back_project": (C.c_int, [_P, _P, _P, _P, _P]),
     "mlem_merge_path_search": (C.c_int, [_P, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint64, _P, _P, _P]),
+    "mlem_forward_project_merge_noalloc": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint64, _P, _P, _P,
+                                                     C.c_uint32, _P]),
     "mlem_transpose_host": (C.c_int, [_P, _P, _P, _P]),
     "mlem_column_sums_host": (C.c_int, [_P, _P]),
     "mlem_partition_rows": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, _P, _P, _P, _P]),

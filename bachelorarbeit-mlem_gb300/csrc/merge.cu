@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <string>
 
 namespace mlem {
 
@@ -341,3 +342,116 @@ void launch_merge_spmv(const DevCsr& op, const MergePlan& plan, const float* x, 
 }
 
 }  // namespace mlem
+
+// ---------------------------------------------------------------------------
+// Forward projection that allocates nothing.
+//
+// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is
+// being captured into a long-lived pool they do not own, host applications
+// whose device memory is handed out once at start-up by their own pool
+// (real-time reconstruction services, plugins inside a framework that
+// accounts for every byte), and callers that must not trigger the implicit
+// synchronisation an allocation can cause.  For them the merge-path forward
+// projection keeps its per-tile scratch (tile coordinates, carries, heads) in
+// one file-scope device array of fixed size instead of allocating it.
+//
+// The array belongs to the library image: every GPU that loads the library
+// holds kNoAllocScratchBytes of it until the process exits.  All calls share
+// it, so calls whose kernels overlap on the GPU race on it; serialise them
+// (one stream, or events).  Nothing in it has to start at zero: every word a
+// call reads was written earlier in the same call.
+namespace mlem {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 4u << 20;  // 4 MiB per device
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of the array, looked up once per device with that device
+// current (in host code the symbol itself is only a host-side stand-in).
+unsigned char* noalloc_scratch_address() {
+    static std::mutex mu;
+    static std::map<int, unsigned char*> addr;
+    int dev = -1;
+    MLEM_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = addr.find(dev);
+    if (it != addr.end()) return it->second;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    MLEM_REQUIRE(e == cudaSuccess && p != nullptr, MLEM_ECUDA,
+                 std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    addr[dev] = static_cast<unsigned char*>(p);
+    return addr[dev];
+}
+
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+}  // namespace mlem
+
+extern "C" mlem_status mlem_forward_project_merge_noalloc(const uint64_t* rowptr_dev, const uint32_t* col_dev,
+                                                          const float* val_dev, uint32_t rows, uint32_t cols,
+                                                          uint64_t nnz, const float* x_dev, const int32_t* g_dev,
+                                                          float* ratio_dev, uint32_t secsize, void* stream) {
+    using namespace mlem;
+    try {
+        MLEM_REQUIRE(rowptr_dev && x_dev && g_dev && ratio_dev && (nnz == 0 || (col_dev && val_dev)), MLEM_EINVAL,
+                     "NULL argument");
+        MLEM_REQUIRE(rows >= 1 && cols >= 1, MLEM_EINVAL, "matrix must have rows and columns");
+        MLEM_REQUIRE(secsize >= 1 && secsize <= 125, MLEM_EINVAL,
+                     "allocation-free merge path: secsize must be in 1..125");
+        // tile of T threads * secsize items, sized so the tile's shared memory
+        // stays within the default 48 KB (no opt-in call needed)
+        uint32_t T = 4000 / secsize;
+        T = std::max(32u, std::min(256u, T & ~31u));
+        const uint64_t TS = (uint64_t)T * secsize;
+        const uint64_t items = (uint64_t)rows + nnz;
+        const uint64_t ntiles = (items + TS - 1) / TS;
+        const size_t need = align256(sizeof(uint32_t) * (ntiles + 1)) + align256(sizeof(uint64_t) * (ntiles + 1)) +
+                            3 * align256(sizeof(float) * ntiles);
+        MLEM_REQUIRE(need <= kNoAllocScratchBytes, MLEM_EINVAL,
+                     "allocation-free merge path: rows + nnz = " + std::to_string(items) + " needs " +
+                         std::to_string(need) + " bytes of scratch, the fixed maximum is " +
+                         std::to_string(kNoAllocScratchBytes) + " (use mlem_forward_project)");
+        unsigned char* base = noalloc_scratch_address();
+        MergePlan p;  // views into the static array; never released
+        p.secsize = secsize;
+        p.threads = T;
+        p.ntiles = ntiles;
+        p.smem = sizeof(uint32_t) * (TS + 4) + 2 * sizeof(float) * TS;
+        size_t off = 0;
+        p.tile_i = reinterpret_cast<uint32_t*>(base + off);
+        off += align256(sizeof(uint32_t) * (ntiles + 1));
+        p.tile_j = reinterpret_cast<uint64_t*>(base + off);
+        off += align256(sizeof(uint64_t) * (ntiles + 1));
+        p.carry = reinterpret_cast<float*>(base + off);
+        off += align256(sizeof(float) * ntiles);
+        p.carry_row = reinterpret_cast<uint32_t*>(base + off);
+        off += align256(sizeof(float) * ntiles);
+        p.head = reinterpret_cast<float*>(base + off);
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        const unsigned grid = std::max(1u, std::min<unsigned>(ceil_div_u(ntiles + 1, 256), 152u * 16u));
+        k_tile_coords<<<grid, 256, 0, s>>>(rowptr_dev, rows, nnz, TS, ntiles, p.tile_i, p.tile_j);
+        MLEM_LAUNCHED();
+        DevCsr A;
+        A.nrows = rows;
+        A.ncols = cols;
+        A.nnz = nnz;
+        A.rowptr = const_cast<uint64_t*>(rowptr_dev);
+        A.idx = const_cast<uint32_t*>(col_dev);
+        A.val = const_cast<float*>(val_dev);
+        A.vt = MLEM_VAL_F32;
+        EpiArgs e;
+        e.kind = Epi::Correl;
+        e.g = g_dev;
+        e.out = ratio_dev;
+        launch_merge_spmv(A, p, x_dev, e, L2Window{}, s);
+        return MLEM_OK;
+    } catch (const Error& err) {
+        set_error(err.msg);
+        return err.code;
+    } catch (const std::exception& err) {
+        set_error(err.what());
+        return MLEM_EINVAL;
+    }
+}

@@ -189,6 +189,24 @@ mlem_status mlem_merge_path_search(const uint64_t* rowptr_dev, uint32_t rows, ui
                                    uint32_t secsize, uint64_t nthreads, int64_t* i_out_dev,
                                    int64_t* j_out_dev, void* stream);
 
+/* Merge-path forward projection with the fused correlation, like
+ * mlem_forward_project with MLEM_SPMV_MERGE, for callers that must not
+ * allocate device memory (an allocation during graph capture or inside a
+ * host-owned memory pool is not possible for them).  No counterpart in the
+ * reference.  It allocates nothing: its per-tile scratch is a fixed 4 MiB
+ * device array inside the library, held by every GPU that loads the library
+ * until exit, which limits rows + nnz to about 220 million at secsize 5
+ * (larger inputs return MLEM_EINVAL with the limit in the message).  The
+ * first call on a device looks the array up (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race, so serialise them.  Device pointers in, ratio
+ * f32[rows] out; requires col[e] < cols; secsize 1..125; asynchronous on
+ * `stream`. */
+mlem_status mlem_forward_project_merge_noalloc(const uint64_t* rowptr_dev, const uint32_t* col_dev,
+                                               const float* val_dev, uint32_t rows, uint32_t cols,
+                                               uint64_t nnz, const float* x_dev, const int32_t* g_dev,
+                                               float* ratio_dev, uint32_t secsize, void* stream);
+
 /* GPU stable counting-sort transpose (CSR -> CSR of Aᵀ), bit-exact with
  * sptrans_scanTrans_specialized (sptrans.h:397-545).  Host in/out buffers. */
 mlem_status mlem_transpose_host(const mlem_csr_host* csr, uint64_t* colptr, uint32_t* rowidx,
