@@ -25,6 +25,7 @@ LIB_PATH = PKG / "lib" / "libmlem_gb300.so"
 CLI_PATH = PKG / "bin" / "mlem_gb300"
 
 SPMV_MERGE, SPMV_CSR_VECTOR = 0, 1
+KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO = 0, 1, 2, 3
 VAL_F32, VAL_F16, VAL_BF16 = 0, 1, 2
 BP_TRANS, BP_SCATTER, BP_FUSED = 0, 1, 2
 
@@ -59,7 +60,7 @@ class MatrixInfo(C.Structure):
 class RunOpts(C.Structure):
     _fields_ = [("spmv", C.c_int), ("bp_mode", C.c_int), ("secsize_fp", C.c_uint32),
                 ("secsize_bp", C.c_uint32), ("use_graph", C.c_uint32), ("loglik_every", C.c_uint32),
-                ("l2_window", C.c_uint32)]
+                ("l2_window", C.c_uint32), ("kernel", C.c_uint32)]
 
 
 class Stats(C.Structure):
@@ -117,6 +118,7 @@ _SIGS = {
     "mlem_matrix_destroy": (C.c_int, [_P]),
     "mlem_matrix_get_info": (C.c_int, [_P, _P]),
     "mlem_matrix_get_norm": (C.c_int, [_P, _P]),
+    "mlem_matrix_get_tuning": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P]),
     "mlem_matrix_get_transpose": (C.c_int, [_P, _P, _P, _P]),
     "mlem_matrix_get_csr": (C.c_int, [_P, _P, _P, _P]),
     "mlem_matrix_generate": (C.c_int, [_P, _P, _P]),
@@ -335,6 +337,15 @@ class Matrix:
         _check(load_library().mlem_matrix_get_norm(self._h, _ptr(out)))
         return out
 
+    def tuning(self, transposed=False) -> dict:
+        """The csr-vector configuration the autotuner chose for A or Aᵀ."""
+        k, ln, u, ms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
+        _check(load_library().mlem_matrix_get_tuning(self._h, int(transposed), C.byref(k), C.byref(ln),
+                                                     C.byref(u), C.byref(ms)))
+        names = {0: "direct", 1: "tma", 2: "persistent"}
+        return {"kernel": names.get(k.value, k.value), "lanes_per_row": ln.value, "vectors_in_flight": u.value,
+                "ms": ms.value}
+
     def transpose(self):
         cp = np.zeros(self.cols + 1, np.uint64)
         ri = np.zeros(max(self.nnz, 1), np.uint32)
@@ -358,11 +369,12 @@ class Matrix:
     # runs -------------------------------------------------------------------
     @staticmethod
     def run_opts(spmv=SPMV_CSR_VECTOR, bp_mode=BP_TRANS, secsize_fp=5, secsize_bp=5, use_graph=True,
-                 loglik_every=0, l2_window=True) -> RunOpts:
+                 loglik_every=0, l2_window=True, kernel=KERNEL_AUTO) -> RunOpts:
         o = RunOpts()
         load_library().mlem_run_opts_default(C.byref(o))
         o.spmv, o.bp_mode, o.secsize_fp, o.secsize_bp = spmv, bp_mode, secsize_fp, secsize_bp
         o.use_graph, o.loglik_every, o.l2_window = int(use_graph), loglik_every, int(l2_window)
+        o.kernel = int(kernel)
         return o
 
     def run(self, g, iterations: int, f0=None, loglik=False, stats=False, **opts):

@@ -32,7 +32,15 @@ struct EpiArgs {
 // Rows of `op` times x, one group of `lanes` (8/16/32) threads per row,
 // 128-bit loads of indices and values, deterministic reduction order.
 void launch_csrvec(const DevCsr& op, const float* x, const EpiArgs& epi, int lanes,
-                   L2Window win, cudaStream_t s);
+                   L2Window win, cudaStream_t s, int unroll = 2);
+// Persistent warp-per-row variant that prefetches the next row's pointers.
+void prepare_csrvec_pf(mlem_value_type vt);
+void launch_csrvec_pf(const DevCsr& op, const float* x, const EpiArgs& epi, L2Window win, cudaStream_t s);
+// Same product through the TMA-pipelined kernel (spmv_tma.cu); *err is set
+// when a bounded wait expires.  prepare_* settles attributes outside captures.
+void prepare_csr_tma(mlem_value_type vt);
+void launch_csr_tma(const DevCsr& op, const float* x, const EpiArgs& epi, uint32_t* err, L2Window win,
+                    cudaStream_t s);
 // bp[idx] += val * ratio[row] over the rows of A (calcBwProj_none_trans, kernel.cu:165-177).
 void launch_scatter(const DevCsr& A, const float* ratio, float* bp, int lanes, L2Window win,
                     cudaStream_t s);

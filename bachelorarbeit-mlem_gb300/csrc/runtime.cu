@@ -42,6 +42,7 @@ void Workspace::release() {
     cudaFree(fwproj);
     cudaFree(ll_part);
     cudaFree(ll_vals);
+    cudaFree(err);
     *this = Workspace();
 }
 
@@ -100,6 +101,8 @@ void ensure_workspace(mlem_matrix* m) {
     MLEM_CUDA(cudaMalloc(&w.bp, sizeof(float) * C));
     MLEM_CUDA(cudaMalloc(&w.fwproj, sizeof(float) * R));
     MLEM_CUDA(cudaMalloc(&w.ll_part, sizeof(double) * kLoglikParts));
+    MLEM_CUDA(cudaMalloc(&w.err, sizeof(uint32_t)));
+    MLEM_CUDA(cudaMemsetAsync(w.err, 0, sizeof(uint32_t), m->stream));
     MLEM_CUDA(cudaMemsetAsync(w.bp, 0, sizeof(float) * C, m->stream));
     MLEM_CUDA(cudaMemsetAsync(w.ratio, 0, sizeof(float) * R, m->stream));
     w.ready = true;
@@ -115,7 +118,10 @@ const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
     return plans.emplace(secsize, p).first->second;
 }
 
+
 void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o) {
+    MLEM_REQUIRE(o.kernel <= MLEM_KERNEL_AUTO, MLEM_EINVAL,
+                 "kernel must be 0 (direct), 1 (tma), 2 (persistent) or 3 (auto)");
     MLEM_REQUIRE(o.spmv == MLEM_SPMV_MERGE || o.spmv == MLEM_SPMV_CSR_VECTOR, MLEM_EINVAL,
                  "spmv must be 0 (merge-based) or 1 (csr-vector)");
     MLEM_REQUIRE(o.bp_mode == MLEM_BP_TRANS || o.bp_mode == MLEM_BP_SCATTER || o.bp_mode == MLEM_BP_FUSED,
@@ -124,6 +130,122 @@ void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o) {
                  MLEM_EINVAL, "section sizes must be in 1..512");
     MLEM_REQUIRE(o.bp_mode != MLEM_BP_TRANS || m->has_t, MLEM_EINVAL,
                  "transposed back projection needs a matrix created with build_transpose = 1");
+}
+
+void check_device_error(mlem_matrix* m, cudaStream_t s) {
+    Workspace& w = m->ws;
+    if (!w.err) return;
+    uint32_t h = 0;
+    MLEM_CUDA(cudaMemcpyAsync(&h, w.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    MLEM_CUDA(cudaStreamSynchronize(s));
+    if (h) {
+        MLEM_CUDA(cudaMemsetAsync(w.err, 0, sizeof(uint32_t), s));
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        fail(MLEM_ETIMEOUT, "a pipelined projection kernel gave up waiting for its copies; results are invalid");
+    }
+}
+
+static void launch_cfg(mlem_matrix* m, const DevCsr& op, const float* x, const EpiArgs& e, const ProjCfg& c,
+                       L2Window win, cudaStream_t s) {
+    if (c.kind == MLEM_KERNEL_TMA) {
+        ensure_workspace(m);
+        launch_csr_tma(op, x, e, m->ws.err, win, s);
+    } else if (c.kind == MLEM_KERNEL_PERSISTENT) {
+        launch_csrvec_pf(op, x, e, win, s);
+    } else {
+        launch_csrvec(op, x, e, c.lanes, win, s, c.unroll);
+    }
+}
+
+// Times every candidate configuration on the operand itself (Raw epilogue
+// into a scratch vector, x = 1) and keeps the fastest.  Runs once per
+// operand, outside any stream capture.
+static void tune_projection(mlem_matrix* m, bool transposed) {
+    if (m->tuned[transposed]) return;
+    const DevCsr& op = transposed ? m->AT : m->A;
+    cudaStream_t s = m->stream;
+    std::vector<ProjCfg> cand;
+    const int base = pick_lanes(op.nnz, op.nrows);
+    for (int lanes : {base / 2, base, base * 2})
+        if (lanes >= 4 && lanes <= 32)
+            for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_DIRECT, lanes, u, 0.f});
+    if (base == 32) cand.push_back(ProjCfg{MLEM_KERNEL_PERSISTENT, 32, 2, 0.f});
+    cand.push_back(ProjCfg{MLEM_KERNEL_TMA, 32, 2, 0.f});
+    prepare_csrvec_pf(op.vt);
+    prepare_csr_tma(op.vt);
+    ensure_workspace(m);
+    float *x = nullptr, *y = nullptr;
+    MLEM_CUDA(cudaMalloc(&x, sizeof(float) * std::max<uint32_t>(op.ncols, 1)));
+    MLEM_CUDA(cudaMalloc(&y, sizeof(float) * std::max<uint32_t>(op.nrows, 1)));
+    cudaEvent_t e0, e1;
+    MLEM_CUDA(cudaEventCreate(&e0));
+    MLEM_CUDA(cudaEventCreate(&e1));
+    ProjCfg best;
+    best.ms = 1e30f;
+    try {
+        std::vector<float> ones(std::max<uint32_t>(op.ncols, 1), 1.0f);
+        MLEM_CUDA(cudaMemcpyAsync(x, ones.data(), sizeof(float) * ones.size(), cudaMemcpyHostToDevice, s));
+        EpiArgs e;
+        e.kind = Epi::Raw;
+        e.out = y;
+        const int reps = op.nnz > (50ull << 20) ? 2 : 4;
+        for (ProjCfg& c : cand) {
+            launch_cfg(m, op, x, e, c, {}, s);  // warm-up
+            MLEM_CUDA(cudaEventRecord(e0, s));
+            for (int r = 0; r < reps; ++r) launch_cfg(m, op, x, e, c, {}, s);
+            MLEM_CUDA(cudaEventRecord(e1, s));
+            MLEM_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            MLEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            c.ms = ms / reps;
+            if (c.ms < best.ms) best = c;
+        }
+        check_device_error(m, s);
+    } catch (...) {
+        cudaFree(x);
+        cudaFree(y);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaFree(x);
+    cudaFree(y);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    m->proj[transposed] = best;
+    m->tuned[transposed] = true;
+}
+
+void prepare_kernel(mlem_matrix* m, const mlem_run_opts& o) {
+    if (o.kernel == MLEM_KERNEL_TMA) prepare_csr_tma(m->vt);
+    else if (o.kernel == MLEM_KERNEL_PERSISTENT) prepare_csrvec_pf(m->vt);
+    else if (o.kernel == MLEM_KERNEL_AUTO) {
+        tune_projection(m, false);
+        if (m->has_t) tune_projection(m, true);
+    }
+}
+
+void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, const mlem_run_opts& o,
+             L2Window win, cudaStream_t s) {
+    const DevCsr& op = transposed ? m->AT : m->A;
+    if (o.spmv == MLEM_SPMV_MERGE) {
+        launch_merge_spmv(op, merge_plan(m, transposed, transposed ? o.secsize_bp : o.secsize_fp), x, e, win, s);
+        return;
+    }
+    ProjCfg c;
+    if (o.kernel == MLEM_KERNEL_AUTO) {
+        MLEM_REQUIRE(m->tuned[transposed], MLEM_EINVAL, "internal: projection used before autotuning");
+        c = m->proj[transposed];
+    } else if (o.kernel == MLEM_KERNEL_PERSISTENT && pick_lanes(op.nnz, op.nrows) == 32) {
+        c.kind = MLEM_KERNEL_PERSISTENT;
+    } else if (o.kernel == MLEM_KERNEL_TMA) {
+        c.kind = MLEM_KERNEL_TMA;
+    } else {
+        c.kind = MLEM_KERNEL_DIRECT;
+        c.lanes = pick_lanes(op.nnz, op.nrows);
+        c.unroll = 2;
+    }
+    launch_cfg(m, op, x, e, c, win, s);
 }
 
 // One MLEM iteration on stream s using the matrix workspace.
@@ -145,16 +267,13 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
         fe.g = w.g;
         fe.out = w.ratio;
         fe.fwproj = want_ll ? w.fwproj : nullptr;
-        if (o.spmv == MLEM_SPMV_MERGE) launch_merge_spmv(A, merge_plan(m, false, o.secsize_fp), w.f, fe, wf, s);
-        else launch_csrvec(A, w.f, fe, pick_lanes(A.nnz, A.nrows), wf, s);
+        project(m, false, w.f, fe, o, wf, s);
         if (o.bp_mode == MLEM_BP_TRANS) {
             EpiArgs be;
             be.kind = Epi::Update;
             be.f = w.f;
             be.norm = m->norm;
-            if (o.spmv == MLEM_SPMV_MERGE)
-                launch_merge_spmv(m->AT, merge_plan(m, true, o.secsize_bp), w.ratio, be, wr, s);
-            else launch_csrvec(m->AT, w.ratio, be, pick_lanes(m->AT.nnz, m->AT.nrows), wr, s);
+            project(m, true, w.ratio, be, o, wr, s);
         } else {
             launch_scatter(A, w.ratio, w.bp, pick_lanes(A.nnz, A.nrows), wr, s);
             launch_update_zero(w.f, w.bp, m->norm, A.ncols, s);
@@ -202,10 +321,11 @@ static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cud
     constexpr uint32_t kChunk = 8;
     auto get_graph = [&](uint32_t chunk) -> cudaGraphExec_t {
         RunKey key{(int)o.spmv, (int)o.bp_mode, (int)o.secsize_fp, (int)o.secsize_bp, (int)o.l2_window,
-                   (int)chunk};
+                   (int)chunk, (int)o.kernel};
         auto it = m->ws.graphs.find(key);
         if (it != m->ws.graphs.end()) return it->second;
-        // plans must exist before capture (their build synchronises)
+        // plans and kernel attributes must exist before capture
+        if (o.spmv == MLEM_SPMV_CSR_VECTOR) prepare_kernel(m, o);
         if (o.spmv == MLEM_SPMV_MERGE && o.bp_mode != MLEM_BP_FUSED) {
             merge_plan(m, false, o.secsize_fp);
             if (o.bp_mode == MLEM_BP_TRANS) merge_plan(m, true, o.secsize_bp);
@@ -237,7 +357,7 @@ static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cud
     auto replay = [&](uint32_t chunk, uint32_t times) {
         cudaGraphExec_t ge = get_graph(chunk);
         const RunKey key{(int)o.spmv, (int)o.bp_mode, (int)o.secsize_fp, (int)o.secsize_bp,
-                         (int)o.l2_window, (int)chunk};
+                         (int)o.l2_window, (int)chunk, (int)o.kernel};
         const uint64_t nodes = m->ws.graph_nodes[key];
         for (uint32_t q = 0; q < times; ++q) {
             MLEM_CUDA(cudaGraphLaunch(ge, s));
@@ -381,6 +501,7 @@ void mlem_run_opts_default(mlem_run_opts* o) {
     o->use_graph = 1;
     o->loglik_every = 0;
     o->l2_window = 1;
+    o->kernel = MLEM_KERNEL_AUTO;
 }
 
 mlem_status mlem_matrix_create(const mlem_csr_host* csr, const mlem_matrix_opts* opts, mlem_matrix** out) {
@@ -440,6 +561,23 @@ mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info) {
         info->device_bytes = m->bytes();
         info->max_row_nnz = m->A.max_row;
         info->max_col_nnz = m->has_t ? m->AT.max_row : 0;
+    });
+}
+
+mlem_status mlem_matrix_get_tuning(mlem_matrix* m, uint32_t transposed, int* kernel, int* lanes, int* unroll,
+                                   float* ms) {
+    return guarded([&] {
+        MLEM_REQUIRE(m && kernel && lanes && unroll && ms, MLEM_EINVAL, "NULL argument");
+        MLEM_REQUIRE(transposed <= 1, MLEM_EINVAL, "transposed must be 0 or 1");
+        MLEM_REQUIRE(!transposed || m->has_t, MLEM_EINVAL, "matrix has no transpose");
+        std::lock_guard<std::mutex> lk(m->mu);
+        DeviceGuard dg(m->device);
+        tune_projection(m, transposed != 0);
+        const ProjCfg& c = m->proj[transposed];
+        *kernel = c.kind;
+        *lanes = c.lanes;
+        *unroll = c.unroll;
+        *ms = c.ms;
     });
 }
 
@@ -512,6 +650,7 @@ mlem_status mlem_run(mlem_matrix* m, const int32_t* g, const float* f0, uint32_t
         cudaStream_t s = m->stream;
         const uint32_t rows = m->A.nrows, cols = m->A.ncols;
         Workspace& w = m->ws;
+        if (o.spmv == MLEM_SPMV_CSR_VECTOR) prepare_kernel(m, o);
         MLEM_CUDA(cudaMemcpyAsync(w.g, g, sizeof(int32_t) * rows, cudaMemcpyHostToDevice, s));
         uint64_t h2d = sizeof(int32_t) * (uint64_t)rows;
         if (f0) {
@@ -553,6 +692,7 @@ mlem_status mlem_run(mlem_matrix* m, const int32_t* g, const float* f0, uint32_t
         cudaEventElapsedTime(&ms, e0, e1);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        check_device_error(m, s);
         if (loglik_out) {
             for (uint32_t i = 0; i < iterations; ++i)
                 loglik_out[i] = ll.empty() ? std::numeric_limits<double>::quiet_NaN() : ll[i];
@@ -591,6 +731,7 @@ mlem_status mlem_run_device(mlem_matrix* m, const int32_t* g_dev, float* f_dev, 
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         const uint32_t rows = m->A.nrows, cols = m->A.ncols;
         Workspace& w = m->ws;
+        if (o.spmv == MLEM_SPMV_CSR_VECTOR) prepare_kernel(m, o);
         MLEM_CUDA(cudaMemcpyAsync(w.g, g_dev, sizeof(int32_t) * rows, cudaMemcpyDeviceToDevice, s));
         MLEM_CUDA(cudaMemcpyAsync(w.f, f_dev, sizeof(float) * cols, cudaMemcpyDeviceToDevice, s));
         run_loop(m, o, iterations, s, nullptr);
@@ -614,8 +755,8 @@ mlem_status mlem_forward_project(mlem_matrix* m, const float* f_dev, const int32
         fe.g = g_dev;
         fe.out = ratio_dev;
         fe.fwproj = fwproj_out_dev;
-        if (o.spmv == MLEM_SPMV_MERGE) launch_merge_spmv(m->A, merge_plan(m, false, o.secsize_fp), f_dev, fe, {}, s);
-        else launch_csrvec(m->A, f_dev, fe, pick_lanes(m->A.nnz, m->A.nrows), {}, s);
+        if (o.spmv == MLEM_SPMV_CSR_VECTOR) prepare_kernel(m, o);
+        project(m, false, f_dev, fe, o, {}, s);
     });
 }
 
@@ -634,8 +775,8 @@ mlem_status mlem_back_project(mlem_matrix* m, const float* ratio_dev, float* bp_
             EpiArgs be;
             be.kind = Epi::Raw;
             be.out = bp_dev;
-            if (o.spmv == MLEM_SPMV_MERGE) launch_merge_spmv(m->AT, merge_plan(m, true, o.secsize_bp), ratio_dev, be, {}, s);
-            else launch_csrvec(m->AT, ratio_dev, be, pick_lanes(m->AT.nnz, m->AT.nrows), {}, s);
+            if (o.spmv == MLEM_SPMV_CSR_VECTOR) prepare_kernel(m, o);
+            project(m, true, ratio_dev, be, o, {}, s);
         } else {
             MLEM_CUDA(cudaMemsetAsync(bp_dev, 0, sizeof(float) * m->A.ncols, s));
             launch_scatter(m->A, ratio_dev, bp_dev, pick_lanes(m->A.nnz, m->A.nrows), {}, s);

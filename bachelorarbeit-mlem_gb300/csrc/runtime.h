@@ -46,10 +46,10 @@ struct DeviceGuard {
 };
 
 struct RunKey {
-    int spmv, bp, ss_fp, ss_bp, l2, chunk;
+    int spmv, bp, ss_fp, ss_bp, l2, chunk, pipe;
     bool operator<(const RunKey& o) const {
-        return std::tie(spmv, bp, ss_fp, ss_bp, l2, chunk) <
-               std::tie(o.spmv, o.bp, o.ss_fp, o.ss_bp, o.l2, o.chunk);
+        return std::tie(spmv, bp, ss_fp, ss_bp, l2, chunk, pipe) <
+               std::tie(o.spmv, o.bp, o.ss_fp, o.ss_bp, o.l2, o.chunk, o.pipe);
     }
 };
 
@@ -64,6 +64,7 @@ struct Workspace {
     double* ll_part = nullptr; // [kLoglikParts]
     double* ll_vals = nullptr; // [ll_cap]
     uint32_t ll_cap = 0;
+    uint32_t* err = nullptr;   // set by kernels whose bounded waits expired
     std::map<RunKey, cudaGraphExec_t> graphs;
     std::map<RunKey, uint64_t> graph_nodes;
     void release();
@@ -96,6 +97,16 @@ struct BatchState {
 
 }  // namespace mlem
 
+namespace mlem {
+// Launch configuration of a csr-vector projection.
+struct ProjCfg {
+    int kind = 0;    // mlem_kernel: DIRECT, TMA or PERSISTENT
+    int lanes = 32;  // DIRECT: lanes per row
+    int unroll = 2;  // DIRECT: 4-element vectors in flight per lane
+    float ms = 0.f;  // measured time of one launch
+};
+}  // namespace mlem
+
 struct mlem_matrix {
     int device = 0;
     mlem_value_type vt = MLEM_VAL_F32;
@@ -107,6 +118,8 @@ struct mlem_matrix {
     mlem::Workspace ws;
     std::map<uint32_t, mlem::MergePlan> plan_A, plan_AT;
     uint32_t batch_tile = 0;          // autotuned batch tile (0 = not yet)
+    bool tuned[2] = {false, false};   // csr-vector configuration of A / Aᵀ measured
+    mlem::ProjCfg proj[2];
     std::mutex mu;
     uint64_t bytes() const;
 };
@@ -119,6 +132,13 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
 void enqueue_batch_iteration(mlem_matrix* m, BatchState& b, cudaStream_t s);
 float reference_initial_value(const mlem_matrix* m, const int32_t* g);
 void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o);
+// Settles kernel attributes / occupancy of the selected variant (outside captures).
+void prepare_kernel(mlem_matrix* m, const mlem_run_opts& o);
+// Reads and clears the workspace error flag; fails with MLEM_ETIMEOUT if set.
+void check_device_error(mlem_matrix* m, cudaStream_t s);
+// One projection of `op` (A or Aᵀ) with the kernel the options select.
+void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, const mlem_run_opts& o,
+             L2Window win, cudaStream_t s);
 // Copies slot b of the interleaved batch state to/from contiguous device buffers.
 void batch_put_slot(BatchState& b, uint32_t rows, uint32_t cols, uint32_t slot, const int32_t* g_dev,
                     float init, const float* f0_dev, uint32_t iters, cudaStream_t s);

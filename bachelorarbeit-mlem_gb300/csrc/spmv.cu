@@ -16,6 +16,10 @@
 // iteration is two launches and never needs a memset.
 #include "kernels.cuh"
 
+#include <algorithm>
+#include <map>
+#include <mutex>
+
 namespace mlem {
 
 namespace {
@@ -49,26 +53,26 @@ __device__ __forceinline__ float fma4(float acc, const float a[4], const float g
     return acc;
 }
 
-// Dot product of row [s, t) with x by one lane of an LPR-lane group.
-template <typename V, int LPR>
+// Dot product of row [s, t) with x by one lane of an LPR-lane group; U
+// vectors of 4 elements are loaded before their gathers are consumed.
+template <typename V, int LPR, int U = 2>
 __device__ __forceinline__ float lane_dot(const uint32_t* __restrict__ idx, const V* __restrict__ val,
                                           const float* __restrict__ x, uint64_t s, uint64_t t, int sub) {
     const uint4* idx4 = reinterpret_cast<const uint4*>(idx);
     const uint64_t v1 = (t + 3) >> 2;
     uint64_t v = (s >> 2) + sub;
     float acc = 0.f;
-    // two vectors in flight per lane before their gathers are consumed
-    for (; v + LPR < v1; v += 2 * LPR) {
-        Vec4<V> p, q;
-        p.load(idx4, val, v);
-        q.load(idx4, val, v + LPR);
-        float gp[4], gq[4];
-        gather4(p.c, v << 2, s, t, x, gp);
-        gather4(q.c, (v + LPR) << 2, s, t, x, gq);
-        acc = fma4(acc, p.a, gp, v << 2, s, t);
-        acc = fma4(acc, q.a, gq, (v + LPR) << 2, s, t);
+    for (; v + (U - 1) * LPR < v1; v += U * LPR) {
+        Vec4<V> p[U];
+#pragma unroll
+        for (int q = 0; q < U; ++q) p[q].load(idx4, val, v + q * LPR);
+        float gq[U][4];
+#pragma unroll
+        for (int q = 0; q < U; ++q) gather4(p[q].c, (v + q * LPR) << 2, s, t, x, gq[q]);
+#pragma unroll
+        for (int q = 0; q < U; ++q) acc = fma4(acc, p[q].a, gq[q], (v + q * LPR) << 2, s, t);
     }
-    if (v < v1) {
+    for (; v < v1; v += LPR) {
         Vec4<V> p;
         p.load(idx4, val, v);
         float gp[4];
@@ -101,7 +105,7 @@ __device__ __forceinline__ void epi_update(uint32_t c, float sum, float* __restr
     f[c] = (n == 0.0f) ? t : __fdiv_rn(t, n);
 }
 
-template <typename V, int LPR, int EPI>
+template <typename V, int LPR, int EPI, int U>
 __global__ void __launch_bounds__(256)
 k_csrvec(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
          const V* __restrict__ val, const float* __restrict__ x, uint32_t nrows,
@@ -113,13 +117,49 @@ k_csrvec(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
     float acc = 0.f;
     if (row < nrows) {
         const uint64_t s = rowptr[row], t = rowptr[row + 1];
-        acc = lane_dot<V, LPR>(idx, val, x, s, t, sub);
+        acc = lane_dot<V, LPR, U>(idx, val, x, s, t, sub);
     }
     acc = group_sum<LPR>(acc);
     if (sub == 0 && row < nrows) {
         if (EPI == (int)Epi::Correl) epi_correl(row, acc, g, out, fwproj);
         else if (EPI == (int)Epi::Update) epi_update(row, acc, f, norm);
         else out[row] = acc;
+    }
+}
+
+// Persistent variant: one warp per row, W warps walk the rows with stride W
+// and fetch the next row's pointers before summing the current row, so the
+// dependent row-pointer load never stalls the stream.  Same per-row
+// arithmetic as k_csrvec<V, 32, EPI> (bit-identical results).
+template <typename V, int EPI>
+__global__ void __launch_bounds__(256)
+k_csrvec_pf(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
+            const V* __restrict__ val, const float* __restrict__ x, uint32_t nrows,
+            const int32_t* __restrict__ g, float* __restrict__ out, float* __restrict__ fwproj,
+            float* __restrict__ f, const float* __restrict__ norm) {
+    const uint32_t W = (gridDim.x * blockDim.x) >> 5;
+    uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= nrows) return;  // warp-uniform
+    uint64_t s = rowptr[row], t = rowptr[row + 1];
+    while (true) {
+        const uint32_t nrow = row + W;
+        uint64_t ns = 0, nt = 0;
+        if (nrow < nrows) {
+            ns = rowptr[nrow];
+            nt = rowptr[nrow + 1];
+        }
+        float acc = lane_dot<V, 32>(idx, val, x, s, t, lane);
+        acc = group_sum<32>(acc);
+        if (lane == 0) {
+            if (EPI == (int)Epi::Correl) epi_correl(row, acc, g, out, fwproj);
+            else if (EPI == (int)Epi::Update) epi_update(row, acc, f, norm);
+            else out[row] = acc;
+        }
+        if (nrow >= nrows) break;
+        row = nrow;
+        s = ns;
+        t = nt;
     }
 }
 
@@ -257,7 +297,7 @@ __global__ void __launch_bounds__(1024) k_reduce_f64(const double* __restrict__ 
     if (threadIdx.x == 0) *out = tot;
 }
 
-template <typename V, int LPR>
+template <typename V, int LPR, int U>
 void csrvec_dispatch_epi(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win,
                          cudaStream_t s) {
     const uint64_t threads = (uint64_t)op.nrows * LPR;
@@ -265,28 +305,67 @@ void csrvec_dispatch_epi(const DevCsr& op, const float* x, const EpiArgs& e, L2W
     const V* val = static_cast<const V*>(op.val);
     switch (e.kind) {
         case Epi::Correl:
-            launch_ex(k_csrvec<V, LPR, (int)Epi::Correl>, grid, block, 0, s, win, op.rowptr, op.idx,
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Correl, U>, grid, block, 0, s, win, op.rowptr, op.idx,
                       val, x, op.nrows, e.g, e.out, e.fwproj, (float*)nullptr, (const float*)nullptr);
             break;
         case Epi::Update:
-            launch_ex(k_csrvec<V, LPR, (int)Epi::Update>, grid, block, 0, s, win, op.rowptr, op.idx,
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Update, U>, grid, block, 0, s, win, op.rowptr, op.idx,
                       val, x, op.nrows, (const int32_t*)nullptr, (float*)nullptr, (float*)nullptr,
                       e.f, e.norm);
             break;
         default:
-            launch_ex(k_csrvec<V, LPR, (int)Epi::Raw>, grid, block, 0, s, win, op.rowptr, op.idx,
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Raw, U>, grid, block, 0, s, win, op.rowptr, op.idx,
                       val, x, op.nrows, (const int32_t*)nullptr, e.out, (float*)nullptr,
                       (float*)nullptr, (const float*)nullptr);
     }
 }
 
+template <typename V, int EPI>
+unsigned pf_grid() {
+    static std::mutex mu;
+    static std::map<int, unsigned> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    int per_sm = 0, sms = 0;
+    MLEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_csrvec_pf<V, EPI>, 256, 0));
+    MLEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return cache[dev] = (unsigned)std::max(1, per_sm) * (unsigned)sms;
+}
+
+template <typename V, int EPI>
+void pf_launch(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+    const unsigned grid = std::min(pf_grid<V, EPI>(), std::max(1u, ceil_div_u((uint64_t)op.nrows * 32, 256)));
+    launch_ex(k_csrvec_pf<V, EPI>, dim3(grid), dim3(256), 0, s, win, op.rowptr, op.idx,
+              static_cast<const V*>(op.val), x, op.nrows, e.g, e.out, e.fwproj, e.f, e.norm);
+}
+
 template <typename V>
-void csrvec_dispatch_lanes(const DevCsr& op, const float* x, const EpiArgs& e, int lanes,
+void pf_dispatch(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+    switch (e.kind) {
+        case Epi::Correl: pf_launch<V, (int)Epi::Correl>(op, x, e, win, s); break;
+        case Epi::Update: pf_launch<V, (int)Epi::Update>(op, x, e, win, s); break;
+        default: pf_launch<V, (int)Epi::Raw>(op, x, e, win, s);
+    }
+}
+
+template <typename V, int LPR>
+void csrvec_dispatch_u(const DevCsr& op, const float* x, const EpiArgs& e, int unroll, L2Window win,
+                       cudaStream_t s) {
+    if (unroll >= 4) csrvec_dispatch_epi<V, LPR, 4>(op, x, e, win, s);
+    else if (unroll == 2) csrvec_dispatch_epi<V, LPR, 2>(op, x, e, win, s);
+    else csrvec_dispatch_epi<V, LPR, 1>(op, x, e, win, s);
+}
+
+template <typename V>
+void csrvec_dispatch_lanes(const DevCsr& op, const float* x, const EpiArgs& e, int lanes, int unroll,
                            L2Window win, cudaStream_t s) {
-    if (lanes >= 32) csrvec_dispatch_epi<V, 32>(op, x, e, win, s);
-    else if (lanes >= 16) csrvec_dispatch_epi<V, 16>(op, x, e, win, s);
-    else if (lanes >= 8) csrvec_dispatch_epi<V, 8>(op, x, e, win, s);
-    else csrvec_dispatch_epi<V, 4>(op, x, e, win, s);
+    if (lanes >= 32) csrvec_dispatch_u<V, 32>(op, x, e, unroll, win, s);
+    else if (lanes >= 16) csrvec_dispatch_u<V, 16>(op, x, e, unroll, win, s);
+    else if (lanes >= 8) csrvec_dispatch_u<V, 8>(op, x, e, unroll, win, s);
+    else csrvec_dispatch_u<V, 4>(op, x, e, unroll, win, s);
 }
 
 template <typename V>
@@ -314,12 +393,29 @@ int pick_lanes(uint64_t nnz, uint32_t rows) {
 }
 
 void launch_csrvec(const DevCsr& op, const float* x, const EpiArgs& epi, int lanes, L2Window win,
-                   cudaStream_t s) {
+                   cudaStream_t s, int unroll) {
     if (op.nrows == 0) return;
     switch (op.vt) {
-        case MLEM_VAL_F32: csrvec_dispatch_lanes<float>(op, x, epi, lanes, win, s); break;
-        case MLEM_VAL_F16: csrvec_dispatch_lanes<__half>(op, x, epi, lanes, win, s); break;
-        default: csrvec_dispatch_lanes<__nv_bfloat16>(op, x, epi, lanes, win, s);
+        case MLEM_VAL_F32: csrvec_dispatch_lanes<float>(op, x, epi, lanes, unroll, win, s); break;
+        case MLEM_VAL_F16: csrvec_dispatch_lanes<__half>(op, x, epi, lanes, unroll, win, s); break;
+        default: csrvec_dispatch_lanes<__nv_bfloat16>(op, x, epi, lanes, unroll, win, s);
+    }
+}
+
+void prepare_csrvec_pf(mlem_value_type vt) {
+    switch (vt) {
+        case MLEM_VAL_F32: pf_grid<float, 0>(); pf_grid<float, 1>(); pf_grid<float, 2>(); break;
+        case MLEM_VAL_F16: pf_grid<__half, 0>(); pf_grid<__half, 1>(); pf_grid<__half, 2>(); break;
+        default: pf_grid<__nv_bfloat16, 0>(); pf_grid<__nv_bfloat16, 1>(); pf_grid<__nv_bfloat16, 2>();
+    }
+}
+
+void launch_csrvec_pf(const DevCsr& op, const float* x, const EpiArgs& epi, L2Window win, cudaStream_t s) {
+    if (op.nrows == 0) return;
+    switch (op.vt) {
+        case MLEM_VAL_F32: pf_dispatch<float>(op, x, epi, win, s); break;
+        case MLEM_VAL_F16: pf_dispatch<__half>(op, x, epi, win, s); break;
+        default: pf_dispatch<__nv_bfloat16>(op, x, epi, win, s);
     }
 }
 

@@ -1,0 +1,314 @@
+// spmv_tma.cu — TMA-pipelined row-parallel projection (csr-vector switch).
+//
+// Same arithmetic contract as k_csrvec (spmv.cu): one warp owns a row, sums
+// val*x[col] in a fixed order and applies the fused epilogue (correlation
+// after the forward projection, multiplicative update after the back
+// projection).  What changes is how the matrix reaches the SM: each warp runs
+// a ring of STAGES shared-memory buffers; one elected lane streams the next
+// chunks of its rows (CH elements of indices and values, 16-byte aligned,
+// rows split at CH boundaries) with cp.async.bulk into the ring, completing on
+// per-stage mbarriers, while the 32 lanes gather x[col] for the chunk that
+// has landed.  The HBM stream therefore never waits on the gathers, and the
+// row pointers are fetched 32 rows ahead.  Chunks never span rows, so every
+// row sum has one deterministic order (lane-strided partials, xor tree).
+//
+// Every mbarrier wait is bounded: on expiry the warp records an error in
+// *err, drains its own copies in flight (again bounded) and returns.
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+
+namespace mlem {
+
+namespace {
+
+constexpr int kTmaCh = 512;       // elements per chunk
+constexpr int kTmaStages = 4;     // ring depth per warp
+constexpr int kTmaWarps = 4;      // warps per CTA
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait; false when the limit expired.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ uint64_t evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// 1-D bulk copy global -> shared, completion counted on bar (bytes % 16 == 0,
+// both addresses 16-byte aligned).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                         uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
+        : "memory");
+}
+
+// Staged values are read from shared memory with plain loads (the streaming
+// global loads of Val4 are not valid on a shared-memory address).
+__device__ __forceinline__ float staged(const float* p, uint32_t i) { return p[i]; }
+__device__ __forceinline__ float staged(const __half* p, uint32_t i) { return __half2float(p[i]); }
+__device__ __forceinline__ float staged(const __nv_bfloat16* p, uint32_t i) { return __bfloat162float(p[i]); }
+
+struct ChunkMeta {
+    uint32_t row;    // row index (0xffffffff: no chunk, the warp is done)
+    uint32_t first;  // offset of the chunk's first element in the stage buffer
+    uint32_t count;  // elements of the row in this chunk
+    uint32_t last;   // 1 if the chunk ends its row
+};
+
+template <typename V>
+struct TmaSmem {
+    uint32_t idx[kTmaStages][kTmaCh];
+    V val[kTmaStages][kTmaCh];
+    uint64_t bar[kTmaStages];
+    ChunkMeta meta[kTmaStages];
+};
+
+template <typename V, int EPI>
+__global__ void __launch_bounds__(kTmaWarps * 32)
+k_csr_tma(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx, const V* __restrict__ val,
+          const float* __restrict__ x, uint32_t nrows, const int32_t* __restrict__ g, float* __restrict__ out,
+          float* __restrict__ fwproj, float* __restrict__ f, const float* __restrict__ norm,
+          uint32_t* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    TmaSmem<V>& S = reinterpret_cast<TmaSmem<V>*>(smem_raw)[w];
+    const uint32_t gw = blockIdx.x * kTmaWarps + w;
+    const uint32_t nw = gridDim.x * kTmaWarps;
+    const uint64_t pol = evict_first_policy();
+
+    if (lane == 0)
+        for (int s = 0; s < kTmaStages; ++s) mbar_init(&S.bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncwarp();
+
+    // row pointers of this warp's rows, 32 at a time: batch kb holds rows
+    // gw + (32*kb + lane) * nw
+    auto load_batch = [&](uint32_t kb, uint64_t& s, uint64_t& t) {
+        const uint64_t r = (uint64_t)gw + ((uint64_t)kb * 32 + lane) * nw;
+        if (r < nrows) {
+            s = rowptr[r];
+            t = rowptr[r + 1];
+        } else {
+            s = t = 0;
+        }
+    };
+    uint64_t cs, ct, ns, nt;
+    uint32_t kb = 0;
+    load_batch(0, cs, ct);
+    load_batch(1, ns, nt);
+
+    // producer state (identical in every lane)
+    uint32_t pk = 0;          // row sequence number of the producer
+    uint64_t pp = ~0ull;      // position inside that row (~0 = row start)
+    auto issue = [&](int slot) {
+        const uint64_t r = (uint64_t)gw + (uint64_t)pk * nw;
+        if (r >= nrows) {
+            if (lane == 0) S.meta[slot].row = 0xffffffffu;
+            return;
+        }
+        if (pk / 32 != kb) {  // move to the next batch of row pointers
+            cs = ns;
+            ct = nt;
+            ++kb;
+            load_batch(kb + 1, ns, nt);
+        }
+        const uint64_t s = __shfl_sync(0xffffffffu, cs, pk % 32);
+        const uint64_t t = __shfl_sync(0xffffffffu, ct, pk % 32);
+        const uint64_t p = (pp == ~0ull) ? s : pp;
+        const uint64_t a0 = p & ~7ull;
+        const uint64_t e_end = t < a0 + kTmaCh ? t : a0 + kTmaCh;
+        const uint64_t a1 = (e_end + 7) & ~7ull;
+        const uint32_t ncopy = (uint32_t)(a1 - a0);
+        if (lane == 0) {
+            S.meta[slot].row = (uint32_t)r;
+            S.meta[slot].first = (uint32_t)(p - a0);
+            S.meta[slot].count = (uint32_t)(e_end - p);
+            S.meta[slot].last = e_end == t ? 1u : 0u;
+            if (ncopy) {
+                mbar_arrive_tx(&S.bar[slot], ncopy * (uint32_t)(sizeof(uint32_t) + sizeof(V)));
+                bulk_g2s(S.idx[slot], idx + a0, ncopy * (uint32_t)sizeof(uint32_t), &S.bar[slot], pol);
+                bulk_g2s(S.val[slot], val + a0, ncopy * (uint32_t)sizeof(V), &S.bar[slot], pol);
+            } else {
+                mbar_arrive(&S.bar[slot]);
+            }
+        }
+        if (e_end == t) {
+            ++pk;
+            pp = ~0ull;
+        } else {
+            pp = e_end;
+        }
+    };
+
+    for (int s = 0; s < kTmaStages; ++s) issue(s);
+    __syncwarp();
+
+    uint32_t phase = 0;  // bit s = parity to wait for on stage s
+    float acc = 0.f;
+    int slot = 0;
+    bool failed = false;
+    while (true) {
+        const ChunkMeta m = S.meta[slot];
+        if (m.row == 0xffffffffu) break;
+        if (!mbar_wait(&S.bar[slot], (phase >> slot) & 1u)) {
+            failed = true;
+            break;
+        }
+        phase ^= 1u << slot;
+        const uint32_t* ci = S.idx[slot] + m.first;
+        const V* cv = S.val[slot] + m.first;
+        // up to 16 elements per lane: 8 gathers in flight, then their FMAs
+        uint32_t i = lane;
+#pragma unroll 1
+        for (; i + 224 < m.count; i += 256) {
+            uint32_t c[8];
+            float v[8], gx[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                c[q] = ci[i + 32 * q];
+                v[q] = staged(cv, i + 32 * q);
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) gx[q] = __ldg(x + c[q]);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc = fmaf(v[q], gx[q], acc);
+        }
+        for (; i < m.count; i += 32) acc = fmaf(staged(cv, i), __ldg(x + ci[i]), acc);
+        if (m.last) {
+            float tot = acc;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+            if (lane == 0) {
+                const uint32_t r = m.row;
+                if (EPI == (int)Epi::Correl) {
+                    out[r] = (tot != 0.0f) ? __fdiv_rn((float)g[r], tot) : 0.0f;
+                    if (fwproj) fwproj[r] = tot;
+                } else if (EPI == (int)Epi::Update) {
+                    const float tt = __fmul_rn(f[r], tot);
+                    const float nn = norm[r];
+                    f[r] = (nn == 0.0f) ? tt : __fdiv_rn(tt, nn);
+                } else {
+                    out[r] = tot;
+                }
+            }
+            acc = 0.f;
+        }
+        __syncwarp();  // every lane is done reading this stage
+        issue(slot);   // refill it with the chunk kTmaStages ahead
+        __syncwarp();
+        slot = (slot + 1) % kTmaStages;
+    }
+    if (failed) {
+        if (lane == 0) atomicOr(err, 1u);
+        // drain this warp's copies still in flight before leaving
+        for (int k = 0; k < kTmaStages; ++k) {
+            const int sl = (slot + k) % kTmaStages;
+            if (S.meta[sl].row != 0xffffffffu) mbar_wait(&S.bar[sl], (phase >> sl) & 1u);
+        }
+    }
+}
+
+template <typename V, int EPI>
+unsigned tma_grid() {
+    static std::mutex mu;
+    static std::map<int, unsigned> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    const size_t smem = sizeof(TmaSmem<V>) * kTmaWarps;
+    MLEM_CUDA(cudaFuncSetAttribute(k_csr_tma<V, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0, sms = 0;
+    MLEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_csr_tma<V, EPI>, kTmaWarps * 32, smem));
+    MLEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const unsigned grid = (unsigned)std::max(1, per_sm) * (unsigned)sms;
+    cache[dev] = grid;
+    return grid;
+}
+
+template <typename V, int EPI>
+void tma_launch(const DevCsr& op, const float* x, const EpiArgs& e, uint32_t* err, L2Window win, cudaStream_t s) {
+    const unsigned grid = tma_grid<V, EPI>();
+    const size_t smem = sizeof(TmaSmem<V>) * kTmaWarps;
+    const unsigned need = ceil_div_u(op.nrows, kTmaWarps);  // no more warps than rows
+    launch_ex(k_csr_tma<V, EPI>, dim3(std::min(grid, std::max(1u, need))), dim3(kTmaWarps * 32), smem, s, win,
+              op.rowptr, op.idx, static_cast<const V*>(op.val), x, op.nrows, e.g, e.out, e.fwproj, e.f, e.norm, err);
+}
+
+template <typename V>
+void tma_dispatch(const DevCsr& op, const float* x, const EpiArgs& e, uint32_t* err, L2Window win, cudaStream_t s) {
+    switch (e.kind) {
+        case Epi::Correl: tma_launch<V, (int)Epi::Correl>(op, x, e, err, win, s); break;
+        case Epi::Update: tma_launch<V, (int)Epi::Update>(op, x, e, err, win, s); break;
+        default: tma_launch<V, (int)Epi::Raw>(op, x, e, err, win, s);
+    }
+}
+
+}  // namespace
+
+void prepare_csr_tma(mlem_value_type vt) {
+    // kernel attributes and occupancy are settled outside any stream capture
+    switch (vt) {
+        case MLEM_VAL_F32:
+            tma_grid<float, 0>(); tma_grid<float, 1>(); tma_grid<float, 2>();
+            break;
+        case MLEM_VAL_F16:
+            tma_grid<__half, 0>(); tma_grid<__half, 1>(); tma_grid<__half, 2>();
+            break;
+        default:
+            tma_grid<__nv_bfloat16, 0>(); tma_grid<__nv_bfloat16, 1>(); tma_grid<__nv_bfloat16, 2>();
+    }
+}
+
+void launch_csr_tma(const DevCsr& op, const float* x, const EpiArgs& epi, uint32_t* err, L2Window win,
+                    cudaStream_t s) {
+    if (op.nrows == 0) return;
+    switch (op.vt) {
+        case MLEM_VAL_F32: tma_dispatch<float>(op, x, epi, err, win, s); break;
+        case MLEM_VAL_F16: tma_dispatch<__half>(op, x, epi, err, win, s); break;
+        default: tma_dispatch<__nv_bfloat16>(op, x, epi, err, win, s);
+    }
+}
+
+}  // namespace mlem

@@ -168,7 +168,7 @@ def make_problem(pkg, name, torch, value_type=0):
     return m, geo, g, t_gen
 
 
-def time_kernels(pkg, m, torch, g_dev, f_dev, reps=10):
+def time_kernels(pkg, m, torch, g_dev, f_dev, reps=10, kernel=3):
     """Average CUDA-event duration of the FP and BP kernels (launched alone)."""
     s = torch.cuda.current_stream()
     ratio = torch.zeros(m.rows, dtype=torch.float32, device="cuda")
@@ -177,18 +177,20 @@ def time_kernels(pkg, m, torch, g_dev, f_dev, reps=10):
     for kind in ("fp", "bp"):
         for _ in range(2):
             if kind == "fp":
-                m.forward_project(f_dev.data_ptr(), g_dev.data_ptr(), ratio.data_ptr(), 0, stream=s.cuda_stream)
+                m.forward_project(f_dev.data_ptr(), g_dev.data_ptr(), ratio.data_ptr(), 0, stream=s.cuda_stream,
+                                  kernel=kernel)
             else:
-                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream)
+                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream, kernel=kernel)
         times = []
         for _ in range(reps):
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(s)
             if kind == "fp":
-                m.forward_project(f_dev.data_ptr(), g_dev.data_ptr(), ratio.data_ptr(), 0, stream=s.cuda_stream)
+                m.forward_project(f_dev.data_ptr(), g_dev.data_ptr(), ratio.data_ptr(), 0, stream=s.cuda_stream,
+                                  kernel=kernel)
             else:
-                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream)
+                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream, kernel=kernel)
             b.record(s)
             b.synchronize()
             times.append(a.elapsed_time(b))
@@ -378,6 +380,9 @@ def main():
 
     # roofline of the dominant kernel
     kt = time_kernels(pkg, m, torch, g_dev, f0_dev)
+    kt_direct = time_kernels(pkg, m, torch, g_dev, f0_dev, kernel=0)
+    kt_tma = time_kernels(pkg, m, torch, g_dev, f0_dev, kernel=1)
+    kt_pers = time_kernels(pkg, m, torch, g_dev, f0_dev, kernel=2)
     fp_b, bp_b = algorithmic_bytes(m.rows, m.cols, m.nnz, 4)
     dom = "fp" if kt["fp"] >= kt["bp"] else "bp"
     dom_bytes = fp_b if dom == "fp" else bp_b
@@ -402,13 +407,15 @@ def main():
                 "d2h_bytes_per_step": int(4 * m.cols)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": "k_csrvec (FP, fused correlation)" if dom == "fp"
-                     else "k_csrvec (BP over Aᵀ)", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     else "k_csrvec (BP over Aᵀ, fused update)", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes": dom_bytes, "kernel_ms": kt[dom],
                      "iteration": {"bytes": iter_bytes, "ms": ms / args.steps / iters,
                                    "achieved_gbs": iter_bytes / (ms / args.steps / iters * 1e-3) / 1e9,
                                    "frac": iter_bytes / (ms / args.steps / iters * 1e-3) / 1e9 / peak},
-                     "fp_ms": kt["fp"], "bp_ms": kt["bp"]},
+                     "fp_ms": kt["fp"], "bp_ms": kt["bp"],
+                     "variants_ms": {"autotuned": kt, "direct": kt_direct, "tma": kt_tma, "persistent": kt_pers},
+                     "autotuned": {"fp": m.tuning(False), "bp": m.tuning(True)}},
         "clocks": clk.summary(),
     }
     m.close()

@@ -108,6 +108,12 @@ typedef struct {
 } mlem_matrix_info;
 
 mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info);
+/* Configuration the autotuner chose for the csr-vector projection of A
+ * (transposed = 0) or Aᵀ (1): kernel (mlem_kernel), lanes per row, vectors in
+ * flight per lane and the measured milliseconds of one launch.  Tunes on
+ * first call if needed. */
+mlem_status mlem_matrix_get_tuning(mlem_matrix* m, uint32_t transposed, int* kernel, int* lanes,
+                                   int* unroll, float* ms);
 /* Copies the sensitivity image (f32[cols]) to the host. */
 mlem_status mlem_matrix_get_norm(const mlem_matrix* m, float* norm_out);
 /* Copies the device-built transpose to the host: colptr u64[cols+1],
@@ -125,9 +131,24 @@ typedef struct {
     uint32_t use_graph;         /* 1: replay the iteration as a CUDA graph */
     uint32_t loglik_every;      /* 0: off; k: FP64 log-likelihood every k-th iteration */
     uint32_t l2_window;         /* 1: keep the image/ratio vector L2-persisting */
+    uint32_t kernel;            /* csr-vector switch only: mlem_kernel variant */
 } mlem_run_opts;
 
-/* Defaults: CSR_VECTOR, BP_TRANS, secsize 5/5, graphs on, no log-likelihood, L2 window on. */
+/* Kernel variants of the csr-vector projections (same arithmetic; the order of
+ * the FP32 additions depends on the variant and its lanes/unroll, so results of
+ * different variants agree to rounding, and one matrix handle always uses one):
+ *   DIRECT     one warp (or 4-32 lanes) per row, a grid of one row per group;
+ *   PERSISTENT resident warps walk the rows and prefetch the next row's pointers;
+ *   TMA        rows streamed into a shared-memory ring with cp.async.bulk. */
+typedef enum {
+    MLEM_KERNEL_DIRECT = 0,
+    MLEM_KERNEL_TMA = 1,
+    MLEM_KERNEL_PERSISTENT = 2,
+    MLEM_KERNEL_AUTO = 3 /* autotuned per matrix operand (lanes per row, vectors in flight, variant) */
+} mlem_kernel;
+
+/* Defaults: CSR_VECTOR, BP_TRANS, secsize 5/5, graphs on, no log-likelihood, L2 window on,
+ * AUTO kernel. */
 void mlem_run_opts_default(mlem_run_opts* o);
 
 typedef struct {

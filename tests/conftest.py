@@ -72,8 +72,16 @@ def cuda():
 
 
 def problem(pkg, O, name, n_shapes=5, total=1e6, seed=0):
-    """Host CSR + sinogram + sensitivity + reference initial image for a preset."""
-    geo = pkg.preset(name)
+    """Host CSR + sinogram + sensitivity + reference initial image for a preset.
+
+    "cyl3d_tiny_dense" is a small cylinder (2 x 24 detectors, 40x40x8 voxels
+    of 0.8 mm, 3x2 sub-rays) dense enough (> 96 nnz per row) to select the
+    one-warp-per-row kernels for the forward projection."""
+    if name == "cyl3d_tiny_dense":
+        geo = pkg.geometry(24, 2, 20.0, 3.0, nx=40, ny=40, nz=8, vx=0.8, vy=0.8, vz=0.8, sub_t=3, sub_z=2,
+                           width_t=1.5, width_z=1.2)
+    else:
+        geo = pkg.preset(name)
     rp, c, v, cols = pkg.siddon_host(geo)
     from mlem_gb300 import synth
     xt = synth.phantom(geo, n_shapes, seed=seed + 1)

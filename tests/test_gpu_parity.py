@@ -136,21 +136,23 @@ def test_mlem_against_reference_fixtures(pkg, golden, spmv, bp_mode):
             ut = 1 if bp_mode else 0
             ref = golden[f"{name}/mlem_s{spmv}_t{ut}_ss5x5_it{iters}"]
             for graph in (True, False):
-                got = m.run(g, iters, f0=f0, spmv=spmv, bp_mode=bp_mode, use_graph=graph)
-                err = float(np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref))
-                assert err < TOL_F32, (name, iters, graph, err)
+                for kern in ((0, 1, 2, 3) if spmv == 1 else (3,)):
+                    got = m.run(g, iters, f0=f0, spmv=spmv, bp_mode=bp_mode, use_graph=graph, kernel=kern)
+                    err = float(np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref))
+                    assert err < TOL_F32, (name, iters, graph, kern, err)
         m.close()
 
 
-@pytest.mark.parametrize("spmv,bp_mode", MODES)
-@pytest.mark.parametrize("name", ["ring2d", "cyl3d_tiny"])
-def test_mlem_against_oracle(pkg, O, spmv, bp_mode, name):
+@pytest.mark.parametrize("spmv,bp_mode,kern", [m + (3,) for m in MODES] + [(1, 0, 0), (1, 1, 0), (1, 0, 1), (1, 2, 1),
+                                                                          (1, 0, 2)])
+@pytest.mark.parametrize("name", ["ring2d", "cyl3d_tiny", "cyl3d_tiny_dense"])
+def test_mlem_against_oracle(pkg, O, spmv, bp_mode, kern, name):
     p = problem(pkg, O, name)
     A = (p["rp"], p["col"], p["val"])
     AT = O.transpose(*A, p["cols"])
     m = pkg.Matrix.from_csr(*A, p["cols"], norm=p["norm"])
     iters = 20
-    got = m.run(p["g"], iters, f0=p["f0"], spmv=spmv, bp_mode=bp_mode, secsize_fp=5, secsize_bp=5)
+    got = m.run(p["g"], iters, f0=p["f0"], spmv=spmv, bp_mode=bp_mode, secsize_fp=5, secsize_bp=5, kernel=kern)
     ref32 = O.mlem_f32(A, AT if bp_mode == 0 else None, p["g"], p["norm"], p["f0"], iters, spmv=spmv,
                        using_trans=1 if bp_mode else 0)
     assert O.rel_l2(got, ref32) < TOL_F32
@@ -200,11 +202,31 @@ def test_section_sizes(pkg, O):
 def test_deterministic_paths_are_bitwise_repeatable(pkg, O):
     p = problem(pkg, O, "ring2d")
     m = pkg.Matrix.from_csr(p["rp"], p["col"], p["val"], p["cols"])
-    for spmv in (0, 1):
-        a = m.run(p["g"], 10, spmv=spmv, bp_mode=0)
-        b = m.run(p["g"], 10, spmv=spmv, bp_mode=0, use_graph=False)
+    runs = {}
+    for spmv, kern in ((0, 3), (1, 0), (1, 1), (1, 2), (1, 3)):
+        a = m.run(p["g"], 10, spmv=spmv, bp_mode=0, kernel=kern)
+        b = m.run(p["g"], 10, spmv=spmv, bp_mode=0, use_graph=False, kernel=kern)
         assert np.array_equal(a, b)
+        runs[(spmv, kern)] = a
     m.close()
+
+
+@pytest.mark.parametrize("vt,kern", [(0, 0), (0, 1), (0, 2), (0, 3), (1, 1), (1, 2), (1, 3)])
+def test_kernel_variants_long_and_empty_rows(pkg, O, golden, cuda, vt, kern):
+    # rows longer than a pipeline chunk (512), empty rows, one-row matrices
+    for name in ("one_row", "rand_long", "empty_rows", "tall", "rand_dup"):
+        rp, c, v, cols = golden_csr(golden, name)
+        m = pkg.Matrix.from_csr(rp, c, v, cols, value_type=vt)
+        x = golden[f"{name}/x"]
+        dx, dg = dev(cuda, x), dev(cuda, np.zeros(m.rows, np.int32))
+        ratio = cuda.zeros(m.rows, dtype=cuda.float32, device="cuda")
+        fp = cuda.full((m.rows,), -1.0, dtype=cuda.float32, device="cuda")
+        m.forward_project(dx.data_ptr(), dg.data_ptr(), ratio.data_ptr(), fp.data_ptr(), kernel=kern)
+        cuda.cuda.synchronize()
+        vq = v if vt == 0 else v.astype(np.float16).astype(np.float32)
+        want = O.spmv_csrvec(rp, c, vq, x)
+        np.testing.assert_allclose(fp.cpu().numpy(), want, rtol=2e-5, atol=1e-5, err_msg=name)
+        m.close()
 
 
 @pytest.mark.parametrize("vt", [1, 2])
