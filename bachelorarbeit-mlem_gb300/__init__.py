@@ -25,7 +25,7 @@ LIB_PATH = PKG / "lib" / "libmlem_gb300.so"
 CLI_PATH = PKG / "bin" / "mlem_gb300"
 
 SPMV_MERGE, SPMV_CSR_VECTOR = 0, 1
-KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO = 0, 1, 2, 3
+KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO, KERNEL_D16, KERNEL_ILV = 0, 1, 2, 3, 4, 5
 VAL_F32, VAL_F16, VAL_BF16 = 0, 1, 2
 BP_TRANS, BP_SCATTER, BP_FUSED = 0, 1, 2
 
@@ -48,7 +48,7 @@ class CsrHost(C.Structure):
 
 class MatrixOpts(C.Structure):
     _fields_ = [("value_type", C.c_int), ("build_transpose", C.c_uint32), ("norm", C.c_void_p),
-                ("device", C.c_int)]
+                ("device", C.c_int), ("compress_indices", C.c_uint32), ("interleave", C.c_uint32)]
 
 
 class MatrixInfo(C.Structure):
@@ -272,11 +272,13 @@ class Matrix:
 
     # construction ---------------------------------------------------------
     @staticmethod
-    def _opts(value_type=VAL_F32, build_transpose=True, norm=None, device=0):
+    def _opts(value_type=VAL_F32, build_transpose=True, norm=None, device=0, compress=False, interleave=False):
         o = MatrixOpts()
         load_library().mlem_matrix_opts_default(C.byref(o))
         o.value_type = value_type
         o.build_transpose = 1 if build_transpose else 0
+        o.compress_indices = 1 if compress else 0
+        o.interleave = 1 if interleave else 0
         keep = None
         if norm is not None:
             keep = _arr(norm, np.float32)
@@ -286,12 +288,12 @@ class Matrix:
 
     @classmethod
     def from_csr(cls, rowptr, col, val, cols: int, value_type=VAL_F32, build_transpose=True, norm=None,
-                 device=0) -> "Matrix":
+                 device=0, compress=False, interleave=False) -> "Matrix":
         rowptr = _arr(rowptr, np.uint64)
         col = _arr(col, np.uint32)
         val = _arr(val, np.float32)
         csr = CsrHost(len(rowptr) - 1, cols, len(col), _ptr(rowptr), _ptr(col), _ptr(val))
-        o, keep = cls._opts(value_type, build_transpose, norm, device)
+        o, keep = cls._opts(value_type, build_transpose, norm, device, compress, interleave)
         h = C.c_void_p()
         _check(load_library().mlem_matrix_create(C.byref(csr), C.byref(o), C.byref(h)))
         return cls(h.value)
@@ -304,8 +306,9 @@ class Matrix:
         return cls(h.value)
 
     @classmethod
-    def generate(cls, geo: Geometry, value_type=VAL_F32, build_transpose=True, device=0) -> "Matrix":
-        o, _ = cls._opts(value_type, build_transpose, None, device)
+    def generate(cls, geo: Geometry, value_type=VAL_F32, build_transpose=True, device=0,
+                 compress=False, interleave=False) -> "Matrix":
+        o, _ = cls._opts(value_type, build_transpose, None, device, compress, interleave)
         h = C.c_void_p()
         _check(load_library().mlem_matrix_generate(C.byref(geo), C.byref(o), C.byref(h)))
         return cls(h.value)
@@ -342,7 +345,7 @@ class Matrix:
         k, ln, u, ms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
         _check(load_library().mlem_matrix_get_tuning(self._h, int(transposed), C.byref(k), C.byref(ln),
                                                      C.byref(u), C.byref(ms)))
-        names = {0: "direct", 1: "tma", 2: "persistent"}
+        names = {0: "direct", 1: "tma", 2: "persistent", 4: "d16", 5: "ilv"}
         return {"kernel": names.get(k.value, k.value), "lanes_per_row": ln.value, "vectors_in_flight": u.value,
                 "ms": ms.value}
 

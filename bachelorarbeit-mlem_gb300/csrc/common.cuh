@@ -116,6 +116,15 @@ struct DevCsr {
     void* val = nullptr;         // f32/f16/bf16 [padded(nnz)]
     mlem_value_type vt = MLEM_VAL_F32;
     uint32_t max_row = 0;        // longest row
+    // optional delta-compressed indices (spmv_d16.cu)
+    uint64_t* rowmeta = nullptr; // [nrows] first column | first escape index << 32
+    uint16_t* d16 = nullptr;     // [padded(nnz)]
+    uint32_t* esc = nullptr;     // [nesc]
+    uint64_t nesc = 0;
+    // optional lane-interleaved copy (spmv_ilv.cu)
+    uint32_t* idx_ilv = nullptr; // [ilv_len]
+    void* val_ilv = nullptr;     // [ilv_len]
+    uint64_t ilv_len = 0;
 };
 
 }  // namespace mlem

@@ -33,6 +33,14 @@ struct EpiArgs {
 // 128-bit loads of indices and values, deterministic reduction order.
 void launch_csrvec(const DevCsr& op, const float* x, const EpiArgs& epi, int lanes,
                    L2Window win, cudaStream_t s, int unroll = 2);
+// Lane-interleaved copy (elements permuted inside 128-blocks) and its projection.
+void build_ilv(DevCsr& op, cudaStream_t s);
+void launch_csr_ilv(const DevCsr& op, const float* x, const EpiArgs& epi, int unroll, L2Window win,
+                    cudaStream_t s);
+// Delta-compressed (16-bit) column indices: build from the u32 indices, and
+// the projection that reads them.
+void build_d16(DevCsr& op, cudaStream_t s);
+void launch_csr_d16(const DevCsr& op, const float* x, const EpiArgs& epi, L2Window win, cudaStream_t s);
 // Persistent warp-per-row variant that prefetches the next row's pointers.
 void prepare_csrvec_pf(mlem_value_type vt);
 void launch_csrvec_pf(const DevCsr& op, const float* x, const EpiArgs& epi, L2Window win, cudaStream_t s);

@@ -82,13 +82,21 @@ static void free_csr(DevCsr& c) {
     cudaFree(c.rowptr);
     cudaFree(c.idx);
     cudaFree(c.val);
+    cudaFree(c.rowmeta);
+    cudaFree(c.d16);
+    cudaFree(c.esc);
+    cudaFree(c.idx_ilv);
+    cudaFree(c.val_ilv);
     c = DevCsr();
 }
 
 static uint64_t csr_bytes(const DevCsr& c) {
     if (!c.rowptr) return 0;
-    return sizeof(uint64_t) * ((uint64_t)c.nrows + 1) + sizeof(uint32_t) * padded(c.nnz) +
-           val_bytes(c.vt) * padded(c.nnz);
+    uint64_t b = sizeof(uint64_t) * ((uint64_t)c.nrows + 1) + sizeof(uint32_t) * padded(c.nnz) +
+                 val_bytes(c.vt) * padded(c.nnz);
+    if (c.d16) b += sizeof(uint64_t) * c.nrows + sizeof(uint16_t) * padded(c.nnz) + sizeof(uint32_t) * c.nesc;
+    if (c.idx_ilv) b += (sizeof(uint32_t) + val_bytes(c.vt)) * c.ilv_len;
+    return b;
 }
 
 void ensure_workspace(mlem_matrix* m) {
@@ -120,8 +128,8 @@ const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
 
 
 void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o) {
-    MLEM_REQUIRE(o.kernel <= MLEM_KERNEL_AUTO, MLEM_EINVAL,
-                 "kernel must be 0 (direct), 1 (tma), 2 (persistent) or 3 (auto)");
+    MLEM_REQUIRE(o.kernel <= MLEM_KERNEL_ILV, MLEM_EINVAL,
+                 "kernel must be 0 (direct), 1 (tma), 2 (persistent), 3 (auto), 4 (d16) or 5 (ilv)");
     MLEM_REQUIRE(o.spmv == MLEM_SPMV_MERGE || o.spmv == MLEM_SPMV_CSR_VECTOR, MLEM_EINVAL,
                  "spmv must be 0 (merge-based) or 1 (csr-vector)");
     MLEM_REQUIRE(o.bp_mode == MLEM_BP_TRANS || o.bp_mode == MLEM_BP_SCATTER || o.bp_mode == MLEM_BP_FUSED,
@@ -150,6 +158,10 @@ static void launch_cfg(mlem_matrix* m, const DevCsr& op, const float* x, const E
     if (c.kind == MLEM_KERNEL_TMA) {
         ensure_workspace(m);
         launch_csr_tma(op, x, e, m->ws.err, win, s);
+    } else if (c.kind == MLEM_KERNEL_D16) {
+        launch_csr_d16(op, x, e, win, s);
+    } else if (c.kind == MLEM_KERNEL_ILV) {
+        launch_csr_ilv(op, x, e, c.unroll, win, s);
     } else if (c.kind == MLEM_KERNEL_PERSISTENT) {
         launch_csrvec_pf(op, x, e, win, s);
     } else {
@@ -171,6 +183,9 @@ static void tune_projection(mlem_matrix* m, bool transposed) {
             for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_DIRECT, lanes, u, 0.f});
     if (base == 32) cand.push_back(ProjCfg{MLEM_KERNEL_PERSISTENT, 32, 2, 0.f});
     cand.push_back(ProjCfg{MLEM_KERNEL_TMA, 32, 2, 0.f});
+    if (op.d16) cand.push_back(ProjCfg{MLEM_KERNEL_D16, 32, 1, 0.f});
+    if (op.idx_ilv)
+        for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_ILV, 32, u, 0.f});
     prepare_csrvec_pf(op.vt);
     prepare_csr_tma(op.vt);
     ensure_workspace(m);
@@ -240,6 +255,13 @@ void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, 
         c.kind = MLEM_KERNEL_PERSISTENT;
     } else if (o.kernel == MLEM_KERNEL_TMA) {
         c.kind = MLEM_KERNEL_TMA;
+    } else if (o.kernel == MLEM_KERNEL_D16) {
+        MLEM_REQUIRE(op.d16 != nullptr, MLEM_EINVAL, "kernel D16 needs a matrix created with compress_indices = 1");
+        c.kind = MLEM_KERNEL_D16;
+    } else if (o.kernel == MLEM_KERNEL_ILV) {
+        MLEM_REQUIRE(op.idx_ilv != nullptr, MLEM_EINVAL, "kernel ILV needs a matrix created with interleave = 1");
+        c.kind = MLEM_KERNEL_ILV;
+        c.unroll = 2;
     } else {
         c.kind = MLEM_KERNEL_DIRECT;
         c.lanes = pick_lanes(op.nnz, op.nrows);
@@ -392,6 +414,14 @@ static void postprocess_matrix(mlem_matrix* m, const mlem_matrix_opts& o) {
         if (m->has_t) lower(m->AT);
     }
     m->vt = o.value_type;
+    if (o.compress_indices) {
+        build_d16(A, s);
+        if (m->has_t) build_d16(m->AT, s);
+    }
+    if (o.interleave) {
+        build_ilv(A, s);
+        if (m->has_t) build_ilv(m->AT, s);
+    }
     MLEM_CUDA(cudaMalloc(&m->norm, sizeof(float) * std::max<uint32_t>(A.ncols, 1)));
     if (o.norm) {
         MLEM_CUDA(cudaMemcpyAsync(m->norm, o.norm, sizeof(float) * A.ncols, cudaMemcpyHostToDevice, s));
@@ -490,6 +520,8 @@ void mlem_matrix_opts_default(mlem_matrix_opts* o) {
     o->build_transpose = 1;
     o->norm = nullptr;
     o->device = 0;
+    o->compress_indices = 0;
+    o->interleave = 0;
 }
 
 void mlem_run_opts_default(mlem_run_opts* o) {

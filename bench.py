@@ -149,12 +149,12 @@ def barrier(dist, torch=None):
             dist.barrier()
 
 
-def make_problem(pkg, name, torch, value_type=0):
+def make_problem(pkg, name, torch, value_type=0, compress=False, interleave=True):
     from mlem_gb300 import synth
     cfg = WORKLOADS[name]
     geo = pkg.preset(name)
     t0 = time.time()
-    m = pkg.Matrix.generate(geo, value_type=value_type)
+    m = pkg.Matrix.generate(geo, value_type=value_type, compress=compress, interleave=interleave)
     t_gen = time.time() - t0
     xt = synth.phantom(geo, cfg["shapes"], seed=1).astype(np.float32)
     dx = torch.from_numpy(xt).cuda()
@@ -258,12 +258,15 @@ def run_forms(pkg, torch, args):
     s = torch.cuda.current_stream()
     name = args.workload
     iters = WORKLOADS[name]["iters"]
-    # FP16 values, same workload
-    m16, geo, g, _ = make_problem(pkg, name, torch, value_type=pkg.VAL_F16)
+    # FP16 values with 16-bit delta-coded indices (4 B per nonzero), same workload
+    m16, geo, g, _ = make_problem(pkg, name, torch, value_type=pkg.VAL_F16, compress=True)
     g_dev = torch.from_numpy(g).cuda()
     f0 = np.full(m16.cols, m16.initial_value(g), np.float32)
     f0_dev = torch.from_numpy(f0).cuda()
     f_dev = torch.empty_like(f0_dev)
+    kt16 = time_kernels(pkg, m16, torch, g_dev, f0_dev)
+    res["fp16_kernels"] = {"fp_ms": kt16["fp"], "bp_ms": kt16["bp"], "fp": m16.tuning(False), "bp": m16.tuning(True),
+                           "device_bytes": m16.device_bytes}
     for bp_mode, label in ((0, "fp16_trans"), (2, "fp16_fused")):
         f_dev.copy_(f0_dev)
         m16.run_device(g_dev.data_ptr(), f_dev.data_ptr(), 5, stream=s.cuda_stream, bp_mode=bp_mode)
@@ -308,6 +311,8 @@ def main():
     ap.add_argument("--workload", default="cyl3d_12gb", choices=sorted(WORKLOADS))
     ap.add_argument("--forms", default="all", choices=["all", "none"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-interleave", action="store_true",
+                    help="skip the lane-interleaved matrix copy (halves device memory)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -318,7 +323,7 @@ def main():
     pkg = load_pkg()
     name = args.workload
     iters = WORKLOADS[name]["iters"]
-    m, geo, g, t_gen = make_problem(pkg, name, torch)
+    m, geo, g, t_gen = make_problem(pkg, name, torch, interleave=not args.no_interleave)
     s = torch.cuda.current_stream()
     g_dev = torch.from_numpy(g).cuda()
     f0 = np.full(m.cols, m.initial_value(g), np.float32)

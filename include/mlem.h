@@ -80,6 +80,10 @@ typedef struct {
     const float* norm;          /* optional host sensitivity image f32[cols];
                                    NULL = computed on the GPU as Aᵀ1 in FP64 */
     int device;                 /* CUDA device ordinal (reference: GPU 0) */
+    uint32_t compress_indices;  /* 1: also keep 16-bit delta-coded column indices (2 B per
+                                   nonzero instead of 4) for the csr-vector projections */
+    uint32_t interleave;        /* 1: also keep a lane-interleaved copy (16-byte loads whose
+                                   gathers cover consecutive columns) for the projections */
 } mlem_matrix_opts;
 
 /* Fills *o with the defaults: F32 values, transpose built, norm computed, device 0. */
@@ -144,7 +148,9 @@ typedef enum {
     MLEM_KERNEL_DIRECT = 0,
     MLEM_KERNEL_TMA = 1,
     MLEM_KERNEL_PERSISTENT = 2,
-    MLEM_KERNEL_AUTO = 3 /* autotuned per matrix operand (lanes per row, vectors in flight, variant) */
+    MLEM_KERNEL_AUTO = 3, /* autotuned per matrix operand (lanes per row, vectors in flight, variant) */
+    MLEM_KERNEL_D16 = 4,  /* delta-compressed indices (matrix created with compress_indices = 1) */
+    MLEM_KERNEL_ILV = 5   /* lane-interleaved copy (matrix created with interleave = 1) */
 } mlem_kernel;
 
 /* Defaults: CSR_VECTOR, BP_TRANS, secsize 5/5, graphs on, no log-likelihood, L2 window on,

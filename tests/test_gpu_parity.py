@@ -265,3 +265,78 @@ def test_device_generator_matches_host(pkg, name, stride):
     assert np.array_equal(gc, c)
     assert np.array_equal(gv.view(np.uint32), v.view(np.uint32))
     m.close()
+
+
+# ------------------------------------------------------- compressed indices
+@pytest.mark.parametrize("vt", [0, 1, 2])
+def test_d16_projection_matches_oracle(pkg, O, golden, cuda, vt):
+    # escapes: unsorted rows (rand_dup has repeated columns), large gaps (rand_long, one_row)
+    for name in ("rand_small", "rand_long", "rand_dup", "one_row", "empty_rows", "tall", "cyl3d_tiny"):
+        rp, c, v, cols = golden_csr(golden, name)
+        m = pkg.Matrix.from_csr(rp, c, v, cols, value_type=vt, compress=True)
+        x = golden[f"{name}/x"]
+        dx, dg = dev(cuda, x), dev(cuda, np.zeros(m.rows, np.int32))
+        ratio = cuda.zeros(m.rows, dtype=cuda.float32, device="cuda")
+        fp = cuda.full((m.rows,), -1.0, dtype=cuda.float32, device="cuda")
+        m.forward_project(dx.data_ptr(), dg.data_ptr(), ratio.data_ptr(), fp.data_ptr(), kernel=pkg.KERNEL_D16)
+        cuda.cuda.synchronize()
+        vq = {0: v, 1: v.astype(np.float16).astype(np.float32)}.get(vt)
+        if vq is None:  # bf16: round to nearest even on the top 16 bits
+            u = v.view(np.uint32).astype(np.uint64)
+            u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+            vq = u.astype(np.uint32).view(np.float32)
+        want = O.spmv_csrvec(rp, c, vq, x)
+        np.testing.assert_allclose(fp.cpu().numpy(), want, rtol=2e-5, atol=1e-5, err_msg=name)
+        m.close()
+
+
+@pytest.mark.parametrize("kern", [3, 4])
+def test_d16_mlem(pkg, O, kern):
+    p = problem(pkg, O, "cyl3d_tiny_dense")
+    A = (p["rp"], p["col"], p["val"])
+    ref64 = O.mlem_f64(A, p["g"], p["norm"], p["f0"], 20)
+    m = pkg.Matrix.from_csr(*A, p["cols"], norm=p["norm"], compress=True)
+    got = m.run(p["g"], 20, f0=p["f0"], kernel=kern)
+    assert O.rel_l2(got, ref64) < TOL_F32
+    m.close()
+    mh = pkg.Matrix.from_csr(*A, p["cols"], value_type=pkg.VAL_F16, compress=True)
+    ref64h = O.mlem_f64(A, p["g"], O.colsum(*A, p["cols"]), p["f0"], 20)
+    got = mh.run(p["g"], 20, f0=p["f0"], kernel=kern)
+    assert O.rel_l2(got, ref64h) < TOL_LOWP
+    assert mh.device_bytes > 0
+    mh.close()
+
+
+@pytest.mark.parametrize("vt", [0, 1, 2])
+def test_interleaved_projection_matches_oracle(pkg, O, golden, cuda, vt):
+    for name in ("rand_small", "rand_long", "rand_dup", "one_row", "empty_rows", "tall", "cyl3d_tiny"):
+        rp, c, v, cols = golden_csr(golden, name)
+        m = pkg.Matrix.from_csr(rp, c, v, cols, value_type=vt, interleave=True)
+        x = golden[f"{name}/x"]
+        dx, dg = dev(cuda, x), dev(cuda, np.zeros(m.rows, np.int32))
+        ratio = cuda.zeros(m.rows, dtype=cuda.float32, device="cuda")
+        fp = cuda.full((m.rows,), -1.0, dtype=cuda.float32, device="cuda")
+        m.forward_project(dx.data_ptr(), dg.data_ptr(), ratio.data_ptr(), fp.data_ptr(), kernel=pkg.KERNEL_ILV)
+        cuda.cuda.synchronize()
+        got = fp.cpu().numpy()
+        if vt == 0:
+            # the lane-strided order of mat_vec_mul_csr_vector: within FMA rounding of the oracle
+            want = O.spmv_csrvec(rp, c, v, x)
+            np.testing.assert_allclose(got, want, rtol=2e-6, atol=1e-6, err_msg=name)
+        else:
+            want = O.spmv_csrvec(rp, c, v, x)
+            np.testing.assert_allclose(got, want, rtol=1e-2, atol=1e-3, err_msg=name)
+        m.close()
+
+
+def test_interleaved_and_compressed_mlem(pkg, O):
+    p = problem(pkg, O, "cyl3d_tiny_dense")
+    A = (p["rp"], p["col"], p["val"])
+    ref64 = O.mlem_f64(A, p["g"], p["norm"], p["f0"], 20)
+    m = pkg.Matrix.from_csr(*A, p["cols"], norm=p["norm"], interleave=True, compress=True)
+    for kern in (3, 4, 5):
+        got = m.run(p["g"], 20, f0=p["f0"], kernel=kern)
+        assert O.rel_l2(got, ref64) < TOL_F32, kern
+    fp_cfg, bp_cfg = m.tuning(False), m.tuning(True)
+    assert fp_cfg["ms"] > 0 and bp_cfg["ms"] > 0
+    m.close()
