@@ -547,7 +547,7 @@ def write_image(path, f) -> None:
 class Server:
     """Continuous-batching reconstruction server over resident matrices."""
 
-    def __init__(self, slots_per_matrix=16, hbm_budget_bytes=0, hbm_reserve_bytes=2 << 30,
+    def __init__(self, slots_per_matrix=0, hbm_budget_bytes=0, hbm_reserve_bytes=2 << 30,
                  queue_capacity=4096):
         lib = load_library()
         o = ServerOpts(slots_per_matrix, hbm_budget_bytes, hbm_reserve_bytes, queue_capacity)

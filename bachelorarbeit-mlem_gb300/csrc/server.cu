@@ -7,13 +7,14 @@
 // captured once as a CUDA graph and replayed until the longest slot of the
 // tile finishes.  BT is picked by timing 8/16/32 on the matrix (autotuner).
 //
-// Server: one worker thread owns per-matrix slot states.  Between iterations
-// it admits queued requests into free slots (a matrix's slot state is
-// allocated on first use if it fits the HBM budget), runs one iteration of
-// every matrix that has active slots, each matrix on its own stream so their
-// kernels overlap on the GPU, and hands finished images back.  A request's
-// arithmetic depends only on its slot's tile size, so its result is the same
-// alone and in a mix.
+// Server: one worker thread owns per-matrix slot states; every matrix runs on
+// its own stream and advances independently: when one of its iterations
+// completes (event query), finished slots hand their images back, queued
+// requests are admitted into free slots (a matrix's slot state is allocated
+// on first use if it fits the HBM budget) and its next iteration is launched.
+// Kernels of different matrices overlap on the GPU, and a small matrix is
+// not paced by a large one.  A request's arithmetic depends only on its
+// slot's tile size, so its result is the same alone and in a mix.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -103,11 +104,15 @@ static uint32_t autotune_tile(mlem_matrix* m, cudaStream_t s) {
             cudaGetLastError();
             continue;
         }
-        // all slots idle (remaining = 0): the kernels run in full, f is kept
-        MLEM_CUDA(cudaMemsetAsync(b.f, 0, sizeof(float) * (uint64_t)std::max(cols, 1u) * bt, s));
+        // representative data (image 1, counts 1) with every slot idle
+        // (remaining = 0): the kernels run in full and f is left as is
+        std::vector<float> ones((uint64_t)std::max(cols, 1u) * bt, 1.0f);
+        std::vector<int32_t> cnt((uint64_t)std::max(rows, 1u) * bt, 1);
+        MLEM_CUDA(cudaMemcpyAsync(b.f, ones.data(), sizeof(float) * ones.size(), cudaMemcpyHostToDevice, s));
+        MLEM_CUDA(cudaMemcpyAsync(b.g, cnt.data(), sizeof(int32_t) * cnt.size(), cudaMemcpyHostToDevice, s));
         enqueue_batch_iteration(m, b, s);  // warm-up
         MLEM_CUDA(cudaEventRecord(e0, s));
-        for (int q = 0; q < 2; ++q) enqueue_batch_iteration(m, b, s);
+        for (int q = 0; q < 3; ++q) enqueue_batch_iteration(m, b, s);
         MLEM_CUDA(cudaEventRecord(e1, s));
         MLEM_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
@@ -150,10 +155,17 @@ struct MatrixSlots {
     BatchState bs;
     bool allocated = false;
     cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;       // recorded after each enqueued iteration
+    bool inflight = false;            // an iteration is running on `stream`
     std::vector<uint64_t> slot_req;   // 0 = free
     std::vector<uint32_t> slot_left;
     uint64_t graph_nodes = 0;
     uint32_t tile = 0;
+    bool active() const {
+        for (uint64_t x : slot_req)
+            if (x) return true;
+        return false;
+    }
 };
 
 }  // namespace
@@ -184,13 +196,16 @@ bool mlem_server::admit_locked() {
         Request& r = reqs[*it];
         MatrixSlots& ms = mats[r.mid];
         const uint32_t rows = ms.m->A.nrows, cols = ms.m->A.ncols;
+        if (ms.inflight) {  // its slots are being read by a running iteration
+            ++it;
+            continue;
+        }
         if (!ms.allocated) {
             const uint64_t need = batch_state_bytes(rows, cols, ms.tile, !ms.m->has_t);
             if (in_use + need > budget) {
                 // release the state of idle matrices, then retry once
                 for (auto& o : mats)
-                    if (o.allocated && std::all_of(o.slot_req.begin(), o.slot_req.end(),
-                                                   [](uint64_t x) { return x == 0; })) {
+                    if (o.allocated && !o.inflight && !o.active()) {
                         cudaStreamSynchronize(o.stream);
                         in_use -= o.bs.bytes;
                         o.bs.release();
@@ -233,49 +248,58 @@ bool mlem_server::admit_locked() {
 
 void mlem_server::run() {
     DeviceGuard dg(device);
-    std::vector<float> host_f;
+    // Each matrix advances on its own stream: as soon as one of its iterations
+    // completes (event), finished slots are handed back, queued requests are
+    // admitted into free slots and its next iteration is launched.  Small
+    // matrices therefore iterate at their own pace next to large ones.
     while (true) {
+        bool any_inflight = false;
         {
             std::unique_lock<std::mutex> lk(mu);
             if (stop) break;
+            // 1. completions
+            for (auto& ms : mats) {
+                if (!ms.inflight) continue;
+                const cudaError_t q = cudaEventQuery(ms.done);
+                if (q == cudaErrorNotReady) continue;
+                MLEM_CUDA(q);
+                ms.inflight = false;
+                const uint32_t cols = ms.m->A.ncols;
+                for (uint32_t b = 0; b < ms.tile; ++b) {
+                    if (ms.slot_req[b] == 0) continue;
+                    ++st.iterations_done;
+                    if (--ms.slot_left[b] > 0) continue;
+                    Request& r = reqs[ms.slot_req[b]];
+                    batch_get_slot(ms.bs, cols, b, ms.bs.stage_f, ms.stream);
+                    r.result.resize(cols);
+                    MLEM_CUDA(cudaMemcpyAsync(r.result.data(), ms.bs.stage_f, sizeof(float) * cols,
+                                              cudaMemcpyDeviceToHost, ms.stream));
+                    MLEM_CUDA(cudaStreamSynchronize(ms.stream));
+                    r.t_done = std::chrono::steady_clock::now();
+                    r.state = ReqState::Done;
+                    ms.slot_req[b] = 0;
+                    --st.active;
+                    ++st.completed;
+                    cv_done.notify_all();
+                }
+            }
+            // 2. admissions into free slots of idle matrices
             admit_locked();
-            bool active = false;
-            for (auto& ms : mats)
-                for (uint64_t x : ms.slot_req) active |= (x != 0);
-            if (!active) {
+            // 3. next iteration of every idle matrix with work
+            for (auto& ms : mats) {
+                if (!ms.inflight && ms.active()) {
+                    batch_step(ms.m, ms.bs, ms.stream, true, ms.graph_nodes);
+                    MLEM_CUDA(cudaEventRecord(ms.done, ms.stream));
+                    ms.inflight = true;
+                }
+                any_inflight |= ms.inflight;
+            }
+            if (!any_inflight) {
                 cv_work.wait_for(lk, std::chrono::milliseconds(20));
                 continue;
             }
         }
-        // one iteration of every matrix with work, overlapping across streams
-        for (auto& ms : mats) {
-            bool act = false;
-            for (uint64_t x : ms.slot_req) act |= (x != 0);
-            if (act) batch_step(ms.m, ms.bs, ms.stream, true, ms.graph_nodes);
-        }
-        for (auto& ms : mats)
-            if (ms.allocated) MLEM_CUDA(cudaStreamSynchronize(ms.stream));
-        std::unique_lock<std::mutex> lk(mu);
-        for (auto& ms : mats) {
-            const uint32_t cols = ms.m->A.ncols;
-            for (uint32_t b = 0; b < ms.tile; ++b) {
-                if (ms.slot_req[b] == 0) continue;
-                ++st.iterations_done;
-                if (--ms.slot_left[b] > 0) continue;
-                Request& r = reqs[ms.slot_req[b]];
-                batch_get_slot(ms.bs, cols, b, ms.bs.stage_f, ms.stream);
-                r.result.resize(cols);
-                MLEM_CUDA(cudaMemcpyAsync(r.result.data(), ms.bs.stage_f, sizeof(float) * cols,
-                                          cudaMemcpyDeviceToHost, ms.stream));
-                MLEM_CUDA(cudaStreamSynchronize(ms.stream));
-                r.t_done = std::chrono::steady_clock::now();
-                r.state = ReqState::Done;
-                ms.slot_req[b] = 0;
-                --st.active;
-                ++st.completed;
-            }
-        }
-        cv_done.notify_all();
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
 }
 
@@ -379,7 +403,7 @@ mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, con
 
 void mlem_server_opts_default(mlem_server_opts* o) {
     if (!o) return;
-    o->slots_per_matrix = 16;
+    o->slots_per_matrix = 0;
     o->hbm_budget_bytes = 0;
     o->hbm_reserve_bytes = 2ull << 30;
     o->queue_capacity = 4096;
@@ -392,9 +416,10 @@ mlem_status mlem_server_create(const mlem_server_opts* opts, mlem_server** out) 
         auto* s = new mlem_server();
         mlem_server_opts_default(&s->opts);
         if (opts) s->opts = *opts;
-        if (!(s->opts.slots_per_matrix == 8 || s->opts.slots_per_matrix == 16 || s->opts.slots_per_matrix == 32)) {
+        if (!(s->opts.slots_per_matrix == 0 || s->opts.slots_per_matrix == 8 || s->opts.slots_per_matrix == 16 ||
+              s->opts.slots_per_matrix == 32)) {
             delete s;
-            fail(MLEM_EINVAL, "slots_per_matrix must be 8, 16 or 32");
+            fail(MLEM_EINVAL, "slots_per_matrix must be 0 (autotuned), 8, 16 or 32");
         }
         cudaGetDevice(&s->device);
         if (s->opts.hbm_budget_bytes) {
@@ -417,11 +442,22 @@ mlem_status mlem_server_add_matrix(mlem_server* s, mlem_matrix* m, uint32_t* mat
         s->device = m->device;
         MatrixSlots ms;
         ms.m = m;
-        ms.tile = s->opts.slots_per_matrix;
+        DeviceGuard dg(m->device);
+        // slots per matrix: fixed by the options, or the batch tile the
+        // autotuner finds best for this matrix (the image tile of a large
+        // matrix should stay L2-resident)
+        ms.tile = s->opts.slots_per_matrix ? s->opts.slots_per_matrix : autotune_tile(m, m->stream);
         ms.slot_req.assign(ms.tile, 0);
         ms.slot_left.assign(ms.tile, 0);
-        DeviceGuard dg(m->device);
-        MLEM_CUDA(cudaStreamCreateWithFlags(&ms.stream, cudaStreamNonBlocking));
+        // smaller matrices get higher stream priority, so their short
+        // iterations are scheduled ahead of the CTAs of large ones
+        int least = 0, greatest = 0;
+        MLEM_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        int prio = least;
+        if (m->A.nnz < (16ull << 20)) prio = greatest;
+        else if (m->A.nnz < (512ull << 20)) prio = (least + greatest) / 2;
+        MLEM_CUDA(cudaStreamCreateWithPriority(&ms.stream, cudaStreamNonBlocking, prio));
+        MLEM_CUDA(cudaEventCreateWithFlags(&ms.done, cudaEventDisableTiming));
         s->mats.push_back(std::move(ms));
         *matrix_id = (uint32_t)(s->mats.size() - 1);
     });
@@ -531,6 +567,7 @@ mlem_status mlem_server_destroy(mlem_server* s) {
         for (auto& ms : s->mats) {
             if (ms.stream) cudaStreamSynchronize(ms.stream);
             ms.bs.release();
+            if (ms.done) cudaEventDestroy(ms.done);
             if (ms.stream) cudaStreamDestroy(ms.stream);
         }
         delete s;

@@ -279,6 +279,24 @@ def run_forms(pkg, torch, args):
         b.synchronize()
         res[label] = {"images_iterations_per_s": iters / (a.elapsed_time(b) * 1e-3)}
     m16.close()
+    # plain FP32 on the smaller matrices (the baselines of the batched and served forms)
+    for small in ("cyl3d_mid", "ring2d"):
+        msm, _, gs, _ = make_problem(pkg, small, torch, interleave=False)
+        gsd = torch.from_numpy(gs).cuda()
+        f0s = torch.from_numpy(np.full(msm.cols, msm.initial_value(gs), np.float32)).cuda()
+        fs = torch.empty_like(f0s)
+        its = WORKLOADS[small]["iters"]
+        fs.copy_(f0s)
+        msm.run_device(gsd.data_ptr(), fs.data_ptr(), its, stream=s.cuda_stream)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(3):
+            fs.copy_(f0s)
+            msm.run_device(gsd.data_ptr(), fs.data_ptr(), its, stream=s.cuda_stream)
+        b.record(s)
+        b.synchronize()
+        res[f"fp32_plain_{small}"] = {"images_iterations_per_s": 3 * its / (a.elapsed_time(b) * 1e-3)}
+        msm.close()
     # batched: the mid-size matrix with FP16 values, 64 sinograms, uneven iterations
     mb = pkg.Matrix.generate(pkg.preset("cyl3d_mid"), value_type=pkg.VAL_F16)
     rng = np.random.Generator(np.random.PCG64(7))
@@ -297,9 +315,86 @@ def run_forms(pkg, torch, args):
     _, st = mb.batch_run(G, its, stats=True)
     res["batched_fp16_64"] = {"images_iterations_per_s": float(its.sum()) / st["seconds_iterations"],
                               "wall_images_iterations_per_s": float(its.sum()) / st["seconds_total"],
-                              "workload": "cyl3d_mid fp16, 64 sinograms, iterations U{10..200}"}
+                              "workload": "cyl3d_mid fp16, 64 sinograms, iterations U{10..200}",
+                              "vs_fp32_plain_same_matrix": float(its.sum()) / st["seconds_iterations"]
+                              / res["fp32_plain_cyl3d_mid"]["images_iterations_per_s"]}
     mb.close()
     return res
+
+
+def run_serving(pkg, torch, n_requests=300, rate=50.0, fp32_iter_s=None):
+    """Serving form: three resident matrices (2-D ring FP32, 3-D mid FP32,
+    12 GB class FP16), Poisson arrivals, continuous batching in the server."""
+    import threading as th
+    from mlem_gb300 import synth
+    s = torch.cuda.current_stream()
+    specs = [("ring2d", pkg.VAL_F32, 0.5), ("cyl3d_mid", pkg.VAL_F32, 0.35), ("cyl3d_12gb", pkg.VAL_F16, 0.15)]
+    mats, expect = [], []
+    for name, vt, _ in specs:
+        geo = pkg.preset(name)
+        m = pkg.Matrix.generate(geo, value_type=vt)
+        dz = torch.zeros(m.rows, dtype=torch.int32, device="cuda")
+        ratio = torch.zeros(m.rows, dtype=torch.float32, device="cuda")
+        fp = torch.zeros(m.rows, dtype=torch.float32, device="cuda")
+        ex = []
+        for k in range(4):  # four phantoms per matrix; requests rescale their counts
+            xt = torch.from_numpy(synth.phantom(geo, WORKLOADS[name]["shapes"], seed=3000 + k)).cuda()
+            m.forward_project(xt.data_ptr(), dz.data_ptr(), ratio.data_ptr(), fp.data_ptr(), stream=s.cuda_stream,
+                              kernel=0)
+            ex.append(fp.cpu().numpy().astype(np.float64))
+        mats.append(m)
+        expect.append(ex)
+    rng = np.random.Generator(np.random.PCG64(11))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    which = rng.choice(3, size=n_requests, p=[p for _, _, p in specs])
+    totals = np.exp(rng.uniform(np.log(1e5), np.log(1e9), n_requests))
+    iters = rng.integers(20, 101, n_requests)
+    sinos = [synth.poisson_sinogram(expect[w][i % 4], totals[i], seed=5000 + i) for i, w in enumerate(which)]
+    lat = [None] * n_requests
+    with pkg.Server() as srv:
+        ids = [srv.add_matrix(m) for m in mats]
+        # warm-up: one request per matrix (graphs captured, slot states allocated)
+        for j in range(3):
+            srv.wait(srv.submit(ids[j], sinos[int(np.argmax(which == j))], 2))
+        rids = [None] * n_requests
+        t0 = time.perf_counter()
+
+        def submitter():
+            for i in range(n_requests):
+                d = t0 + arrivals[i] - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                rids[i] = srv.submit(ids[which[i]], sinos[i], int(iters[i]))
+
+        st = th.Thread(target=submitter)
+        st.start()
+        for i in range(n_requests):
+            while rids[i] is None:
+                time.sleep(0.0005)
+            _, lat[i] = srv.wait(rids[i])
+        st.join()
+        wall = time.perf_counter() - t0
+        stats = srv.stats()
+    lat = np.array(lat)
+    for m in mats:
+        m.close()
+    out = {"requests": n_requests, "arrival_rate_per_s": rate, "p50_latency_s": float(np.percentile(lat, 50)),
+           "p99_latency_s": float(np.percentile(lat, 99)), "mean_latency_s": float(lat.mean()),
+           "reconstructions_per_s": n_requests / wall, "wall_s": wall,
+           "iterations_done": int(stats["iterations_done"]),
+           "mix": "ring2d fp32 0.5 / cyl3d_mid fp32 0.35 / cyl3d_12gb fp16 0.15, counts log-U[1e5,1e9], "
+                  "iterations U{20..100}, autotuned slots per matrix, stream priority by matrix size"}
+    for j, (name, _, _) in enumerate(specs):
+        sel = which == j
+        if sel.any():
+            out[f"p50_latency_s_{name}"] = float(np.percentile(lat[sel], 50))
+            out[f"p99_latency_s_{name}"] = float(np.percentile(lat[sel], 99))
+    if fp32_iter_s:
+        # serial plain FP32 execution of the same request mix: one reconstruction at a time
+        serial_s = sum(float(iters[i]) / fp32_iter_s[specs[which[i]][0]] for i in range(n_requests))
+        out["serial_fp32_reconstructions_per_s"] = n_requests / serial_s
+        out["serial_fp32_busy_s"] = serial_s
+    return out
 
 
 def main():
@@ -427,6 +522,11 @@ def main():
     if args.forms == "all":
         line["forms"] = run_forms(pkg, torch, args)
         line["forms"]["fp32_plain"] = {"images_iterations_per_s": value / world}
+        rates = {name: value / world, "cyl3d_mid": line["forms"].get("fp32_plain_cyl3d_mid", {}).get(
+            "images_iterations_per_s"), "ring2d": line["forms"].get("fp32_plain_ring2d", {}).get(
+            "images_iterations_per_s")}
+        if all(rates.values()):
+            line["forms"]["serving"] = run_serving(pkg, torch, fp32_iter_s=rates)
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(pkg, name, WORKLOADS[name]["cpu_stride"])
         full_nnz = line["config"]["nnz"]

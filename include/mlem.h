@@ -342,7 +342,8 @@ mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g,
 typedef struct mlem_server mlem_server;
 
 typedef struct {
-    uint32_t slots_per_matrix;  /* concurrent reconstructions per matrix (batch tile) */
+    uint32_t slots_per_matrix;  /* concurrent reconstructions per matrix (batch tile 8/16/32,
+                                   0 = the tile the batch autotuner picks for each matrix) */
     uint64_t hbm_budget_bytes;  /* admission limit for per-request state (0 = free HBM - reserve) */
     uint64_t hbm_reserve_bytes; /* HBM kept free when hbm_budget_bytes == 0 */
     uint32_t queue_capacity;    /* max queued requests before submit returns EBUSY */
