@@ -25,7 +25,7 @@ LIB_PATH = PKG / "lib" / "libmlem_gb300.so"
 CLI_PATH = PKG / "bin" / "mlem_gb300"
 
 SPMV_MERGE, SPMV_CSR_VECTOR = 0, 1
-KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO, KERNEL_D16, KERNEL_ILV = 0, 1, 2, 3, 4, 5
+KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO, KERNEL_D16, KERNEL_ILV, KERNEL_ORDERED = 0, 1, 2, 3, 4, 5, 6
 VAL_F32, VAL_F16, VAL_BF16 = 0, 1, 2
 BP_TRANS, BP_SCATTER, BP_FUSED = 0, 1, 2
 
@@ -118,7 +118,7 @@ _SIGS = {
     "mlem_matrix_destroy": (C.c_int, [_P]),
     "mlem_matrix_get_info": (C.c_int, [_P, _P]),
     "mlem_matrix_get_norm": (C.c_int, [_P, _P]),
-    "mlem_matrix_get_tuning": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P]),
+    "mlem_matrix_get_tuning": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P, _P]),
     "mlem_matrix_get_transpose": (C.c_int, [_P, _P, _P, _P]),
     "mlem_matrix_get_csr": (C.c_int, [_P, _P, _P, _P]),
     "mlem_matrix_generate": (C.c_int, [_P, _P, _P]),
@@ -342,12 +342,12 @@ class Matrix:
 
     def tuning(self, transposed=False) -> dict:
         """The csr-vector configuration the autotuner chose for A or Aᵀ."""
-        k, ln, u, ms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
+        k, ln, u, od, ms = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_float()
         _check(load_library().mlem_matrix_get_tuning(self._h, int(transposed), C.byref(k), C.byref(ln),
-                                                     C.byref(u), C.byref(ms)))
+                                                     C.byref(u), C.byref(od), C.byref(ms)))
         names = {0: "direct", 1: "tma", 2: "persistent", 4: "d16", 5: "ilv"}
         return {"kernel": names.get(k.value, k.value), "lanes_per_row": ln.value, "vectors_in_flight": u.value,
-                "ms": ms.value}
+                "locality_order": bool(od.value), "ms": ms.value}
 
     def transpose(self):
         cp = np.zeros(self.cols + 1, np.uint64)

@@ -121,6 +121,9 @@ struct DevCsr {
     uint16_t* d16 = nullptr;     // [padded(nnz)]
     uint32_t* esc = nullptr;     // [nesc]
     uint64_t nesc = 0;
+    // optional processing order of the rows (locality of the gathers); the
+    // k-th row group handles row order[k].  Results are written per row.
+    uint32_t* order = nullptr;   // [nrows]
     // optional lane-interleaved copy (spmv_ilv.cu)
     uint32_t* idx_ilv = nullptr; // [ilv_len]
     void* val_ilv = nullptr;     // [ilv_len]

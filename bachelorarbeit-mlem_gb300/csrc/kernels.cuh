@@ -4,6 +4,8 @@
 
 #include "common.cuh"
 
+#include <vector>
+
 namespace mlem {
 
 // L2 persisting window for the gathered vector of one launch (0 bytes = none).
@@ -32,7 +34,7 @@ struct EpiArgs {
 // Rows of `op` times x, one group of `lanes` (8/16/32) threads per row,
 // 128-bit loads of indices and values, deterministic reduction order.
 void launch_csrvec(const DevCsr& op, const float* x, const EpiArgs& epi, int lanes,
-                   L2Window win, cudaStream_t s, int unroll = 2);
+                   L2Window win, cudaStream_t s, int unroll = 2, bool ordered = false);
 // Lane-interleaved copy (elements permuted inside 128-blocks) and its projection.
 void build_ilv(DevCsr& op, cudaStream_t s);
 void launch_csr_ilv(const DevCsr& op, const float* x, const EpiArgs& epi, int unroll, L2Window win,
@@ -109,6 +111,10 @@ uint64_t siddon_rows(const mlem_geometry& geo);
 void siddon_count_host(const mlem_geometry& geo, uint64_t* rowptr);
 void siddon_fill_host(const mlem_geometry& geo, const uint64_t* rowptr, uint32_t* col, float* val);
 void siddon_generate_device(const mlem_geometry& geo, DevCsr& A, cudaStream_t s);
+// Locality-friendly processing orders for a generated matrix: LORs in 4x4
+// detector tubes (rows of A) and voxels in 4x2x2 bricks (rows of Aᵀ).
+std::vector<uint32_t> siddon_lor_order(const mlem_geometry& geo);
+std::vector<uint32_t> voxel_brick_order(uint32_t nx, uint32_t ny, uint32_t nz);
 
 // ------------------------------------------------------------- batch.cu
 // Interleaved batch state: slot b of voxel c is f[c*tile + b]; g and ratio

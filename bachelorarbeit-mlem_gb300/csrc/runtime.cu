@@ -87,6 +87,7 @@ static void free_csr(DevCsr& c) {
     cudaFree(c.esc);
     cudaFree(c.idx_ilv);
     cudaFree(c.val_ilv);
+    cudaFree(c.order);
     c = DevCsr();
 }
 
@@ -96,6 +97,7 @@ static uint64_t csr_bytes(const DevCsr& c) {
                  val_bytes(c.vt) * padded(c.nnz);
     if (c.d16) b += sizeof(uint64_t) * c.nrows + sizeof(uint16_t) * padded(c.nnz) + sizeof(uint32_t) * c.nesc;
     if (c.idx_ilv) b += (sizeof(uint32_t) + val_bytes(c.vt)) * c.ilv_len;
+    if (c.order) b += sizeof(uint32_t) * c.nrows;
     return b;
 }
 
@@ -128,8 +130,8 @@ const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
 
 
 void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o) {
-    MLEM_REQUIRE(o.kernel <= MLEM_KERNEL_ILV, MLEM_EINVAL,
-                 "kernel must be 0 (direct), 1 (tma), 2 (persistent), 3 (auto), 4 (d16) or 5 (ilv)");
+    MLEM_REQUIRE(o.kernel <= MLEM_KERNEL_ORDERED, MLEM_EINVAL,
+                 "kernel must be 0 direct, 1 tma, 2 persistent, 3 auto, 4 d16, 5 ilv or 6 ordered");
     MLEM_REQUIRE(o.spmv == MLEM_SPMV_MERGE || o.spmv == MLEM_SPMV_CSR_VECTOR, MLEM_EINVAL,
                  "spmv must be 0 (merge-based) or 1 (csr-vector)");
     MLEM_REQUIRE(o.bp_mode == MLEM_BP_TRANS || o.bp_mode == MLEM_BP_SCATTER || o.bp_mode == MLEM_BP_FUSED,
@@ -165,7 +167,7 @@ static void launch_cfg(mlem_matrix* m, const DevCsr& op, const float* x, const E
     } else if (c.kind == MLEM_KERNEL_PERSISTENT) {
         launch_csrvec_pf(op, x, e, win, s);
     } else {
-        launch_csrvec(op, x, e, c.lanes, win, s, c.unroll);
+        launch_csrvec(op, x, e, c.lanes, win, s, c.unroll, c.ordered);
     }
 }
 
@@ -179,8 +181,11 @@ static void tune_projection(mlem_matrix* m, bool transposed) {
     std::vector<ProjCfg> cand;
     const int base = pick_lanes(op.nnz, op.nrows);
     for (int lanes : {base / 2, base, base * 2})
-        if (lanes >= 4 && lanes <= 32)
-            for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_DIRECT, lanes, u, 0.f});
+        if (lanes >= 4 && lanes <= 32) {
+            for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_DIRECT, lanes, u, 0.f, false});
+            if (op.order && lanes >= 16)
+                for (int u : {1, 2}) cand.push_back(ProjCfg{MLEM_KERNEL_DIRECT, lanes, u, 0.f, true});
+        }
     if (base == 32) cand.push_back(ProjCfg{MLEM_KERNEL_PERSISTENT, 32, 2, 0.f});
     cand.push_back(ProjCfg{MLEM_KERNEL_TMA, 32, 2, 0.f});
     if (op.d16) cand.push_back(ProjCfg{MLEM_KERNEL_D16, 32, 1, 0.f});
@@ -258,6 +263,12 @@ void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, 
     } else if (o.kernel == MLEM_KERNEL_D16) {
         MLEM_REQUIRE(op.d16 != nullptr, MLEM_EINVAL, "kernel D16 needs a matrix created with compress_indices = 1");
         c.kind = MLEM_KERNEL_D16;
+    } else if (o.kernel == MLEM_KERNEL_ORDERED) {
+        MLEM_REQUIRE(op.order != nullptr, MLEM_EINVAL, "kernel ORDERED needs a generated matrix (row orders)");
+        c.kind = MLEM_KERNEL_DIRECT;
+        c.lanes = 32;
+        c.unroll = 2;
+        c.ordered = true;
     } else if (o.kernel == MLEM_KERNEL_ILV) {
         MLEM_REQUIRE(op.idx_ilv != nullptr, MLEM_EINVAL, "kernel ILV needs a matrix created with interleave = 1");
         c.kind = MLEM_KERNEL_ILV;
@@ -570,6 +581,14 @@ mlem_status mlem_matrix_generate(const mlem_geometry* geo, const mlem_matrix_opt
             siddon_generate_device(*geo, m->A, m->stream);
             MLEM_REQUIRE(m->A.nrows >= 1, MLEM_EINVAL, "geometry produced no rows");
             postprocess_matrix(m, o);
+            // locality orders of the rows: LOR tubes for A, voxel bricks for Aᵀ
+            auto upload = [&](DevCsr& op, const std::vector<uint32_t>& ord) {
+                if (ord.size() != op.nrows || op.nrows == 0) return;
+                MLEM_CUDA(cudaMalloc(&op.order, sizeof(uint32_t) * ord.size()));
+                MLEM_CUDA(cudaMemcpy(op.order, ord.data(), sizeof(uint32_t) * ord.size(), cudaMemcpyHostToDevice));
+            };
+            upload(m->A, siddon_lor_order(*geo));
+            if (m->has_t) upload(m->AT, voxel_brick_order(geo->nx, geo->ny, geo->nz));
         } catch (...) {
             destroy_matrix(m);
             throw;
@@ -597,9 +616,9 @@ mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info) {
 }
 
 mlem_status mlem_matrix_get_tuning(mlem_matrix* m, uint32_t transposed, int* kernel, int* lanes, int* unroll,
-                                   float* ms) {
+                                   int* ordered, float* ms) {
     return guarded([&] {
-        MLEM_REQUIRE(m && kernel && lanes && unroll && ms, MLEM_EINVAL, "NULL argument");
+        MLEM_REQUIRE(m && kernel && lanes && unroll && ordered && ms, MLEM_EINVAL, "NULL argument");
         MLEM_REQUIRE(transposed <= 1, MLEM_EINVAL, "transposed must be 0 or 1");
         MLEM_REQUIRE(!transposed || m->has_t, MLEM_EINVAL, "matrix has no transpose");
         std::lock_guard<std::mutex> lk(m->mu);
@@ -609,6 +628,7 @@ mlem_status mlem_matrix_get_tuning(mlem_matrix* m, uint32_t transposed, int* ker
         *kernel = c.kind;
         *lanes = c.lanes;
         *unroll = c.unroll;
+        *ordered = c.ordered ? 1 : 0;
         *ms = c.ms;
     });
 }

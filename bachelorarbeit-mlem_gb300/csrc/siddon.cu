@@ -393,6 +393,39 @@ void siddon_fill_host(const mlem_geometry& g, const uint64_t* rowptr, uint32_t* 
     }
 }
 
+std::vector<uint32_t> siddon_lor_order(const mlem_geometry& g) {
+    check_geo(g);
+    const Geo G = make_geo(g);
+    std::vector<uint32_t> ord;
+    if (G.stride != 1) return ord;  // sampled matrices keep their order
+    ord.reserve(G.nrows);
+    const uint32_t T = 4;
+    for (uint32_t ra = 0; ra < G.rings; ++ra)
+        for (uint32_t rb = ra; rb < G.rings; ++rb)
+            for (uint32_t i = 0; i < G.dpr; i += T)
+                for (uint32_t j = 0; j < G.dpr; j += T)
+                    for (uint32_t ka = i; ka < std::min(i + T, G.dpr); ++ka)
+                        for (uint32_t kb = j; kb < std::min(j + T, G.dpr); ++kb) {
+                            const uint64_t a = (uint64_t)ra * G.dpr + ka, b = (uint64_t)rb * G.dpr + kb;
+                            if (a < b) ord.push_back((uint32_t)(lor_start(a, G.D) + (b - a - 1)));
+                        }
+    return ord;
+}
+
+std::vector<uint32_t> voxel_brick_order(uint32_t nx, uint32_t ny, uint32_t nz) {
+    std::vector<uint32_t> ord;
+    ord.reserve((uint64_t)nx * ny * nz);
+    const uint32_t bx = 4, by = 2, bz = 2;
+    for (uint32_t z0 = 0; z0 < nz; z0 += bz)
+        for (uint32_t y0 = 0; y0 < ny; y0 += by)
+            for (uint32_t x0 = 0; x0 < nx; x0 += bx)
+                for (uint32_t z = z0; z < std::min(z0 + bz, nz); ++z)
+                    for (uint32_t y = y0; y < std::min(y0 + by, ny); ++y)
+                        for (uint32_t x = x0; x < std::min(x0 + bx, nx); ++x)
+                            ord.push_back(x + nx * (y + ny * z));
+    return ord;
+}
+
 void siddon_generate_device(const mlem_geometry& g, DevCsr& A, cudaStream_t s) {
     check_geo(g);
     const Geo G = make_geo(g);

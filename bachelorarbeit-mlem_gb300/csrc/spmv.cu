@@ -105,22 +105,24 @@ __device__ __forceinline__ void epi_update(uint32_t c, float sum, float* __restr
     f[c] = (n == 0.0f) ? t : __fdiv_rn(t, n);
 }
 
-template <typename V, int LPR, int EPI, int U>
+template <typename V, int LPR, int EPI, int U, bool ORD>
 __global__ void __launch_bounds__(256)
 k_csrvec(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
          const V* __restrict__ val, const float* __restrict__ x, uint32_t nrows,
          const int32_t* __restrict__ g, float* __restrict__ out, float* __restrict__ fwproj,
-         float* __restrict__ f, const float* __restrict__ norm) {
+         float* __restrict__ f, const float* __restrict__ norm, const uint32_t* __restrict__ order) {
     const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t row = gt / LPR;
+    const uint32_t k = gt / LPR;
     const int sub = threadIdx.x & (LPR - 1);
     float acc = 0.f;
-    if (row < nrows) {
+    uint32_t row = k;
+    if (k < nrows) {
+        if (ORD) row = __ldg(order + k);
         const uint64_t s = rowptr[row], t = rowptr[row + 1];
         acc = lane_dot<V, LPR, U>(idx, val, x, s, t, sub);
     }
     acc = group_sum<LPR>(acc);
-    if (sub == 0 && row < nrows) {
+    if (sub == 0 && k < nrows) {
         if (EPI == (int)Epi::Correl) epi_correl(row, acc, g, out, fwproj);
         else if (EPI == (int)Epi::Update) epi_update(row, acc, f, norm);
         else out[row] = acc;
@@ -297,26 +299,27 @@ __global__ void __launch_bounds__(1024) k_reduce_f64(const double* __restrict__ 
     if (threadIdx.x == 0) *out = tot;
 }
 
-template <typename V, int LPR, int U>
+template <typename V, int LPR, int U, bool ORD>
 void csrvec_dispatch_epi(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win,
                          cudaStream_t s) {
     const uint64_t threads = (uint64_t)op.nrows * LPR;
     const dim3 grid(ceil_div_u(threads, 256)), block(256);
     const V* val = static_cast<const V*>(op.val);
+    const uint32_t* ord = op.order;
     switch (e.kind) {
         case Epi::Correl:
-            launch_ex(k_csrvec<V, LPR, (int)Epi::Correl, U>, grid, block, 0, s, win, op.rowptr, op.idx,
-                      val, x, op.nrows, e.g, e.out, e.fwproj, (float*)nullptr, (const float*)nullptr);
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Correl, U, ORD>, grid, block, 0, s, win, op.rowptr, op.idx,
+                      val, x, op.nrows, e.g, e.out, e.fwproj, (float*)nullptr, (const float*)nullptr, ord);
             break;
         case Epi::Update:
-            launch_ex(k_csrvec<V, LPR, (int)Epi::Update, U>, grid, block, 0, s, win, op.rowptr, op.idx,
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Update, U, ORD>, grid, block, 0, s, win, op.rowptr, op.idx,
                       val, x, op.nrows, (const int32_t*)nullptr, (float*)nullptr, (float*)nullptr,
-                      e.f, e.norm);
+                      e.f, e.norm, ord);
             break;
         default:
-            launch_ex(k_csrvec<V, LPR, (int)Epi::Raw, U>, grid, block, 0, s, win, op.rowptr, op.idx,
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Raw, U, ORD>, grid, block, 0, s, win, op.rowptr, op.idx,
                       val, x, op.nrows, (const int32_t*)nullptr, e.out, (float*)nullptr,
-                      (float*)nullptr, (const float*)nullptr);
+                      (float*)nullptr, (const float*)nullptr, ord);
     }
 }
 
@@ -352,20 +355,25 @@ void pf_dispatch(const DevCsr& op, const float* x, const EpiArgs& e, L2Window wi
 }
 
 template <typename V, int LPR>
-void csrvec_dispatch_u(const DevCsr& op, const float* x, const EpiArgs& e, int unroll, L2Window win,
-                       cudaStream_t s) {
-    if (unroll >= 4) csrvec_dispatch_epi<V, LPR, 4>(op, x, e, win, s);
-    else if (unroll == 2) csrvec_dispatch_epi<V, LPR, 2>(op, x, e, win, s);
-    else csrvec_dispatch_epi<V, LPR, 1>(op, x, e, win, s);
+void csrvec_dispatch_u(const DevCsr& op, const float* x, const EpiArgs& e, int unroll, bool ordered,
+                       L2Window win, cudaStream_t s) {
+    if (ordered && op.order && LPR >= 16) {
+        if (unroll >= 2) csrvec_dispatch_epi<V, LPR, 2, true>(op, x, e, win, s);
+        else csrvec_dispatch_epi<V, LPR, 1, true>(op, x, e, win, s);
+        return;
+    }
+    if (unroll >= 4) csrvec_dispatch_epi<V, LPR, 4, false>(op, x, e, win, s);
+    else if (unroll == 2) csrvec_dispatch_epi<V, LPR, 2, false>(op, x, e, win, s);
+    else csrvec_dispatch_epi<V, LPR, 1, false>(op, x, e, win, s);
 }
 
 template <typename V>
 void csrvec_dispatch_lanes(const DevCsr& op, const float* x, const EpiArgs& e, int lanes, int unroll,
-                           L2Window win, cudaStream_t s) {
-    if (lanes >= 32) csrvec_dispatch_u<V, 32>(op, x, e, unroll, win, s);
-    else if (lanes >= 16) csrvec_dispatch_u<V, 16>(op, x, e, unroll, win, s);
-    else if (lanes >= 8) csrvec_dispatch_u<V, 8>(op, x, e, unroll, win, s);
-    else csrvec_dispatch_u<V, 4>(op, x, e, unroll, win, s);
+                           bool ordered, L2Window win, cudaStream_t s) {
+    if (lanes >= 32) csrvec_dispatch_u<V, 32>(op, x, e, unroll, ordered, win, s);
+    else if (lanes >= 16) csrvec_dispatch_u<V, 16>(op, x, e, unroll, ordered, win, s);
+    else if (lanes >= 8) csrvec_dispatch_u<V, 8>(op, x, e, unroll, false, win, s);
+    else csrvec_dispatch_u<V, 4>(op, x, e, unroll, false, win, s);
 }
 
 template <typename V>
@@ -393,12 +401,12 @@ int pick_lanes(uint64_t nnz, uint32_t rows) {
 }
 
 void launch_csrvec(const DevCsr& op, const float* x, const EpiArgs& epi, int lanes, L2Window win,
-                   cudaStream_t s, int unroll) {
+                   cudaStream_t s, int unroll, bool ordered) {
     if (op.nrows == 0) return;
     switch (op.vt) {
-        case MLEM_VAL_F32: csrvec_dispatch_lanes<float>(op, x, epi, lanes, unroll, win, s); break;
-        case MLEM_VAL_F16: csrvec_dispatch_lanes<__half>(op, x, epi, lanes, unroll, win, s); break;
-        default: csrvec_dispatch_lanes<__nv_bfloat16>(op, x, epi, lanes, unroll, win, s);
+        case MLEM_VAL_F32: csrvec_dispatch_lanes<float>(op, x, epi, lanes, unroll, ordered, win, s); break;
+        case MLEM_VAL_F16: csrvec_dispatch_lanes<__half>(op, x, epi, lanes, unroll, ordered, win, s); break;
+        default: csrvec_dispatch_lanes<__nv_bfloat16>(op, x, epi, lanes, unroll, ordered, win, s);
     }
 }
 

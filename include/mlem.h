@@ -114,10 +114,10 @@ typedef struct {
 mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info);
 /* Configuration the autotuner chose for the csr-vector projection of A
  * (transposed = 0) or Aᵀ (1): kernel (mlem_kernel), lanes per row, vectors in
- * flight per lane and the measured milliseconds of one launch.  Tunes on
- * first call if needed. */
+ * flight per lane, whether rows run in locality order, and the measured
+ * milliseconds of one launch.  Tunes on first call if needed. */
 mlem_status mlem_matrix_get_tuning(mlem_matrix* m, uint32_t transposed, int* kernel, int* lanes,
-                                   int* unroll, float* ms);
+                                   int* unroll, int* ordered, float* ms);
 /* Copies the sensitivity image (f32[cols]) to the host. */
 mlem_status mlem_matrix_get_norm(const mlem_matrix* m, float* norm_out);
 /* Copies the device-built transpose to the host: colptr u64[cols+1],
@@ -150,7 +150,9 @@ typedef enum {
     MLEM_KERNEL_PERSISTENT = 2,
     MLEM_KERNEL_AUTO = 3, /* autotuned per matrix operand (lanes per row, vectors in flight, variant) */
     MLEM_KERNEL_D16 = 4,  /* delta-compressed indices (matrix created with compress_indices = 1) */
-    MLEM_KERNEL_ILV = 5   /* lane-interleaved copy (matrix created with interleave = 1) */
+    MLEM_KERNEL_ILV = 5,  /* lane-interleaved copy (matrix created with interleave = 1) */
+    MLEM_KERNEL_ORDERED = 6 /* DIRECT with rows in locality order (generated matrices:
+                               LORs in 4x4 detector tubes, voxels in 4x2x2 bricks) */
 } mlem_kernel;
 
 /* Defaults: CSR_VECTOR, BP_TRANS, secsize 5/5, graphs on, no log-likelihood, L2 window on,

@@ -340,3 +340,22 @@ def test_interleaved_and_compressed_mlem(pkg, O):
     fp_cfg, bp_cfg = m.tuning(False), m.tuning(True)
     assert fp_cfg["ms"] > 0 and bp_cfg["ms"] > 0
     m.close()
+
+
+@pytest.mark.parametrize("name", ["ring2d", "cyl3d_tiny"])
+def test_generated_matrix_locality_order(pkg, O, name):
+    """Rows processed in LOR-tube / voxel-brick order give the same image."""
+    geo = pkg.preset(name, sub_t=4, sub_z=2, width_t=6.0, width_z=2.0) if name == "cyl3d_tiny" else pkg.preset(name)
+    rp, c, v, cols = pkg.siddon_host(geo)
+    from mlem_gb300 import synth
+    g = synth.poisson_sinogram(synth.project_host(rp, c, v, synth.phantom(geo, 4, seed=9)), 1e6, seed=10)
+    m = pkg.Matrix.generate(geo)
+    norm = m.norm()
+    f0 = np.full(cols, m.initial_value(g), np.float32)
+    ref64 = O.mlem_f64((rp, c, v), g, norm, f0, 15)
+    for kern in (pkg.KERNEL_ORDERED, pkg.KERNEL_AUTO):
+        got = m.run(g, 15, f0=f0, kernel=kern)
+        assert O.rel_l2(got, ref64) < TOL_F32, kern
+    t = m.tuning(False)
+    assert set(t) >= {"kernel", "lanes_per_row", "vectors_in_flight", "locality_order", "ms"}
+    m.close()
