@@ -60,7 +60,8 @@ class MatrixInfo(C.Structure):
 class RunOpts(C.Structure):
     _fields_ = [("spmv", C.c_int), ("bp_mode", C.c_int), ("secsize_fp", C.c_uint32),
                 ("secsize_bp", C.c_uint32), ("use_graph", C.c_uint32), ("loglik_every", C.c_uint32),
-                ("l2_window", C.c_uint32), ("kernel", C.c_uint32)]
+                ("l2_window", C.c_uint32), ("kernel", C.c_uint32), ("lanes", C.c_uint32), ("unroll", C.c_uint32),
+                ("row_order", C.c_uint32), ("pipeline", C.c_uint32)]
 
 
 class Stats(C.Structure):
@@ -118,7 +119,7 @@ _SIGS = {
     "mlem_matrix_destroy": (C.c_int, [_P]),
     "mlem_matrix_get_info": (C.c_int, [_P, _P]),
     "mlem_matrix_get_norm": (C.c_int, [_P, _P]),
-    "mlem_matrix_get_tuning": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P, _P]),
+    "mlem_matrix_get_tuning": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P, _P, _P]),
     "mlem_matrix_get_transpose": (C.c_int, [_P, _P, _P, _P]),
     "mlem_matrix_get_csr": (C.c_int, [_P, _P, _P, _P]),
     "mlem_matrix_generate": (C.c_int, [_P, _P, _P]),
@@ -238,6 +239,11 @@ def preset(name: str, row_stride: int = 1, row_phase: int = 0, **over) -> Geomet
     return geometry(**kw, row_stride=row_stride, row_phase=row_phase)
 
 
+def siddon_rows(geo: Geometry) -> int:
+    """Number of LOR rows the geometry's matrix has (after its row stride)."""
+    return int(load_library().mlem_siddon_rows(C.byref(geo)))
+
+
 def siddon_host(geo: Geometry):
     """Generates the geometry's system matrix on the host (OpenMP).
 
@@ -342,12 +348,12 @@ class Matrix:
 
     def tuning(self, transposed=False) -> dict:
         """The csr-vector configuration the autotuner chose for A or Aᵀ."""
-        k, ln, u, od, ms = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_float()
+        k, ln, u, od, pp, ms = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_float()
         _check(load_library().mlem_matrix_get_tuning(self._h, int(transposed), C.byref(k), C.byref(ln),
-                                                     C.byref(u), C.byref(od), C.byref(ms)))
+                                                     C.byref(u), C.byref(od), C.byref(pp), C.byref(ms)))
         names = {0: "direct", 1: "tma", 2: "persistent", 4: "d16", 5: "ilv"}
         return {"kernel": names.get(k.value, k.value), "lanes_per_row": ln.value, "vectors_in_flight": u.value,
-                "locality_order": bool(od.value), "ms": ms.value}
+                "locality_order": bool(od.value), "pipelined": bool(pp.value), "ms": ms.value}
 
     def transpose(self):
         cp = np.zeros(self.cols + 1, np.uint64)
@@ -372,12 +378,14 @@ class Matrix:
     # runs -------------------------------------------------------------------
     @staticmethod
     def run_opts(spmv=SPMV_CSR_VECTOR, bp_mode=BP_TRANS, secsize_fp=5, secsize_bp=5, use_graph=True,
-                 loglik_every=0, l2_window=True, kernel=KERNEL_AUTO) -> RunOpts:
+                 loglik_every=0, l2_window=True, kernel=KERNEL_AUTO, lanes=0, unroll=0,
+                 row_order=False, pipeline=False) -> RunOpts:
         o = RunOpts()
         load_library().mlem_run_opts_default(C.byref(o))
         o.spmv, o.bp_mode, o.secsize_fp, o.secsize_bp = spmv, bp_mode, secsize_fp, secsize_bp
         o.use_graph, o.loglik_every, o.l2_window = int(use_graph), loglik_every, int(l2_window)
-        o.kernel = int(kernel)
+        o.kernel, o.lanes, o.unroll, o.row_order = int(kernel), int(lanes), int(unroll), int(row_order)
+        o.pipeline = int(pipeline)
         return o
 
     def run(self, g, iterations: int, f0=None, loglik=False, stats=False, **opts):

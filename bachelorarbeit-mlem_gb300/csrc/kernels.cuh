@@ -31,10 +31,12 @@ struct EpiArgs {
     const float* norm = nullptr;  // Update
 };
 
-// Rows of `op` times x, one group of `lanes` (8/16/32) threads per row,
+// Rows of `op` times x, one group of `lanes` (4/8/16/32) threads per row,
 // 128-bit loads of indices and values, deterministic reduction order.
+// ordered: rows in op.order; pipelined: the next vectors are loaded before
+// the current gathers (both for 16 or 32 lanes; same results).
 void launch_csrvec(const DevCsr& op, const float* x, const EpiArgs& epi, int lanes,
-                   L2Window win, cudaStream_t s, int unroll = 2, bool ordered = false);
+                   L2Window win, cudaStream_t s, int unroll = 2, bool ordered = false, bool pipelined = false);
 // Lane-interleaved copy (elements permuted inside 128-blocks) and its projection.
 void build_ilv(DevCsr& op, cudaStream_t s);
 void launch_csr_ilv(const DevCsr& op, const float* x, const EpiArgs& epi, int unroll, L2Window win,
@@ -43,9 +45,13 @@ void launch_csr_ilv(const DevCsr& op, const float* x, const EpiArgs& epi, int un
 // the projection that reads them.
 void build_d16(DevCsr& op, cudaStream_t s);
 void launch_csr_d16(const DevCsr& op, const float* x, const EpiArgs& epi, L2Window win, cudaStream_t s);
-// Persistent warp-per-row variant that prefetches the next row's pointers.
-void prepare_csrvec_pf(mlem_value_type vt);
-void launch_csrvec_pf(const DevCsr& op, const float* x, const EpiArgs& epi, L2Window win, cudaStream_t s);
+// Persistent, software-pipelined csr-vector variant (16 or 32 lanes per row,
+// 1 or 2 vectors per lane and step, optional locality order); bit-identical
+// to launch_csrvec with the same lanes.  prepare_* settles the grid sizes
+// outside stream captures.
+void prepare_csrvec_pipe(mlem_value_type vt);
+void launch_csrvec_pipe(const DevCsr& op, const float* x, const EpiArgs& epi, int lanes, int unroll, bool ordered,
+                        L2Window win, cudaStream_t s);
 // Same product through the TMA-pipelined kernel (spmv_tma.cu); *err is set
 // when a bounded wait expires.  prepare_* settles attributes outside captures.
 void prepare_csr_tma(mlem_value_type vt);

@@ -132,6 +132,20 @@ const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
 void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o) {
     MLEM_REQUIRE(o.kernel <= MLEM_KERNEL_ORDERED, MLEM_EINVAL,
                  "kernel must be 0 direct, 1 tma, 2 persistent, 3 auto, 4 d16, 5 ilv or 6 ordered");
+    MLEM_REQUIRE(o.lanes == 0 || o.lanes == 4 || o.lanes == 8 || o.lanes == 16 || o.lanes == 32, MLEM_EINVAL,
+                 "lanes must be 0, 4, 8, 16 or 32");
+    MLEM_REQUIRE(o.unroll == 0 || o.unroll == 1 || o.unroll == 2 || o.unroll == 4, MLEM_EINVAL,
+                 "unroll must be 0, 1, 2 or 4");
+    MLEM_REQUIRE(o.kernel != MLEM_KERNEL_PERSISTENT || (o.lanes != 4 && o.lanes != 8 && o.unroll != 4),
+                 MLEM_EINVAL, "the persistent kernel takes 16 or 32 lanes and unroll 1 or 2");
+    MLEM_REQUIRE(o.row_order <= 1, MLEM_EINVAL, "row_order must be 0 or 1");
+    MLEM_REQUIRE(o.pipeline <= 1, MLEM_EINVAL, "pipeline must be 0 or 1");
+    MLEM_REQUIRE(!o.pipeline || o.lanes == 0 || o.lanes >= 16, MLEM_EINVAL, "pipeline needs 16 or 32 lanes");
+    const bool ordered = o.kernel == MLEM_KERNEL_ORDERED ||
+                         (o.row_order && (o.kernel == MLEM_KERNEL_DIRECT || o.kernel == MLEM_KERNEL_PERSISTENT));
+    MLEM_REQUIRE(!ordered || o.lanes == 0 || o.lanes >= 16, MLEM_EINVAL, "row order needs 16 or 32 lanes");
+    MLEM_REQUIRE(!ordered || o.spmv != MLEM_SPMV_CSR_VECTOR || m->A.order != nullptr, MLEM_EINVAL,
+                 "row order needs a generated matrix");
     MLEM_REQUIRE(o.spmv == MLEM_SPMV_MERGE || o.spmv == MLEM_SPMV_CSR_VECTOR, MLEM_EINVAL,
                  "spmv must be 0 (merge-based) or 1 (csr-vector)");
     MLEM_REQUIRE(o.bp_mode == MLEM_BP_TRANS || o.bp_mode == MLEM_BP_SCATTER || o.bp_mode == MLEM_BP_FUSED,
@@ -165,9 +179,9 @@ static void launch_cfg(mlem_matrix* m, const DevCsr& op, const float* x, const E
     } else if (c.kind == MLEM_KERNEL_ILV) {
         launch_csr_ilv(op, x, e, c.unroll, win, s);
     } else if (c.kind == MLEM_KERNEL_PERSISTENT) {
-        launch_csrvec_pf(op, x, e, win, s);
+        launch_csrvec_pipe(op, x, e, c.lanes, c.unroll, c.ordered, win, s);
     } else {
-        launch_csrvec(op, x, e, c.lanes, win, s, c.unroll, c.ordered);
+        launch_csrvec(op, x, e, c.lanes, win, s, c.unroll, c.ordered, c.pipelined);
     }
 }
 
@@ -182,16 +196,20 @@ static void tune_projection(mlem_matrix* m, bool transposed) {
     const int base = pick_lanes(op.nnz, op.nrows);
     for (int lanes : {base / 2, base, base * 2})
         if (lanes >= 4 && lanes <= 32) {
-            for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_DIRECT, lanes, u, 0.f, false});
-            if (op.order && lanes >= 16)
-                for (int u : {1, 2}) cand.push_back(ProjCfg{MLEM_KERNEL_DIRECT, lanes, u, 0.f, true});
+            for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_DIRECT, lanes, u, 0.f, false, false});
+            if (lanes >= 16)
+                for (int u : {1, 2})
+                    for (bool ord : {false, true})
+                        for (bool pipe : {false, true})
+                            if ((ord || pipe) && (!ord || op.order))
+                                cand.push_back(ProjCfg{MLEM_KERNEL_DIRECT, lanes, u, 0.f, ord, pipe});
         }
-    if (base == 32) cand.push_back(ProjCfg{MLEM_KERNEL_PERSISTENT, 32, 2, 0.f});
+    if (base >= 16) cand.push_back(ProjCfg{MLEM_KERNEL_PERSISTENT, base, 1, 0.f, false, false});
     cand.push_back(ProjCfg{MLEM_KERNEL_TMA, 32, 2, 0.f});
     if (op.d16) cand.push_back(ProjCfg{MLEM_KERNEL_D16, 32, 1, 0.f});
     if (op.idx_ilv)
         for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_ILV, 32, u, 0.f});
-    prepare_csrvec_pf(op.vt);
+    prepare_csrvec_pipe(op.vt);
     prepare_csr_tma(op.vt);
     ensure_workspace(m);
     float *x = nullptr, *y = nullptr;
@@ -238,7 +256,7 @@ static void tune_projection(mlem_matrix* m, bool transposed) {
 
 void prepare_kernel(mlem_matrix* m, const mlem_run_opts& o) {
     if (o.kernel == MLEM_KERNEL_TMA) prepare_csr_tma(m->vt);
-    else if (o.kernel == MLEM_KERNEL_PERSISTENT) prepare_csrvec_pf(m->vt);
+    else if (o.kernel == MLEM_KERNEL_PERSISTENT) prepare_csrvec_pipe(m->vt);
     else if (o.kernel == MLEM_KERNEL_AUTO) {
         tune_projection(m, false);
         if (m->has_t) tune_projection(m, true);
@@ -256,8 +274,11 @@ void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, 
     if (o.kernel == MLEM_KERNEL_AUTO) {
         MLEM_REQUIRE(m->tuned[transposed], MLEM_EINVAL, "internal: projection used before autotuning");
         c = m->proj[transposed];
-    } else if (o.kernel == MLEM_KERNEL_PERSISTENT && pick_lanes(op.nnz, op.nrows) == 32) {
+    } else if (o.kernel == MLEM_KERNEL_PERSISTENT && (o.lanes >= 16 || pick_lanes(op.nnz, op.nrows) >= 16)) {
         c.kind = MLEM_KERNEL_PERSISTENT;
+        c.lanes = o.lanes ? (int)o.lanes : pick_lanes(op.nnz, op.nrows);
+        c.unroll = o.unroll ? (int)o.unroll : 2;
+        c.ordered = o.row_order && op.order && c.lanes >= 16;
     } else if (o.kernel == MLEM_KERNEL_TMA) {
         c.kind = MLEM_KERNEL_TMA;
     } else if (o.kernel == MLEM_KERNEL_D16) {
@@ -266,17 +287,20 @@ void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, 
     } else if (o.kernel == MLEM_KERNEL_ORDERED) {
         MLEM_REQUIRE(op.order != nullptr, MLEM_EINVAL, "kernel ORDERED needs a generated matrix (row orders)");
         c.kind = MLEM_KERNEL_DIRECT;
-        c.lanes = 32;
-        c.unroll = 2;
+        c.lanes = o.lanes ? (int)o.lanes : 32;
+        c.unroll = o.unroll ? std::min<int>((int)o.unroll, 2) : 2;
         c.ordered = true;
+        c.pipelined = o.pipeline != 0;
     } else if (o.kernel == MLEM_KERNEL_ILV) {
         MLEM_REQUIRE(op.idx_ilv != nullptr, MLEM_EINVAL, "kernel ILV needs a matrix created with interleave = 1");
         c.kind = MLEM_KERNEL_ILV;
         c.unroll = 2;
     } else {
         c.kind = MLEM_KERNEL_DIRECT;
-        c.lanes = pick_lanes(op.nnz, op.nrows);
-        c.unroll = 2;
+        c.lanes = o.lanes ? (int)o.lanes : pick_lanes(op.nnz, op.nrows);
+        c.unroll = o.unroll ? (int)o.unroll : 2;
+        c.ordered = o.row_order && op.order && c.lanes >= 16;
+        c.pipelined = o.pipeline && c.lanes >= 16;
     }
     launch_cfg(m, op, x, e, c, win, s);
 }
@@ -354,7 +378,7 @@ static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cud
     constexpr uint32_t kChunk = 8;
     auto get_graph = [&](uint32_t chunk) -> cudaGraphExec_t {
         RunKey key{(int)o.spmv, (int)o.bp_mode, (int)o.secsize_fp, (int)o.secsize_bp, (int)o.l2_window,
-                   (int)chunk, (int)o.kernel};
+                   (int)chunk, (int)(o.kernel | o.lanes << 8 | o.unroll << 16 | o.row_order << 24 | o.pipeline << 25)};
         auto it = m->ws.graphs.find(key);
         if (it != m->ws.graphs.end()) return it->second;
         // plans and kernel attributes must exist before capture
@@ -390,7 +414,7 @@ static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cud
     auto replay = [&](uint32_t chunk, uint32_t times) {
         cudaGraphExec_t ge = get_graph(chunk);
         const RunKey key{(int)o.spmv, (int)o.bp_mode, (int)o.secsize_fp, (int)o.secsize_bp,
-                         (int)o.l2_window, (int)chunk, (int)o.kernel};
+                         (int)o.l2_window, (int)chunk, (int)(o.kernel | o.lanes << 8 | o.unroll << 16 | o.row_order << 24 | o.pipeline << 25)};
         const uint64_t nodes = m->ws.graph_nodes[key];
         for (uint32_t q = 0; q < times; ++q) {
             MLEM_CUDA(cudaGraphLaunch(ge, s));
@@ -545,6 +569,10 @@ void mlem_run_opts_default(mlem_run_opts* o) {
     o->loglik_every = 0;
     o->l2_window = 1;
     o->kernel = MLEM_KERNEL_AUTO;
+    o->lanes = 0;
+    o->unroll = 0;
+    o->row_order = 0;
+    o->pipeline = 0;
 }
 
 mlem_status mlem_matrix_create(const mlem_csr_host* csr, const mlem_matrix_opts* opts, mlem_matrix** out) {
@@ -616,9 +644,9 @@ mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info) {
 }
 
 mlem_status mlem_matrix_get_tuning(mlem_matrix* m, uint32_t transposed, int* kernel, int* lanes, int* unroll,
-                                   int* ordered, float* ms) {
+                                   int* ordered, int* pipelined, float* ms) {
     return guarded([&] {
-        MLEM_REQUIRE(m && kernel && lanes && unroll && ordered && ms, MLEM_EINVAL, "NULL argument");
+        MLEM_REQUIRE(m && kernel && lanes && unroll && ordered && pipelined && ms, MLEM_EINVAL, "NULL argument");
         MLEM_REQUIRE(transposed <= 1, MLEM_EINVAL, "transposed must be 0 or 1");
         MLEM_REQUIRE(!transposed || m->has_t, MLEM_EINVAL, "matrix has no transpose");
         std::lock_guard<std::mutex> lk(m->mu);
@@ -629,6 +657,7 @@ mlem_status mlem_matrix_get_tuning(mlem_matrix* m, uint32_t transposed, int* ker
         *lanes = c.lanes;
         *unroll = c.unroll;
         *ordered = c.ordered ? 1 : 0;
+        *pipelined = c.pipelined ? 1 : 0;
         *ms = c.ms;
     });
 }

@@ -104,7 +104,8 @@ struct ProjCfg {
     int lanes = 32;  // DIRECT: lanes per row
     int unroll = 2;  // DIRECT: 4-element vectors in flight per lane
     float ms = 0.f;  // measured time of one launch
-    bool ordered = false;  // DIRECT: rows in the operand's locality order
+    bool ordered = false;    // DIRECT / PERSISTENT: rows in the operand's locality order
+    bool pipelined = false;  // DIRECT: next vectors loaded before the current gathers
 };
 }  // namespace mlem
 

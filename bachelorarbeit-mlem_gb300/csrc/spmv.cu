@@ -82,6 +82,52 @@ __device__ __forceinline__ float lane_dot(const uint32_t* __restrict__ idx, cons
     return acc;
 }
 
+template <typename V, int LPR, int U>
+__device__ __forceinline__ void load_step(Vec4<V> (&p)[U], const uint4* __restrict__ idx4,
+                                          const V* __restrict__ val, uint64_t b, uint64_t v1, int sub) {
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+        const uint64_t v = b + sub + (uint64_t)q * LPR;
+        if (v < v1) p[q].load(idx4, val, v);
+    }
+}
+
+// Software-pipelined form of lane_dot: the U vectors of the next step are
+// loaded before the gathers of the current step, so the index/value stream
+// stays in flight while the gathers wait.  Same per-lane order of additions
+// as lane_dot (bit-identical results).
+template <typename V, int LPR, int U>
+__device__ __forceinline__ float lane_dot_pipe(const uint32_t* __restrict__ idx, const V* __restrict__ val,
+                                               const float* __restrict__ x, uint64_t s, uint64_t t, int sub) {
+    const uint4* idx4 = reinterpret_cast<const uint4*>(idx);
+    const uint64_t v1 = (t + 3) >> 2;
+    uint64_t b = s >> 2;
+    Vec4<V> cur[U];
+    load_step<V, LPR, U>(cur, idx4, val, b, v1, sub);
+    float acc = 0.f;
+    for (;;) {
+        const bool last = b + (uint64_t)U * LPR >= v1;
+        Vec4<V> nxt[U];
+        if (!last) load_step<V, LPR, U>(nxt, idx4, val, b + (uint64_t)U * LPR, v1, sub);
+        float gq[U][4];
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+            const uint64_t v = b + sub + (uint64_t)q * LPR;
+            if (v < v1) gather4(cur[q].c, v << 2, s, t, x, gq[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+            const uint64_t v = b + sub + (uint64_t)q * LPR;
+            if (v < v1) acc = fma4(acc, cur[q].a, gq[q], v << 2, s, t);
+        }
+        if (last) break;
+        b += (uint64_t)U * LPR;
+#pragma unroll
+        for (int q = 0; q < U; ++q) cur[q] = nxt[q];
+    }
+    return acc;
+}
+
 template <int LPR>
 __device__ __forceinline__ float group_sum(float acc) {
 #pragma unroll
@@ -105,7 +151,7 @@ __device__ __forceinline__ void epi_update(uint32_t c, float sum, float* __restr
     f[c] = (n == 0.0f) ? t : __fdiv_rn(t, n);
 }
 
-template <typename V, int LPR, int EPI, int U, bool ORD>
+template <typename V, int LPR, int EPI, int U, bool ORD, bool PIPE>
 __global__ void __launch_bounds__(256)
 k_csrvec(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
          const V* __restrict__ val, const float* __restrict__ x, uint32_t nrows,
@@ -119,7 +165,7 @@ k_csrvec(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
     if (k < nrows) {
         if (ORD) row = __ldg(order + k);
         const uint64_t s = rowptr[row], t = rowptr[row + 1];
-        acc = lane_dot<V, LPR, U>(idx, val, x, s, t, sub);
+        acc = PIPE ? lane_dot_pipe<V, LPR, U>(idx, val, x, s, t, sub) : lane_dot<V, LPR, U>(idx, val, x, s, t, sub);
     }
     acc = group_sum<LPR>(acc);
     if (sub == 0 && k < nrows) {
@@ -129,39 +175,90 @@ k_csrvec(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
     }
 }
 
-// Persistent variant: one warp per row, W warps walk the rows with stride W
-// and fetch the next row's pointers before summing the current row, so the
-// dependent row-pointer load never stalls the stream.  Same per-row
-// arithmetic as k_csrvec<V, 32, EPI> (bit-identical results).
-template <typename V, int EPI>
+// Persistent, software-pipelined variant.  The grid holds as many groups of
+// LPR lanes as fit on the device; group k handles rows k, k+G, k+2G, ... (or
+// order[k], order[k+G], ... in locality order).  A step is U vectors per
+// lane; the index/value vectors of step i+1 (of the same row, or the first
+// step of the group's next row, whose pointers were fetched one row ahead)
+// are issued before the gathers of step i, so the HBM stream is in flight
+// while the gathers wait on L2.  Each lane accumulates its vectors
+// v = (s>>2)+sub, +LPR, +2*LPR, ... in increasing order and the group reduces
+// with the same xor butterfly as k_csrvec<V, LPR>: the results are
+// bit-identical to that kernel for every U.
+template <int LPR>
+__device__ __forceinline__ float group_sum_masked(float acc, unsigned mask) {
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(mask, acc, o);
+    return acc;
+}
+
+template <typename V, int LPR, int EPI, int U, bool ORD>
 __global__ void __launch_bounds__(256)
-k_csrvec_pf(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
-            const V* __restrict__ val, const float* __restrict__ x, uint32_t nrows,
-            const int32_t* __restrict__ g, float* __restrict__ out, float* __restrict__ fwproj,
-            float* __restrict__ f, const float* __restrict__ norm) {
-    const uint32_t W = (gridDim.x * blockDim.x) >> 5;
-    uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (row >= nrows) return;  // warp-uniform
+k_csrvec_pipe(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
+              const V* __restrict__ val, const float* __restrict__ x, uint32_t nrows,
+              const int32_t* __restrict__ g, float* __restrict__ out, float* __restrict__ fwproj,
+              float* __restrict__ f, const float* __restrict__ norm, const uint32_t* __restrict__ order) {
+    const uint32_t G = (gridDim.x * blockDim.x) / LPR;
+    uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) / LPR;
+    const int sub = threadIdx.x & (LPR - 1);
+    const unsigned mask = LPR == 32 ? 0xffffffffu : (((1u << LPR) - 1u) << ((threadIdx.x & 31) & ~(LPR - 1)));
+    if (k >= nrows) return;  // group-uniform
+    const uint4* idx4 = reinterpret_cast<const uint4*>(idx);
+    uint32_t row = ORD ? __ldg(order + k) : k;
     uint64_t s = rowptr[row], t = rowptr[row + 1];
-    while (true) {
-        const uint32_t nrow = row + W;
-        uint64_t ns = 0, nt = 0;
-        if (nrow < nrows) {
-            ns = rowptr[nrow];
-            nt = rowptr[nrow + 1];
+    uint32_t kn = k + G, nrow = 0;
+    uint64_t ns = 0, nt = 0;
+    if (kn < nrows) {
+        nrow = ORD ? __ldg(order + kn) : kn;
+        ns = rowptr[nrow];
+        nt = rowptr[nrow + 1];
+    }
+    uint64_t b = s >> 2, v1 = (t + 3) >> 2;
+    Vec4<V> cur[U];
+    load_step<V, LPR, U>(cur, idx4, val, b, v1, sub);
+    float acc = 0.f;
+    for (;;) {
+        const bool last = b + (uint64_t)U * LPR >= v1;  // no vector of this row after this step
+        const bool more = !last || kn < nrows;
+        const uint64_t nb = last ? (ns >> 2) : b + (uint64_t)U * LPR;
+        const uint64_t nv1 = last ? ((nt + 3) >> 2) : v1;
+        Vec4<V> nxt[U];
+        if (more) load_step<V, LPR, U>(nxt, idx4, val, nb, nv1, sub);
+        float gq[U][4];
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+            const uint64_t v = b + sub + (uint64_t)q * LPR;
+            if (v < v1) gather4(cur[q].c, v << 2, s, t, x, gq[q]);
         }
-        float acc = lane_dot<V, 32>(idx, val, x, s, t, lane);
-        acc = group_sum<32>(acc);
-        if (lane == 0) {
-            if (EPI == (int)Epi::Correl) epi_correl(row, acc, g, out, fwproj);
-            else if (EPI == (int)Epi::Update) epi_update(row, acc, f, norm);
-            else out[row] = acc;
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+            const uint64_t v = b + sub + (uint64_t)q * LPR;
+            if (v < v1) acc = fma4(acc, cur[q].a, gq[q], v << 2, s, t);
         }
-        if (nrow >= nrows) break;
-        row = nrow;
-        s = ns;
-        t = nt;
+        if (last) {
+            acc = group_sum_masked<LPR>(acc, mask);
+            if (sub == 0) {
+                if (EPI == (int)Epi::Correl) epi_correl(row, acc, g, out, fwproj);
+                else if (EPI == (int)Epi::Update) epi_update(row, acc, f, norm);
+                else out[row] = acc;
+            }
+            acc = 0.f;
+            if (!more) break;
+            k = kn;
+            row = nrow;
+            s = ns;
+            t = nt;
+            kn = k + G;
+            if (kn < nrows) {
+                nrow = ORD ? __ldg(order + kn) : kn;
+                ns = rowptr[nrow];
+                nt = rowptr[nrow + 1];
+            }
+        }
+        b = nb;
+        v1 = nv1;
+#pragma unroll
+        for (int q = 0; q < U; ++q) cur[q] = nxt[q];
     }
 }
 
@@ -299,7 +396,7 @@ __global__ void __launch_bounds__(1024) k_reduce_f64(const double* __restrict__ 
     if (threadIdx.x == 0) *out = tot;
 }
 
-template <typename V, int LPR, int U, bool ORD>
+template <typename V, int LPR, int U, bool ORD, bool PIPE>
 void csrvec_dispatch_epi(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win,
                          cudaStream_t s) {
     const uint64_t threads = (uint64_t)op.nrows * LPR;
@@ -308,72 +405,113 @@ void csrvec_dispatch_epi(const DevCsr& op, const float* x, const EpiArgs& e, L2W
     const uint32_t* ord = op.order;
     switch (e.kind) {
         case Epi::Correl:
-            launch_ex(k_csrvec<V, LPR, (int)Epi::Correl, U, ORD>, grid, block, 0, s, win, op.rowptr, op.idx,
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Correl, U, ORD, PIPE>, grid, block, 0, s, win, op.rowptr, op.idx,
                       val, x, op.nrows, e.g, e.out, e.fwproj, (float*)nullptr, (const float*)nullptr, ord);
             break;
         case Epi::Update:
-            launch_ex(k_csrvec<V, LPR, (int)Epi::Update, U, ORD>, grid, block, 0, s, win, op.rowptr, op.idx,
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Update, U, ORD, PIPE>, grid, block, 0, s, win, op.rowptr, op.idx,
                       val, x, op.nrows, (const int32_t*)nullptr, (float*)nullptr, (float*)nullptr,
                       e.f, e.norm, ord);
             break;
         default:
-            launch_ex(k_csrvec<V, LPR, (int)Epi::Raw, U, ORD>, grid, block, 0, s, win, op.rowptr, op.idx,
+            launch_ex(k_csrvec<V, LPR, (int)Epi::Raw, U, ORD, PIPE>, grid, block, 0, s, win, op.rowptr, op.idx,
                       val, x, op.nrows, (const int32_t*)nullptr, e.out, (float*)nullptr,
                       (float*)nullptr, (const float*)nullptr, ord);
     }
 }
 
-template <typename V, int EPI>
-unsigned pf_grid() {
+template <typename V, int LPR, int EPI, int U, bool ORD>
+unsigned pipe_grid() {
     static std::mutex mu;
     static std::map<int, unsigned> cache;
     int dev = 0;
-    cudaGetDevice(&dev);
+    MLEM_CUDA(cudaGetDevice(&dev));
     std::lock_guard<std::mutex> lk(mu);
     auto it = cache.find(dev);
     if (it != cache.end()) return it->second;
     int per_sm = 0, sms = 0;
-    MLEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_csrvec_pf<V, EPI>, 256, 0));
+    MLEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_csrvec_pipe<V, LPR, EPI, U, ORD>, 256, 0));
     MLEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     return cache[dev] = (unsigned)std::max(1, per_sm) * (unsigned)sms;
 }
 
-template <typename V, int EPI>
-void pf_launch(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
-    const unsigned grid = std::min(pf_grid<V, EPI>(), std::max(1u, ceil_div_u((uint64_t)op.nrows * 32, 256)));
-    launch_ex(k_csrvec_pf<V, EPI>, dim3(grid), dim3(256), 0, s, win, op.rowptr, op.idx,
-              static_cast<const V*>(op.val), x, op.nrows, e.g, e.out, e.fwproj, e.f, e.norm);
+template <typename V, int LPR, int EPI, int U, bool ORD>
+void pipe_launch(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+    const unsigned grid =
+        std::min(pipe_grid<V, LPR, EPI, U, ORD>(), std::max(1u, ceil_div_u((uint64_t)op.nrows * LPR, 256)));
+    launch_ex(k_csrvec_pipe<V, LPR, EPI, U, ORD>, dim3(grid), dim3(256), 0, s, win, op.rowptr, op.idx,
+              static_cast<const V*>(op.val), x, op.nrows, e.g, e.out, e.fwproj, e.f, e.norm,
+              (const uint32_t*)op.order);
 }
 
-template <typename V>
-void pf_dispatch(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
-    switch (e.kind) {
-        case Epi::Correl: pf_launch<V, (int)Epi::Correl>(op, x, e, win, s); break;
-        case Epi::Update: pf_launch<V, (int)Epi::Update>(op, x, e, win, s); break;
-        default: pf_launch<V, (int)Epi::Raw>(op, x, e, win, s);
+// kind: 0 = launch, 1 = settle the grid size only (outside stream captures).
+template <typename V, int LPR, int U, bool ORD>
+void pipe_epi(int kind, const DevCsr* op, const float* x, const EpiArgs* e, L2Window win, cudaStream_t s) {
+    if (kind == 1) {
+        pipe_grid<V, LPR, (int)Epi::Correl, U, ORD>();
+        pipe_grid<V, LPR, (int)Epi::Update, U, ORD>();
+        pipe_grid<V, LPR, (int)Epi::Raw, U, ORD>();
+        return;
+    }
+    switch (e->kind) {
+        case Epi::Correl: pipe_launch<V, LPR, (int)Epi::Correl, U, ORD>(*op, x, *e, win, s); break;
+        case Epi::Update: pipe_launch<V, LPR, (int)Epi::Update, U, ORD>(*op, x, *e, win, s); break;
+        default: pipe_launch<V, LPR, (int)Epi::Raw, U, ORD>(*op, x, *e, win, s);
     }
 }
 
 template <typename V, int LPR>
-void csrvec_dispatch_u(const DevCsr& op, const float* x, const EpiArgs& e, int unroll, bool ordered,
-                       L2Window win, cudaStream_t s) {
-    if (ordered && op.order && LPR >= 16) {
-        if (unroll >= 2) csrvec_dispatch_epi<V, LPR, 2, true>(op, x, e, win, s);
-        else csrvec_dispatch_epi<V, LPR, 1, true>(op, x, e, win, s);
-        return;
+void pipe_u(int kind, const DevCsr* op, const float* x, const EpiArgs* e, int unroll, bool ordered, L2Window win,
+            cudaStream_t s) {
+    if (ordered) {
+        if (unroll >= 2) pipe_epi<V, LPR, 2, true>(kind, op, x, e, win, s);
+        else pipe_epi<V, LPR, 1, true>(kind, op, x, e, win, s);
+    } else {
+        if (unroll >= 2) pipe_epi<V, LPR, 2, false>(kind, op, x, e, win, s);
+        else pipe_epi<V, LPR, 1, false>(kind, op, x, e, win, s);
     }
-    if (unroll >= 4) csrvec_dispatch_epi<V, LPR, 4, false>(op, x, e, win, s);
-    else if (unroll == 2) csrvec_dispatch_epi<V, LPR, 2, false>(op, x, e, win, s);
-    else csrvec_dispatch_epi<V, LPR, 1, false>(op, x, e, win, s);
+}
+
+template <typename V>
+void pipe_lanes(int kind, const DevCsr* op, const float* x, const EpiArgs* e, int lanes, int unroll, bool ordered,
+                L2Window win, cudaStream_t s) {
+    if (lanes >= 32) pipe_u<V, 32>(kind, op, x, e, unroll, ordered, win, s);
+    else pipe_u<V, 16>(kind, op, x, e, unroll, ordered, win, s);
+}
+
+template <typename V, int LPR>
+void csrvec_dispatch_u(const DevCsr& op, const float* x, const EpiArgs& e, int unroll, bool ordered, bool pipelined,
+                       L2Window win, cudaStream_t s) {
+    if constexpr (LPR >= 16) {
+        const bool ord = ordered && op.order;
+        if (pipelined) {
+            if (ord) {
+                if (unroll >= 2) csrvec_dispatch_epi<V, LPR, 2, true, true>(op, x, e, win, s);
+                else csrvec_dispatch_epi<V, LPR, 1, true, true>(op, x, e, win, s);
+            } else {
+                if (unroll >= 2) csrvec_dispatch_epi<V, LPR, 2, false, true>(op, x, e, win, s);
+                else csrvec_dispatch_epi<V, LPR, 1, false, true>(op, x, e, win, s);
+            }
+            return;
+        }
+        if (ord) {
+            if (unroll >= 2) csrvec_dispatch_epi<V, LPR, 2, true, false>(op, x, e, win, s);
+            else csrvec_dispatch_epi<V, LPR, 1, true, false>(op, x, e, win, s);
+            return;
+        }
+    }
+    if (unroll >= 4) csrvec_dispatch_epi<V, LPR, 4, false, false>(op, x, e, win, s);
+    else if (unroll == 2) csrvec_dispatch_epi<V, LPR, 2, false, false>(op, x, e, win, s);
+    else csrvec_dispatch_epi<V, LPR, 1, false, false>(op, x, e, win, s);
 }
 
 template <typename V>
 void csrvec_dispatch_lanes(const DevCsr& op, const float* x, const EpiArgs& e, int lanes, int unroll,
-                           bool ordered, L2Window win, cudaStream_t s) {
-    if (lanes >= 32) csrvec_dispatch_u<V, 32>(op, x, e, unroll, ordered, win, s);
-    else if (lanes >= 16) csrvec_dispatch_u<V, 16>(op, x, e, unroll, ordered, win, s);
-    else if (lanes >= 8) csrvec_dispatch_u<V, 8>(op, x, e, unroll, false, win, s);
-    else csrvec_dispatch_u<V, 4>(op, x, e, unroll, false, win, s);
+                           bool ordered, bool pipelined, L2Window win, cudaStream_t s) {
+    if (lanes >= 32) csrvec_dispatch_u<V, 32>(op, x, e, unroll, ordered, pipelined, win, s);
+    else if (lanes >= 16) csrvec_dispatch_u<V, 16>(op, x, e, unroll, ordered, pipelined, win, s);
+    else if (lanes >= 8) csrvec_dispatch_u<V, 8>(op, x, e, unroll, false, false, win, s);
+    else csrvec_dispatch_u<V, 4>(op, x, e, unroll, false, false, win, s);
 }
 
 template <typename V>
@@ -401,29 +539,38 @@ int pick_lanes(uint64_t nnz, uint32_t rows) {
 }
 
 void launch_csrvec(const DevCsr& op, const float* x, const EpiArgs& epi, int lanes, L2Window win,
-                   cudaStream_t s, int unroll, bool ordered) {
+                   cudaStream_t s, int unroll, bool ordered, bool pipelined) {
     if (op.nrows == 0) return;
     switch (op.vt) {
-        case MLEM_VAL_F32: csrvec_dispatch_lanes<float>(op, x, epi, lanes, unroll, ordered, win, s); break;
-        case MLEM_VAL_F16: csrvec_dispatch_lanes<__half>(op, x, epi, lanes, unroll, ordered, win, s); break;
-        default: csrvec_dispatch_lanes<__nv_bfloat16>(op, x, epi, lanes, unroll, ordered, win, s);
+        case MLEM_VAL_F32: csrvec_dispatch_lanes<float>(op, x, epi, lanes, unroll, ordered, pipelined, win, s); break;
+        case MLEM_VAL_F16:
+            csrvec_dispatch_lanes<__half>(op, x, epi, lanes, unroll, ordered, pipelined, win, s);
+            break;
+        default: csrvec_dispatch_lanes<__nv_bfloat16>(op, x, epi, lanes, unroll, ordered, pipelined, win, s);
     }
 }
 
-void prepare_csrvec_pf(mlem_value_type vt) {
-    switch (vt) {
-        case MLEM_VAL_F32: pf_grid<float, 0>(); pf_grid<float, 1>(); pf_grid<float, 2>(); break;
-        case MLEM_VAL_F16: pf_grid<__half, 0>(); pf_grid<__half, 1>(); pf_grid<__half, 2>(); break;
-        default: pf_grid<__nv_bfloat16, 0>(); pf_grid<__nv_bfloat16, 1>(); pf_grid<__nv_bfloat16, 2>();
-    }
+void prepare_csrvec_pipe(mlem_value_type vt) {
+    for (int lanes : {16, 32})
+        for (int u : {1, 2})
+            for (bool ord : {false, true}) {
+                switch (vt) {
+                    case MLEM_VAL_F32: pipe_lanes<float>(1, nullptr, nullptr, nullptr, lanes, u, ord, {}, 0); break;
+                    case MLEM_VAL_F16: pipe_lanes<__half>(1, nullptr, nullptr, nullptr, lanes, u, ord, {}, 0); break;
+                    default: pipe_lanes<__nv_bfloat16>(1, nullptr, nullptr, nullptr, lanes, u, ord, {}, 0);
+                }
+            }
 }
 
-void launch_csrvec_pf(const DevCsr& op, const float* x, const EpiArgs& epi, L2Window win, cudaStream_t s) {
+void launch_csrvec_pipe(const DevCsr& op, const float* x, const EpiArgs& epi, int lanes, int unroll, bool ordered,
+                        L2Window win, cudaStream_t s) {
     if (op.nrows == 0) return;
+    MLEM_REQUIRE(lanes == 16 || lanes == 32, MLEM_EINVAL, "pipelined projection needs 16 or 32 lanes per row");
+    MLEM_REQUIRE(!ordered || op.order != nullptr, MLEM_EINVAL, "operand has no row order");
     switch (op.vt) {
-        case MLEM_VAL_F32: pf_dispatch<float>(op, x, epi, win, s); break;
-        case MLEM_VAL_F16: pf_dispatch<__half>(op, x, epi, win, s); break;
-        default: pf_dispatch<__nv_bfloat16>(op, x, epi, win, s);
+        case MLEM_VAL_F32: pipe_lanes<float>(0, &op, x, &epi, lanes, unroll, ordered, win, s); break;
+        case MLEM_VAL_F16: pipe_lanes<__half>(0, &op, x, &epi, lanes, unroll, ordered, win, s); break;
+        default: pipe_lanes<__nv_bfloat16>(0, &op, x, &epi, lanes, unroll, ordered, win, s);
     }
 }
 

@@ -17,9 +17,13 @@ roofline: the dominant kernel's algorithmic bytes / its CUDA-event duration
 cpu_baseline: the oracle's OpenMP MLEM (FP32 values, FP64 accumulation) on a
          row sample of the same matrix, scaled to the full matrix by nnz.
 
---impl reference runs only the CPU implementation (the reference has no CPU
-path of its own and its CUDA code cannot be built on the GPU host; the
-oracle port stands in) and prints its line.
+--impl reference times the CPU implementation of the path (the reference has
+no CPU path of its own; the oracle port, pinned bit-exact to the reference's
+compiled code, stands in) and prints its line.  The line also carries
+"reference_cuda": the reference's own kernel.cu, compiled unmodified for
+sm_103a into oracle/_ref/mlemref_kernels.cubin, launched with the grids and
+step order of its single-GPU MLEM loop on the same workload (all four
+argv[7]/argv[8] modes).
 """
 from __future__ import annotations
 
@@ -248,7 +252,51 @@ def run_reference(args):
         "note": "the reference's MLEM loop exists only as CUDA kernels + NCCL; its CPU-side restatement "
                 "(oracle/mlem_oracle.c, pinned bit-exact to the reference's compiled kernels) is timed",
     }
+    if not args.no_ref_cuda:
+        line["reference_cuda"] = reference_cuda(pkg, name, args)
     print(json.dumps(line), flush=True)
+
+
+def reference_cuda(pkg, name, args):
+    """The reference's kernel.cu on this GPU, launched as its main.cu loop does."""
+    try:
+        import torch
+        from oracle import ref_cuda
+        from oracle import oracle as O
+        from mlem_gb300 import synth
+    except Exception as e:  # pragma: no cover
+        return {"unavailable": f"import failed: {e}"}
+    if not torch.cuda.is_available():
+        return {"unavailable": "no CUDA device"}
+    if not ref_cuda.available():
+        return {"unavailable": "oracle/_ref/mlemref_kernels.cubin not built (needs the reference sources)"}
+    t0 = time.perf_counter()
+    geo = pkg.preset(name)
+    rp, col, val, cols = pkg.siddon_host(geo)
+    AT = O.transpose(rp, col, val, cols)
+    xt = synth.phantom(geo, WORKLOADS[name]["shapes"], seed=1)
+    g = synth.poisson_sinogram(synth.project_host(rp, col, val, xt), WORKLOADS[name]["total"], seed=2)
+    norm = O.colsum(rp, col, val, cols).astype(np.float32)
+    f0 = np.full(cols, O.initial_value(g, norm), np.float32)
+    prep = time.perf_counter() - t0
+    out = {"kind": "reference kernel.cu compiled unmodified for sm_103a; main.cu:302-449 loop replayed at 1 GPU "
+                   "(blocksize 1024, secsize 5/5, host synchronisations and memsets included)",
+           "workload": name, "input_prep_s": round(prep, 1), "modes": {}}
+    iters = max(3, min(args.steps, 10))
+    with ref_cuda.ReferenceCudaMLEM((rp, col, val), cols, AT) as R:
+        for label, spmv, trans in (("csr_vector_trans", 1, 0), ("merge_trans", 0, 0),
+                                   ("csr_vector_scatter", 1, 1), ("merge_scatter", 0, 1)):
+            if spmv == 1 and not R.csr_vector_ok(trans):
+                out["modes"][label] = {"unavailable": "row count not a multiple of 32"}
+                continue
+            t = R.time(g, norm, f0, iters, warmup=max(1, args.warmup), spmv=spmv, using_trans=trans)
+            out["modes"][label] = {k: round(v, 4) for k, v in t.items()}
+    best = max((m for m in out["modes"].values() if "iterations_per_s" in m),
+               key=lambda m: m["iterations_per_s"], default=None)
+    if best is not None:
+        out["value"] = best["iterations_per_s"]
+        out["unit"] = "iter/s"
+    return out
 
 
 def run_forms(pkg, torch, args):
@@ -406,6 +454,8 @@ def main():
     ap.add_argument("--workload", default="cyl3d_12gb", choices=sorted(WORKLOADS))
     ap.add_argument("--forms", default="all", choices=["all", "none"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ref-cuda", action="store_true",
+                    help="reference arm: skip timing the reference's CUDA kernels")
     ap.add_argument("--no-interleave", action="store_true",
                     help="skip the lane-interleaved matrix copy (halves device memory)")
     args = ap.parse_args()

@@ -114,10 +114,11 @@ typedef struct {
 mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info);
 /* Configuration the autotuner chose for the csr-vector projection of A
  * (transposed = 0) or Aᵀ (1): kernel (mlem_kernel), lanes per row, vectors in
- * flight per lane, whether rows run in locality order, and the measured
+ * flight per lane, whether rows run in locality order, whether the row's
+ * vector loads are software-pipelined, and the measured
  * milliseconds of one launch.  Tunes on first call if needed. */
 mlem_status mlem_matrix_get_tuning(mlem_matrix* m, uint32_t transposed, int* kernel, int* lanes,
-                                   int* unroll, int* ordered, float* ms);
+                                   int* unroll, int* ordered, int* pipelined, float* ms);
 /* Copies the sensitivity image (f32[cols]) to the host. */
 mlem_status mlem_matrix_get_norm(const mlem_matrix* m, float* norm_out);
 /* Copies the device-built transpose to the host: colptr u64[cols+1],
@@ -136,13 +137,23 @@ typedef struct {
     uint32_t loglik_every;      /* 0: off; k: FP64 log-likelihood every k-th iteration */
     uint32_t l2_window;         /* 1: keep the image/ratio vector L2-persisting */
     uint32_t kernel;            /* csr-vector switch only: mlem_kernel variant */
+    uint32_t lanes;             /* DIRECT / PERSISTENT / ORDERED: lanes per row (4, 8, 16, 32;
+                                   PERSISTENT 16 or 32); 0 = chosen from the mean row length */
+    uint32_t unroll;            /* same kernels: vectors of 4 elements in flight per lane
+                                   (1, 2, 4; PERSISTENT 1 or 2); 0 = 2 */
+    uint32_t row_order;         /* DIRECT / PERSISTENT with 16 or 32 lanes: 1 = process the rows in
+                                   the locality order of a generated matrix */
+    uint32_t pipeline;          /* DIRECT / ORDERED with 16 or 32 lanes: 1 = load a row's next vectors
+                                   before the gathers of the current ones (same results) */
 } mlem_run_opts;
 
 /* Kernel variants of the csr-vector projections (same arithmetic; the order of
  * the FP32 additions depends on the variant and its lanes/unroll, so results of
  * different variants agree to rounding, and one matrix handle always uses one):
  *   DIRECT     one warp (or 4-32 lanes) per row, a grid of one row per group;
- *   PERSISTENT resident warps walk the rows and prefetch the next row's pointers;
+ *   PERSISTENT resident groups walk the rows, software-pipelined: the next
+ *              step's index/value vectors (and the next row's pointers) are
+ *              loaded before the current step's gathers;
  *   TMA        rows streamed into a shared-memory ring with cp.async.bulk. */
 typedef enum {
     MLEM_KERNEL_DIRECT = 0,
@@ -156,7 +167,7 @@ typedef enum {
 } mlem_kernel;
 
 /* Defaults: CSR_VECTOR, BP_TRANS, secsize 5/5, graphs on, no log-likelihood, L2 window on,
- * AUTO kernel. */
+ * AUTO kernel, lanes, unroll, row_order and pipeline 0. */
 void mlem_run_opts_default(mlem_run_opts* o);
 
 typedef struct {

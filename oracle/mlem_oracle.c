@@ -28,24 +28,63 @@ static inline float madd(float acc, float a, float b, int use_fma) {
 
 /* ------------------------------------------------------------ transpose */
 /* Stable counting sort of the nonzeros by column: the permutation produced by
- * sptrans_scanTrans_specialized (sptrans.h:397-545) — column histogram and
- * prefix (sptrans.h:432-463), row unrolling (sptrans.h:465-472) and the
- * write-back in original order (sptrans.h:474-545). */
+ * sptrans_scanTrans_specialized (sptrans.h:397-545) — per-thread column
+ * histograms over contiguous row ranges (sptrans.h:432-449), their prefix
+ * over columns and threads (sptrans.h:450-463), and the write-back of each
+ * thread's rows in original order (sptrans.h:465-545).  Entries of a column
+ * keep their original order, so the output does not depend on the thread
+ * count. */
 void oracle_transpose(uint32_t rows, uint32_t cols, uint64_t nnz, const uint64_t* rowptr,
                       const uint32_t* col, const float* val, uint64_t* colptr, uint32_t* rowT,
                       float* valT) {
-    uint64_t* cur = (uint64_t*)calloc((size_t)cols + 1, sizeof(uint64_t));
-    memset(colptr, 0, sizeof(uint64_t) * ((size_t)cols + 1));
-    for (uint64_t e = 0; e < nnz; ++e) colptr[col[e] + 1]++;
-    for (uint32_t c = 0; c < cols; ++c) colptr[c + 1] += colptr[c];
-    for (uint32_t c = 0; c <= cols; ++c) cur[c] = colptr[c];
-    for (uint32_t r = 0; r < rows; ++r)
-        for (uint64_t e = rowptr[r]; e < rowptr[r + 1]; ++e) {
-            const uint64_t p = cur[col[e]]++;
-            rowT[p] = r;
-            if (val) valT[p] = val[e];
+    int T = omp_get_max_threads();
+    if (T < 1) T = 1;
+    if ((uint64_t)T > (uint64_t)rows) T = rows ? (int)rows : 1;
+    /* nnz-balanced contiguous row ranges */
+    uint32_t* rb = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)T + 1));
+    rb[0] = 0;
+    for (int t = 1; t < T; ++t) {
+        const uint64_t target = nnz * (uint64_t)t / (uint64_t)T;
+        uint32_t lo = rb[t - 1], hi = rows;
+        while (lo < hi) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (rowptr[mid] < target) lo = mid + 1;
+            else hi = mid;
         }
-    free(cur);
+        rb[t] = lo;
+    }
+    rb[T] = rows;
+    uint64_t* cnt = (uint64_t*)calloc((size_t)T * ((size_t)cols + 1), sizeof(uint64_t));
+#pragma omp parallel for num_threads(T) schedule(static, 1)
+    for (int t = 0; t < T; ++t) {
+        uint64_t* h = cnt + (size_t)t * ((size_t)cols + 1);
+        for (uint64_t e = rowptr[rb[t]]; e < rowptr[rb[t + 1]]; ++e) h[col[e]]++;
+    }
+    /* column-major prefix: column c of thread t starts after all of columns
+     * < c and after column c of threads < t */
+    uint64_t run = 0;
+    for (uint32_t c = 0; c < cols; ++c) {
+        colptr[c] = run;
+        for (int t = 0; t < T; ++t) {
+            uint64_t* h = cnt + (size_t)t * ((size_t)cols + 1);
+            const uint64_t k = h[c];
+            h[c] = run;
+            run += k;
+        }
+    }
+    colptr[cols] = run;
+#pragma omp parallel for num_threads(T) schedule(static, 1)
+    for (int t = 0; t < T; ++t) {
+        uint64_t* cur = cnt + (size_t)t * ((size_t)cols + 1);
+        for (uint32_t r = rb[t]; r < rb[t + 1]; ++r)
+            for (uint64_t e = rowptr[r]; e < rowptr[r + 1]; ++e) {
+                const uint64_t p = cur[col[e]]++;
+                rowT[p] = r;
+                if (val) valT[p] = val[e];
+            }
+    }
+    free(cnt);
+    free(rb);
 }
 
 /* ---------------------------------------------------------- merge search */

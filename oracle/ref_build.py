@@ -1,4 +1,5 @@
-"""Compiles the reference's own sources into oracle/_ref/libmlemref.so.
+"""Compiles the reference's own sources into oracle/_ref/libmlemref.so and
+oracle/_ref/mlemref_kernels.cubin.
 
 Test infrastructure: the library pins the oracle (mlem_oracle.c) against the
 reference itself.  It needs the reference checkout at REF (default
@@ -47,5 +48,27 @@ def build() -> Path | None:
     return OUT
 
 
+CUBIN = HERE / "_ref" / "mlemref_kernels.cubin"
+
+
+def build_cubin() -> Path | None:
+    """The reference's kernel.cu, unmodified, compiled for sm_103a as a cubin.
+
+    Device code only, so it also loads on a GPU host of another CPU
+    architecture (ref_cuda.py launches its kernels through the driver API)."""
+    if not available():
+        return None
+    CUBIN.parent.mkdir(parents=True, exist_ok=True)
+    src = [REF / "kernel.cu", REF / "kernel.cuh"]
+    if CUBIN.exists() and CUBIN.stat().st_mtime >= max(p.stat().st_mtime for p in src):
+        return CUBIN
+    cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-I", str(REF),
+           str(REF / "kernel.cu"), "-o", str(CUBIN)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference cubin build failed:\n{r.stdout}\n{r.stderr}")
+    return CUBIN
+
+
 if __name__ == "__main__":
-    print(build())
+    print(build(), build_cubin())

@@ -77,7 +77,12 @@ def problem(pkg, O, name, n_shapes=5, total=1e6, seed=0):
     "cyl3d_tiny_dense" is a small cylinder (2 x 24 detectors, 40x40x8 voxels
     of 0.8 mm, 3x2 sub-rays) dense enough (> 96 nnz per row) to select the
     one-warp-per-row kernels for the forward projection."""
-    if name == "cyl3d_tiny_dense":
+    if name == "cyl3d_rows32":
+        # 2 x 32 detectors (2,016 rows) and 24x24x8 voxels (4,608 cols): both
+        # multiples of 32, the shapes the reference's csr-vector grid assumes
+        geo = pkg.geometry(32, 2, 20.0, 3.0, nx=24, ny=24, nz=8, vx=1.0, vy=1.0, vz=1.0, sub_t=2, sub_z=2,
+                           width_t=1.0, width_z=0.8)
+    elif name == "cyl3d_tiny_dense":
         geo = pkg.geometry(24, 2, 20.0, 3.0, nx=40, ny=40, nz=8, vx=0.8, vy=0.8, vz=0.8, sub_t=3, sub_z=2,
                            width_t=1.5, width_z=1.2)
     else:

@@ -357,5 +357,40 @@ def test_generated_matrix_locality_order(pkg, O, name):
         got = m.run(g, 15, f0=f0, kernel=kern)
         assert O.rel_l2(got, ref64) < TOL_F32, kern
     t = m.tuning(False)
-    assert set(t) >= {"kernel", "lanes_per_row", "vectors_in_flight", "locality_order", "ms"}
+    assert set(t) >= {"kernel", "lanes_per_row", "vectors_in_flight", "locality_order", "pipelined", "ms"}
     m.close()
+
+
+@pytest.mark.parametrize("name", ["ring2d", "cyl3d_tiny_dense"])
+def test_pipelined_and_ordered_kernels_bit_identical_to_direct(pkg, O, name):
+    """The persistent software-pipelined kernel (1 or 2 vectors per step) and
+    the locality row order change neither a row's summation order nor the
+    result: images are bitwise equal to the direct kernel with the same lanes."""
+    p = problem(pkg, O, name)
+    m = pkg.Matrix.generate(p["geo"])
+    f0 = np.full(m.cols, m.initial_value(p["g"]), np.float32)
+    ref64 = O.mlem_f64((p["rp"], p["col"], p["val"]), p["g"], m.norm().astype(np.float64), f0, 8)
+    for lanes in (16, 32):
+        want = m.run(p["g"], 8, f0=f0, kernel=pkg.KERNEL_DIRECT, lanes=lanes, unroll=2)
+        assert O.rel_l2(want, ref64) < TOL_F32
+        for kern in (pkg.KERNEL_DIRECT, pkg.KERNEL_PERSISTENT):
+            for unroll in (1, 2):
+                for order in (False, True):
+                    for pipe in ((False, True) if kern == pkg.KERNEL_DIRECT else (False,)):
+                        for graph in (True, False):
+                            got = m.run(p["g"], 8, f0=f0, kernel=kern, lanes=lanes, unroll=unroll, row_order=order,
+                                        pipeline=pipe, use_graph=graph)
+                            assert np.array_equal(got, want), (lanes, kern, unroll, order, pipe, graph)
+        got = m.run(p["g"], 8, f0=f0, kernel=pkg.KERNEL_ORDERED, lanes=lanes)
+        assert np.array_equal(got, want)
+        got = m.run(p["g"], 8, f0=f0, kernel=pkg.KERNEL_ORDERED, lanes=lanes, pipeline=True)
+        assert np.array_equal(got, want)
+    with pytest.raises(pkg.MlemError):
+        m.run(p["g"], 1, kernel=pkg.KERNEL_PERSISTENT, lanes=8)
+    with pytest.raises(pkg.MlemError):
+        m.run(p["g"], 1, kernel=pkg.KERNEL_DIRECT, lanes=8, row_order=True)
+    m.close()
+    h = pkg.Matrix.from_csr(p["rp"], p["col"], p["val"], p["cols"])
+    with pytest.raises(pkg.MlemError):
+        h.run(p["g"], 1, kernel=pkg.KERNEL_DIRECT, row_order=True)
+    h.close()
