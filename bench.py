@@ -344,6 +344,21 @@ def run_forms(pkg, torch, args):
         b.record(s)
         b.synchronize()
         res[f"fp32_plain_{small}"] = {"images_iterations_per_s": 3 * its / (a.elapsed_time(b) * 1e-3)}
+        if small == "cyl3d_mid":
+            # the reference's four switch combinations (argv[8] merge/csr-vector x argv[7]
+            # transposed/scatter) and the fused single pass, FP32, 100 iterations each
+            modes = {}
+            for label, spmv, bp in (("csr_vector_trans", 1, 0), ("merge_trans", 0, 0),
+                                    ("csr_vector_scatter", 1, 1), ("merge_scatter", 0, 1), ("fused", 1, 2)):
+                fs.copy_(f0s)
+                msm.run_device(gsd.data_ptr(), fs.data_ptr(), 5, stream=s.cuda_stream, spmv=spmv, bp_mode=bp)
+                fs.copy_(f0s)
+                a.record(s)
+                msm.run_device(gsd.data_ptr(), fs.data_ptr(), its, stream=s.cuda_stream, spmv=spmv, bp_mode=bp)
+                b.record(s)
+                b.synchronize()
+                modes[label] = {"iterations_per_s": its / (a.elapsed_time(b) * 1e-3)}
+            res["modes_cyl3d_mid"] = modes
         msm.close()
     # batched: the mid-size matrix with FP16 values, 64 sinograms, uneven iterations
     mb = pkg.Matrix.generate(pkg.preset("cyl3d_mid"), value_type=pkg.VAL_F16)

@@ -300,6 +300,38 @@ void oracle_mlem_f64(const uint64_t* rowptr, const uint32_t* col, const float* v
     free(bp);
 }
 
+/* The FP64 oracle with the back projection over rows of Aᵀ (parallel over
+ * columns): the same quantities as oracle_mlem_f64, summed in another order,
+ * so results agree to FP64 rounding.  For full-size matrices. */
+void oracle_mlem_f64_t(const uint64_t* rowptr, const uint32_t* col, const float* val,
+                       const uint64_t* rowptrT, const uint32_t* colT, const float* valT, const int32_t* g,
+                       const double* norm, const double* f0, uint32_t rows, uint32_t cols,
+                       uint32_t iterations, double* f_out, double* loglik) {
+    double* f = (double*)malloc(sizeof(double) * (cols ? cols : 1));
+    double* ratio = (double*)malloc(sizeof(double) * (rows ? rows : 1));
+    memcpy(f, f0, sizeof(double) * cols);
+    for (uint32_t it = 0; it < iterations; ++it) {
+        double ll = 0.0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : ll)
+        for (int64_t r = 0; r < (int64_t)rows; ++r) {
+            double s = 0.0;
+            for (uint64_t e = rowptr[r]; e < rowptr[r + 1]; ++e) s += (double)val[e] * f[col[e]];
+            ratio[r] = s != 0.0 ? (double)g[r] / s : 0.0;
+            if (s > 0.0) ll += (g[r] > 0 ? (double)g[r] * log(s) : 0.0) - s;
+        }
+        if (loglik) loglik[it] = ll;
+#pragma omp parallel for schedule(dynamic, 1024)
+        for (int64_t c = 0; c < (int64_t)cols; ++c) {
+            double s = 0.0;
+            for (uint64_t e = rowptrT[c]; e < rowptrT[c + 1]; ++e) s += (double)valT[e] * ratio[colT[e]];
+            f[c] = norm[c] == 0.0 ? f[c] * s : f[c] * s / norm[c];
+        }
+    }
+    memcpy(f_out, f, sizeof(double) * cols);
+    free(f);
+    free(ratio);
+}
+
 /* CPU baseline: transposed-form MLEM with FP32 values and image, FP64
  * accumulation, OpenMP over rows of A (forward) and rows of Aᵀ (back).
  * nthreads <= 0 uses the OpenMP default. */

@@ -29,6 +29,7 @@ _SIGS = {
     "oracle_mlem_f32": (None, [_P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint64,
                                C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
     "oracle_mlem_f64": (None, [_P, _P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P]),
+    "oracle_mlem_f64_t": (None, [_P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P]),
     "oracle_mlem_omp": (None, [_P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
     "oracle_max_threads": (C.c_int, []),
 }
@@ -171,6 +172,20 @@ def mlem_f64(A, g, norm, f0, iterations, loglik=False):
     out = np.zeros(len(norm), np.float64)
     ll = np.zeros(iterations, np.float64)
     lib().oracle_mlem_f64(P(rp), P(c), P(v), P(g), P(norm), P(f0), len(rp) - 1, len(norm), iterations, P(out), P(ll))
+    return (out, ll) if loglik else out
+
+
+def mlem_f64_t(A, AT, g, norm, f0, iterations, loglik=False):
+    """mlem_f64 with the back projection over rows of AT (OpenMP), for full-size matrices."""
+    rp, c, v = c64(A[0]), c32(A[1]), f32(A[2])
+    rpt, ct, vt = c64(AT[0]), c32(AT[1]), f32(AT[2])
+    g = i32(g)
+    norm = np.ascontiguousarray(norm, np.float64)
+    f0 = np.ascontiguousarray(f0, np.float64)
+    out = np.zeros(len(norm), np.float64)
+    ll = np.zeros(iterations, np.float64)
+    lib().oracle_mlem_f64_t(P(rp), P(c), P(v), P(rpt), P(ct), P(vt), P(g), P(norm), P(f0), len(rp) - 1, len(norm),
+                            iterations, P(out), P(ll))
     return (out, ll) if loglik else out
 
 

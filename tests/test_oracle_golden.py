@@ -124,3 +124,16 @@ def test_merge_search_equals_merrill_garland(O, rows, mean):
         else:
             assert np.array_equal(i[inside], mi[inside]) and np.array_equal(j[inside], mj[inside])
         assert np.array_equal(i + j, d)  # every coordinate lies on its diagonal
+
+
+def test_f64_oracle_transposed_form_agrees(pkg, O):
+    """The FP64 oracle with its back projection over Aᵀ (used at full size)
+    equals the row-scatter form to FP64 rounding."""
+    from conftest import problem
+    p = problem(pkg, O, "cyl3d_tiny")
+    A = (p["rp"], p["col"], p["val"])
+    AT = O.transpose(*A, p["cols"])
+    a, lla = O.mlem_f64(A, p["g"], p["norm"], p["f0"], 12, loglik=True)
+    b, llb = O.mlem_f64_t(A, AT, p["g"], p["norm"], p["f0"], 12, loglik=True)
+    assert O.rel_l2(b, a) < 1e-13
+    np.testing.assert_allclose(llb, lla, rtol=1e-13)
