@@ -106,6 +106,95 @@ void write_exact(FILE* f, const void* src, uint64_t bytes, const std::string& wh
     if (bytes && std::fwrite(src, 1, bytes, f) != bytes) fail(MLEM_EIO, "short write: " + what);
 }
 
+// {u32 column, f32 value} pairs (matrixelement.hpp:37-46) -> SoA idx/val;
+// any column >= cols raises *err.
+__global__ void k_csr4_split(const uint2* __restrict__ pairs, uint64_t n, uint32_t cols, uint32_t* __restrict__ idx,
+                             uint32_t* __restrict__ val_bits, uint32_t* __restrict__ err) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint2 p = pairs[i];
+        if (p.x >= cols) atomicOr(err, 1u);
+        idx[i] = p.x;
+        val_bits[i] = p.y;
+    }
+}
+
+// Streams the csr4 file into the device CSR A: the row END offsets are read on
+// the host and checked like mlem_csr4_read; the element pairs are read in
+// chunks into two pinned staging buffers (the read of chunk i+1 overlaps the
+// copy and the split of chunk i) and split on the GPU into the column and
+// value arrays (the host AoS->SoA loop of csr_format_for_cuda, main.cu:518-554,
+// moved to the device).
+void csr4_ingest(const char* path, const Csr4Info& info, DevCsr& A, cudaStream_t s) {
+    const uint32_t rows = info.h.rows;
+    const uint64_t nnz = info.h.nnz;
+    File fh(path, "rb");
+    if (!fh.f) fail(MLEM_EIO, std::string("Cannot open file ") + path);
+    if (fseeko(fh.f, (off_t)(28 + info.scan_bytes), SEEK_SET) != 0) fail(MLEM_EIO, "seek failed");
+    std::vector<uint64_t> rp((uint64_t)rows + 1);
+    rp[0] = 0;
+    read_exact(fh.f, rp.data() + 1, 8ull * rows, "row indexes");
+    for (uint32_t r = 0; r < rows; ++r)
+        if (rp[r + 1] < rp[r]) fail(MLEM_EIO, "csr4: row offsets are not monotone");
+    if (rows && rp[rows] != nnz) fail(MLEM_EIO, "csr4: last row offset differs from nnz");
+    A.nrows = rows;
+    A.ncols = info.h.cols;
+    A.nnz = nnz;
+    A.vt = MLEM_VAL_F32;
+    MLEM_CUDA(cudaMalloc(&A.rowptr, sizeof(uint64_t) * ((uint64_t)rows + 1)));
+    MLEM_CUDA(cudaMalloc(&A.idx, sizeof(uint32_t) * padded(nnz)));
+    MLEM_CUDA(cudaMalloc(&A.val, sizeof(float) * padded(nnz)));
+    if (padded(nnz) > nnz) {
+        MLEM_CUDA(cudaMemsetAsync(A.idx + nnz, 0, sizeof(uint32_t) * (padded(nnz) - nnz), s));
+        MLEM_CUDA(cudaMemsetAsync(static_cast<float*>(A.val) + nnz, 0, sizeof(float) * (padded(nnz) - nnz), s));
+    }
+    MLEM_CUDA(cudaMemcpyAsync(A.rowptr, rp.data(), sizeof(uint64_t) * ((uint64_t)rows + 1), cudaMemcpyHostToDevice,
+                              s));
+    const uint64_t chunk = std::min<uint64_t>(nnz ? nnz : 1, 1ull << 23);  // pairs per chunk (64 MiB)
+    uint2* host[2] = {nullptr, nullptr};
+    uint2* dev[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    uint32_t* err = nullptr;
+    auto release = [&] {
+        cudaStreamSynchronize(s);
+        for (int k = 0; k < 2; ++k) {
+            if (host[k]) cudaFreeHost(host[k]);
+            if (dev[k]) cudaFree(dev[k]);
+            if (done[k]) cudaEventDestroy(done[k]);
+        }
+        if (err) cudaFree(err);
+    };
+    try {
+        MLEM_CUDA(cudaMalloc(&err, sizeof(uint32_t)));
+        MLEM_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), s));
+        for (int k = 0; k < 2 && nnz; ++k) {
+            MLEM_CUDA(cudaMallocHost(&host[k], sizeof(uint2) * chunk));
+            MLEM_CUDA(cudaMalloc(&dev[k], sizeof(uint2) * chunk));
+            MLEM_CUDA(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming));
+        }
+        uint64_t i = 0;
+        for (uint64_t e = 0; e < nnz; e += chunk, ++i) {
+            const int k = (int)(i & 1);
+            const uint64_t n = std::min(chunk, nnz - e);
+            if (i >= 2) MLEM_CUDA(cudaEventSynchronize(done[k]));  // staging k free again
+            read_exact(fh.f, host[k], 8 * n, "matrix elements");
+            MLEM_CUDA(cudaMemcpyAsync(dev[k], host[k], 8 * n, cudaMemcpyHostToDevice, s));
+            const unsigned grid = std::max(1u, std::min<unsigned>(ceil_div_u(n, 256), 152u * 16u));
+            k_csr4_split<<<grid, 256, 0, s>>>(dev[k], n, info.h.cols, A.idx + e,
+                                              reinterpret_cast<uint32_t*>(A.val) + e, err);
+            MLEM_LAUNCHED();
+            MLEM_CUDA(cudaEventRecord(done[k], s));
+        }
+        uint32_t h = 0;
+        MLEM_CUDA(cudaMemcpyAsync(&h, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        if (h) fail(MLEM_EIO, "csr4: column index out of range");
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
+}
+
 }  // namespace
 }  // namespace mlem
 
@@ -204,17 +293,13 @@ mlem_status mlem_csr4_write(const char* path, const mlem_csr4_scanner* sc, const
 mlem_status mlem_matrix_load_csr4(const char* path, const mlem_matrix_opts* opts, mlem_matrix** out) {
     return guarded([&] {
         MLEM_REQUIRE(path && out, MLEM_EINVAL, "NULL argument");
-        mlem_csr4_header h;
-        mlem_status st = mlem_csr4_read_header(path, &h);
-        if (st != MLEM_OK) fail(st, get_error());
-        std::vector<uint64_t> rp((uint64_t)h.rows + 1);
-        std::vector<uint32_t> col(h.nnz);
-        std::vector<float> val(h.nnz);
-        st = mlem_csr4_read(path, rp.data(), col.data(), val.data());
-        if (st != MLEM_OK) fail(st, get_error());
-        mlem_csr_host c{h.rows, h.cols, h.nnz, rp.data(), col.data(), val.data()};
-        st = mlem_matrix_create(&c, opts, out);
-        if (st != MLEM_OK) fail(st, get_error());
+        *out = nullptr;
+        mlem_matrix_opts o;
+        mlem_matrix_opts_default(&o);
+        if (opts) o = *opts;
+        const Csr4Info info = parse_header(path);
+        MLEM_REQUIRE(info.h.rows >= 1 && info.h.cols >= 1, MLEM_EINVAL, "matrix must have rows and columns");
+        *out = create_matrix_filled(o, [&](mlem_matrix* m) { csr4_ingest(path, info, m->A, m->stream); });
     });
 }
 

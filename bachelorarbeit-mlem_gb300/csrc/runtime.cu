@@ -531,6 +531,22 @@ static void upload_csr(const mlem_csr_host* c, DevCsr& A, cudaStream_t s) {
     MLEM_REQUIRE(validate_csr(A, s), MLEM_EINVAL, "csr column index >= cols or malformed row pointers");
 }
 
+mlem_matrix* create_matrix_filled(const mlem_matrix_opts& o, const std::function<void(mlem_matrix*)>& fill) {
+    DeviceGuard dg(o.device);
+    mlem_matrix* m = new_matrix(o);
+    try {
+        fill(m);
+        MLEM_CUDA(cudaStreamSynchronize(m->stream));
+        MLEM_REQUIRE(validate_csr(m->A, m->stream), MLEM_EINVAL,
+                     "csr column index >= cols or malformed row pointers");
+        postprocess_matrix(m, o);
+    } catch (...) {
+        destroy_matrix(m);
+        throw;
+    }
+    return m;
+}
+
 }  // namespace mlem
 
 using namespace mlem;

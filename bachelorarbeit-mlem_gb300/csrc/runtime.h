@@ -2,6 +2,7 @@
 #pragma once
 
 #include <condition_variable>
+#include <functional>
 #include <new>
 #include <stdexcept>
 #include <tuple>
@@ -145,4 +146,8 @@ void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, 
 void batch_put_slot(BatchState& b, uint32_t rows, uint32_t cols, uint32_t slot, const int32_t* g_dev,
                     float init, const float* f0_dev, uint32_t iters, cudaStream_t s);
 void batch_get_slot(const BatchState& b, uint32_t cols, uint32_t slot, float* f_dev, cudaStream_t s);
+// A matrix whose operand A (FP32) is filled on the device by `fill` on the
+// matrix stream, then validated and post-processed like mlem_matrix_create
+// (transpose, value type, index copies, sensitivity image).
+mlem_matrix* create_matrix_filled(const mlem_matrix_opts& o, const std::function<void(mlem_matrix*)>& fill);
 }  // namespace mlem

@@ -299,6 +299,39 @@ def reference_cuda(pkg, name, args):
     return out
 
 
+def time_csr4_ingest(pkg, m):
+    """Loading the matrix from a csr4 file (the reference's input format):
+    mlem_matrix_load_csr4 (pinned staging + GPU split) against reading the file
+    into host SoA arrays and uploading them (mlem_csr4_read + mlem_matrix_create).
+    The file is read from the page cache in both cases (written just before)."""
+    import shutil
+    import tempfile
+    d = tempfile.mkdtemp(prefix="mlem_csr4_")
+    try:
+        rp, col, val = m.csr()
+        path = os.path.join(d, "m.csr4")
+        pkg.csr4_write(path, rp, col, val, m.cols, geo=pkg.preset("cyl3d_mid"))
+        size = os.path.getsize(path)
+        del rp, col, val
+        out = {"file_bytes": size}
+        for label in ("host_path_s", "device_ingest_s"):
+            t0 = time.perf_counter()
+            if label == "device_ingest_s":
+                mm = pkg.Matrix.from_csr4(path, build_transpose=False)
+            else:
+                r, c, v, _ = pkg.csr4_read(path)
+                mm = pkg.Matrix.from_csr(r, c, v, m.cols, build_transpose=False)
+                del r, c, v
+            out[label] = time.perf_counter() - t0
+            mm.close()
+        out["device_ingest_gbs"] = size / out["device_ingest_s"] / 1e9
+        return out
+    except Exception as e:  # disk space or permissions on the host
+        return {"unavailable": str(e)[:200]}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
 def run_forms(pkg, torch, args):
     """FP16-value and batched forms (images*iterations/s)."""
     from mlem_gb300 import synth
@@ -359,6 +392,7 @@ def run_forms(pkg, torch, args):
                 b.synchronize()
                 modes[label] = {"iterations_per_s": its / (a.elapsed_time(b) * 1e-3)}
             res["modes_cyl3d_mid"] = modes
+            res["csr4_ingest_cyl3d_mid"] = time_csr4_ingest(pkg, msm)
         msm.close()
     # batched: the mid-size matrix with FP16 values, 64 sinograms, uneven iterations
     mb = pkg.Matrix.generate(pkg.preset("cyl3d_mid"), value_type=pkg.VAL_F16)

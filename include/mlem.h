@@ -96,7 +96,11 @@ mlem_status mlem_matrix_create(const mlem_csr_host* csr, const mlem_matrix_opts*
                                mlem_matrix** out);
 
 /* Reads a csr4 file (helper_files_common/csr4matrix.cpp:36-178 format) and
- * creates the device matrix from it. */
+ * creates the device matrix from it: the row offsets are read and checked on
+ * the host, the {column, value} pairs stream through pinned staging buffers
+ * and are split into the device CSR arrays on the GPU (replaces Csr4Matrix +
+ * csr_format_for_cuda, main.cu:76-79, 518-554).  Malformed files fail with
+ * MLEM_EIO, as mlem_csr4_read. */
 mlem_status mlem_matrix_load_csr4(const char* path, const mlem_matrix_opts* opts,
                                   mlem_matrix** out);
 

@@ -150,3 +150,48 @@ def test_cli_dropin(pkg, O, tmp_path):
             assert O.rel_l2(f, ref) < 1e-5
             s = float(r.stdout.split("Sum f:")[1])
             assert abs(s - float(np.sum(f, dtype=np.float32))) <= 1e-3 * abs(s)
+
+
+def test_csr4_device_ingest(pkg, O, tmp_path):
+    """mlem_matrix_load_csr4 streams the pairs through pinned staging and splits
+    them on the GPU: the device matrix equals the file, across chunk borders
+    (a 9 M-nonzero matrix spans two 8 M-pair chunks), and malformed files fail
+    with EIO like the host reader."""
+    rng = np.random.default_rng(5)
+    rows, cols = 30000, 5000
+    lens = rng.integers(0, 600, rows)
+    lens[rng.integers(0, rows, 50)] = 0
+    rp = np.zeros(rows + 1, np.uint64)
+    rp[1:] = np.cumsum(lens)
+    nnz = int(rp[-1])
+    assert nnz > (1 << 23)
+    col = np.empty(nnz, np.uint32)
+    for r in range(0, rows, 1):
+        s, t = int(rp[r]), int(rp[r + 1])
+        if t > s:
+            col[s:t] = np.sort(rng.choice(cols, t - s, replace=False))
+    val = rng.uniform(0.01, 2.0, nnz).astype(np.float32)
+    geo = pkg.preset("cyl3d_tiny")
+    path = tmp_path / "big.csr4"
+    pkg.csr4_write(path, rp, col, val, cols, geo=geo)
+    m = pkg.Matrix.from_csr4(path)
+    rp2, c2, v2 = m.csr()
+    assert np.array_equal(rp2, rp) and np.array_equal(c2, col) and np.array_equal(v2.view(np.uint32), val.view(np.uint32))
+    cp, ri, vt = m.transpose()
+    cp0, ri0, vt0 = O.transpose(rp, col, val, cols)
+    assert np.array_equal(cp, cp0) and np.array_equal(ri, ri0) and np.array_equal(vt, vt0)
+    m.close()
+    data = bytearray(path.read_bytes())
+    scan = int(np.frombuffer(bytes(data[24:28]), np.uint32)[0])
+    off = 28 + scan + 8 * rows + 8 * (nnz - 3)  # a column in the second chunk
+    data[off:off + 4] = np.uint32(cols).tobytes()
+    bad = tmp_path / "bad.csr4"
+    bad.write_bytes(bytes(data))
+    with pytest.raises(pkg.MlemError) as e:
+        pkg.Matrix.from_csr4(bad)
+    assert e.value.status == "EIO"
+    short = tmp_path / "short.csr4"
+    short.write_bytes(bytes(data[:-9]))
+    with pytest.raises(pkg.MlemError) as e:
+        pkg.Matrix.from_csr4(short)
+    assert e.value.status == "EIO"
