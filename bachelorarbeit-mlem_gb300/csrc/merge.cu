@@ -101,8 +101,13 @@ struct EpiDev {
 template <typename V>
 __device__ __forceinline__ float load_val(const V* p, uint64_t e) { return Val4<V>::one(p, e); }
 
-// One CTA per tile.  Dynamic shared memory: s_end[T*S+1] (u32, row ends
-// relative to the tile's first nonzero), s_val[T*S], s_x[T*S].
+// One CTA per tile.  Dynamic shared memory: s_end[T*S+4] (u32, row ends
+// relative to the tile's first nonzero) and s_prod[T*S] (val * x[col] of the
+// tile's nonzeros).  The staging is element by element: consecutive lanes
+// take consecutive nonzeros, so the loads are coalesced and one gather
+// instruction covers 32 consecutive columns of a row (few cache lines).  Each
+// product is formed once, and the walk along the merge path keeps the current
+// row end in a register, so it reads one shared word per nonzero.
 template <typename V>
 __global__ void __launch_bounds__(256)
 k_merge_tile(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
@@ -114,8 +119,7 @@ k_merge_tile(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ i
     const uint32_t T = blockDim.x;
     const uint32_t TS = T * S;
     uint32_t* s_end = reinterpret_cast<uint32_t*>(smem);
-    float* s_val = reinterpret_cast<float*>(smem + sizeof(uint32_t) * (TS + 4));
-    float* s_x = s_val + TS;
+    float* s_prod = reinterpret_cast<float*>(smem + sizeof(uint32_t) * (TS + 4));
     __shared__ float s_wv[32], s_inv[32];
     __shared__ int s_wk[32], s_ink[32];
 
@@ -135,8 +139,7 @@ k_merge_tile(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ i
     }
     for (uint32_t u = threadIdx.x; u < nj; u += T) {
         const uint64_t e = J0 + u;
-        s_val[u] = load_val<V>(val, e);
-        s_x[u] = __ldg(x + __ldcs(idx + e));
+        s_prod[u] = __fmul_rn(load_val<V>(val, e), __ldg(x + __ldcs(idx + e)));
     }
     __syncthreads();
 
@@ -159,9 +162,10 @@ k_merge_tile(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ i
         j = dl - lo;
         first_row = i;
         const uint32_t steps = min(S, total - dl);
+        uint32_t end_i = s_end[i];
         for (uint32_t st = 0; st < steps; ++st) {
-            if (s_end[i] > j) {
-                acc = fmaf(s_val[j], s_x[j], acc);
+            if (end_i > j) {
+                acc = __fadd_rn(acc, s_prod[j]);
                 ++j;
             } else {
                 if (!has_first) {
@@ -172,6 +176,7 @@ k_merge_tile(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ i
                 }
                 acc = 0.f;
                 ++i;
+                end_i = s_end[i];
             }
         }
     }
@@ -294,7 +299,7 @@ void merge_plan_build(const DevCsr& op, uint32_t secsize, MergePlan& plan, cudaS
     const uint64_t items = (uint64_t)op.nrows + op.nnz;
     plan.ntiles = (items + TS - 1) / TS;
     MLEM_REQUIRE(plan.ntiles < (1ull << 31), MLEM_EUNSUPPORTED, "merge path: too many tiles");
-    plan.smem = sizeof(uint32_t) * (TS + 4) + 2 * sizeof(float) * TS;
+    plan.smem = sizeof(uint32_t) * (TS + 4) + sizeof(float) * TS;
     const uint64_t nt = std::max<uint64_t>(plan.ntiles, 1);
     MLEM_CUDA(cudaMalloc(&plan.tile_i, sizeof(uint32_t) * (nt + 1)));
     MLEM_CUDA(cudaMalloc(&plan.tile_j, sizeof(uint64_t) * (nt + 1)));
@@ -418,7 +423,7 @@ extern "C" mlem_status mlem_forward_project_merge_noalloc(const uint64_t* rowptr
         p.secsize = secsize;
         p.threads = T;
         p.ntiles = ntiles;
-        p.smem = sizeof(uint32_t) * (TS + 4) + 2 * sizeof(float) * TS;
+        p.smem = sizeof(uint32_t) * (TS + 4) + sizeof(float) * TS;
         size_t off = 0;
         p.tile_i = reinterpret_cast<uint32_t*>(base + off);
         off += align256(sizeof(uint32_t) * (ntiles + 1));

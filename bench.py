@@ -172,7 +172,7 @@ def make_problem(pkg, name, torch, value_type=0, compress=False, interleave=True
     return m, geo, g, t_gen
 
 
-def time_kernels(pkg, m, torch, g_dev, f_dev, reps=10, kernel=3):
+def time_kernels(pkg, m, torch, g_dev, f_dev, reps=10, kernel=3, spmv=1):
     """Average CUDA-event duration of the FP and BP kernels (launched alone)."""
     s = torch.cuda.current_stream()
     ratio = torch.zeros(m.rows, dtype=torch.float32, device="cuda")
@@ -182,9 +182,9 @@ def time_kernels(pkg, m, torch, g_dev, f_dev, reps=10, kernel=3):
         for _ in range(2):
             if kind == "fp":
                 m.forward_project(f_dev.data_ptr(), g_dev.data_ptr(), ratio.data_ptr(), 0, stream=s.cuda_stream,
-                                  kernel=kernel)
+                                  kernel=kernel, spmv=spmv)
             else:
-                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream, kernel=kernel)
+                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream, kernel=kernel, spmv=spmv)
         times = []
         for _ in range(reps):
             a = torch.cuda.Event(enable_timing=True)
@@ -192,9 +192,9 @@ def time_kernels(pkg, m, torch, g_dev, f_dev, reps=10, kernel=3):
             a.record(s)
             if kind == "fp":
                 m.forward_project(f_dev.data_ptr(), g_dev.data_ptr(), ratio.data_ptr(), 0, stream=s.cuda_stream,
-                                  kernel=kernel)
+                                  kernel=kernel, spmv=spmv)
             else:
-                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream, kernel=kernel)
+                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream, kernel=kernel, spmv=spmv)
             b.record(s)
             b.synchronize()
             times.append(a.elapsed_time(b))
@@ -503,6 +503,10 @@ def main():
     ap.add_argument("--workload", default="cyl3d_12gb", choices=sorted(WORKLOADS))
     ap.add_argument("--forms", default="all", choices=["all", "none"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--spmv", default="csr-vector", choices=["csr-vector", "merge"],
+                    help="SpMV of the timed reconstruction (the reference's argv[8])")
+    ap.add_argument("--bp", default="trans", choices=["trans", "scatter", "fused"],
+                    help="back projection of the timed reconstruction (argv[7]; fused: single pass)")
     ap.add_argument("--no-ref-cuda", action="store_true",
                     help="reference arm: skip timing the reference's CUDA kernels")
     ap.add_argument("--no-interleave", action="store_true",
@@ -524,9 +528,13 @@ def main():
     f0_dev = torch.from_numpy(f0).cuda()
     f_dev = torch.empty_like(f0_dev)
 
+    SPMV = 0 if args.spmv == "merge" else 1
+    BP = {"trans": 0, "scatter": 1, "fused": 2}[args.bp]
+    default_form = SPMV == 1 and BP == 0
+
     def step():
         f_dev.copy_(f0_dev)
-        m.run_device(g_dev.data_ptr(), f_dev.data_ptr(), iters, stream=s.cuda_stream)
+        m.run_device(g_dev.data_ptr(), f_dev.data_ptr(), iters, stream=s.cuda_stream, spmv=SPMV, bp_mode=BP)
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -556,7 +564,7 @@ def main():
     out_pin = torch.empty(m.cols, dtype=torch.float32).pin_memory()
     import ctypes as C
     lib = pkg.load_library()
-    ro = pkg.Matrix.run_opts()
+    ro = pkg.Matrix.run_opts(spmv=SPMV, bp_mode=BP)
 
     def e2e_step():
         st = lib.mlem_run(m.handle, C.c_void_p(g_pin.data_ptr()), C.c_void_p(f0_pin.data_ptr()), iters,
@@ -578,7 +586,7 @@ def main():
     e2e_value = world * args.steps * iters / float(te.item())
 
     # roofline of the dominant kernel
-    kt = time_kernels(pkg, m, torch, g_dev, f0_dev)
+    kt = time_kernels(pkg, m, torch, g_dev, f0_dev, spmv=SPMV)
     kt_direct = time_kernels(pkg, m, torch, g_dev, f0_dev, kernel=0)
     kt_tma = time_kernels(pkg, m, torch, g_dev, f0_dev, kernel=1)
     kt_pers = time_kernels(pkg, m, torch, g_dev, f0_dev, kernel=2)
@@ -590,7 +598,7 @@ def main():
     iter_bytes = fp_b + bp_b
     traffic = None
     tf = PROFILES / "dram_traffic.json"
-    if tf.exists():
+    if tf.exists() and default_form:
         traffic = json.loads(tf.read_text()).get(f"{name}/{dom}")
 
     line = {
@@ -599,7 +607,7 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded multi-ray Siddon matrix, ellipsoid phantom, Poisson sinogram)",
         "config": {"workload": name, "rows": m.rows, "cols": m.cols, "nnz": m.nnz, "iterations_per_step": iters,
-                   "form": "fp32 plain: csr-vector FP + transposed BP", "l2": "inputs larger than L2 "
+                   "form": f"fp32 plain: {args.spmv} SpMV, {args.bp} BP", "l2": "inputs larger than L2 "
                    f"({(m.device_bytes) / 1e9:.1f} GB resident matrix)", "replicas": world,
                    "matrix_generation_s": round(t_gen, 2)},
         "e2e": {"value": e2e_value, "unit": "iter/s", "h2d_bytes_per_step": int(4 * m.rows + 4 * m.cols),
