@@ -26,6 +26,7 @@ CLI_PATH = PKG / "bin" / "mlem_gb300"
 
 SPMV_MERGE, SPMV_CSR_VECTOR = 0, 1
 KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO, KERNEL_D16, KERNEL_ILV, KERNEL_ORDERED = 0, 1, 2, 3, 4, 5, 6
+LAYOUT_NATURAL, LAYOUT_LOCALITY = 0, 1
 VAL_F32, VAL_F16, VAL_BF16 = 0, 1, 2
 BP_TRANS, BP_SCATTER, BP_FUSED = 0, 1, 2
 
@@ -48,7 +49,8 @@ class CsrHost(C.Structure):
 
 class MatrixOpts(C.Structure):
     _fields_ = [("value_type", C.c_int), ("build_transpose", C.c_uint32), ("norm", C.c_void_p),
-                ("device", C.c_int), ("compress_indices", C.c_uint32), ("interleave", C.c_uint32)]
+                ("device", C.c_int), ("compress_indices", C.c_uint32), ("interleave", C.c_uint32),
+                ("layout", C.c_uint32), ("grid_nx", C.c_uint32), ("grid_ny", C.c_uint32), ("grid_nz", C.c_uint32)]
 
 
 class MatrixInfo(C.Structure):
@@ -61,13 +63,14 @@ class RunOpts(C.Structure):
     _fields_ = [("spmv", C.c_int), ("bp_mode", C.c_int), ("secsize_fp", C.c_uint32),
                 ("secsize_bp", C.c_uint32), ("use_graph", C.c_uint32), ("loglik_every", C.c_uint32),
                 ("l2_window", C.c_uint32), ("kernel", C.c_uint32), ("lanes", C.c_uint32), ("unroll", C.c_uint32),
-                ("row_order", C.c_uint32), ("pipeline", C.c_uint32)]
+                ("row_order", C.c_uint32), ("pipeline", C.c_uint32), ("kernel_timing", C.c_uint32)]
 
 
 class Stats(C.Structure):
     _fields_ = [("seconds_total", C.c_double), ("seconds_iterations", C.c_double),
                 ("iterations", C.c_uint32), ("kernel_launches", C.c_uint32),
-                ("bytes_h2d", C.c_uint64), ("bytes_d2h", C.c_uint64), ("loglik_last", C.c_double)]
+                ("bytes_h2d", C.c_uint64), ("bytes_d2h", C.c_uint64), ("loglik_last", C.c_double),
+                ("fp_ms", C.c_double), ("bp_ms", C.c_double)]
 
 
 class Csr4Header(C.Structure):
@@ -278,13 +281,17 @@ class Matrix:
 
     # construction ---------------------------------------------------------
     @staticmethod
-    def _opts(value_type=VAL_F32, build_transpose=True, norm=None, device=0, compress=False, interleave=False):
+    def _opts(value_type=VAL_F32, build_transpose=True, norm=None, device=0, compress=False, interleave=False,
+              layout=0, grid=None):
         o = MatrixOpts()
         load_library().mlem_matrix_opts_default(C.byref(o))
         o.value_type = value_type
         o.build_transpose = 1 if build_transpose else 0
         o.compress_indices = 1 if compress else 0
         o.interleave = 1 if interleave else 0
+        o.layout = int(layout)
+        if grid is not None:
+            o.grid_nx, o.grid_ny, o.grid_nz = (int(v) for v in grid)
         keep = None
         if norm is not None:
             keep = _arr(norm, np.float32)
@@ -294,27 +301,29 @@ class Matrix:
 
     @classmethod
     def from_csr(cls, rowptr, col, val, cols: int, value_type=VAL_F32, build_transpose=True, norm=None,
-                 device=0, compress=False, interleave=False) -> "Matrix":
+                 device=0, compress=False, interleave=False, layout=LAYOUT_NATURAL, grid=None) -> "Matrix":
+        """grid = (nx, ny, nz) of the voxel columns, needed by the locality layout."""
         rowptr = _arr(rowptr, np.uint64)
         col = _arr(col, np.uint32)
         val = _arr(val, np.float32)
         csr = CsrHost(len(rowptr) - 1, cols, len(col), _ptr(rowptr), _ptr(col), _ptr(val))
-        o, keep = cls._opts(value_type, build_transpose, norm, device, compress, interleave)
+        o, keep = cls._opts(value_type, build_transpose, norm, device, compress, interleave, layout, grid)
         h = C.c_void_p()
         _check(load_library().mlem_matrix_create(C.byref(csr), C.byref(o), C.byref(h)))
         return cls(h.value)
 
     @classmethod
-    def from_csr4(cls, path, value_type=VAL_F32, build_transpose=True, norm=None, device=0) -> "Matrix":
-        o, keep = cls._opts(value_type, build_transpose, norm, device)
+    def from_csr4(cls, path, value_type=VAL_F32, build_transpose=True, norm=None, device=0,
+                  layout=LAYOUT_NATURAL) -> "Matrix":
+        o, keep = cls._opts(value_type, build_transpose, norm, device, layout=layout)
         h = C.c_void_p()
         _check(load_library().mlem_matrix_load_csr4(str(path).encode(), C.byref(o), C.byref(h)))
         return cls(h.value)
 
     @classmethod
     def generate(cls, geo: Geometry, value_type=VAL_F32, build_transpose=True, device=0,
-                 compress=False, interleave=False) -> "Matrix":
-        o, _ = cls._opts(value_type, build_transpose, None, device, compress, interleave)
+                 compress=False, interleave=False, layout=LAYOUT_NATURAL) -> "Matrix":
+        o, _ = cls._opts(value_type, build_transpose, None, device, compress, interleave, layout)
         h = C.c_void_p()
         _check(load_library().mlem_matrix_generate(C.byref(geo), C.byref(o), C.byref(h)))
         return cls(h.value)
@@ -379,13 +388,14 @@ class Matrix:
     @staticmethod
     def run_opts(spmv=SPMV_CSR_VECTOR, bp_mode=BP_TRANS, secsize_fp=5, secsize_bp=5, use_graph=True,
                  loglik_every=0, l2_window=True, kernel=KERNEL_AUTO, lanes=0, unroll=0,
-                 row_order=False, pipeline=False) -> RunOpts:
+                 row_order=False, pipeline=False, kernel_timing=False) -> RunOpts:
         o = RunOpts()
         load_library().mlem_run_opts_default(C.byref(o))
         o.spmv, o.bp_mode, o.secsize_fp, o.secsize_bp = spmv, bp_mode, secsize_fp, secsize_bp
         o.use_graph, o.loglik_every, o.l2_window = int(use_graph), loglik_every, int(l2_window)
         o.kernel, o.lanes, o.unroll, o.row_order = int(kernel), int(lanes), int(unroll), int(row_order)
         o.pipeline = int(pipeline)
+        o.kernel_timing = int(kernel_timing)
         return o
 
     def run(self, g, iterations: int, f0=None, loglik=False, stats=False, **opts):

@@ -177,36 +177,36 @@ void sc_v(const DevCsr& A, const BatchArgs& b, float* bp, cudaStream_t s) {
 __global__ void k_slot_put(int32_t* __restrict__ G, float* __restrict__ F, uint32_t rows,
                            uint32_t cols, uint32_t BT, uint32_t b, const int32_t* __restrict__ g,
                            float init, const float* __restrict__ f0, uint32_t* __restrict__ remaining,
-                           uint32_t iters) {
+                           uint32_t iters, const uint32_t* __restrict__ lor_of, const uint32_t* __restrict__ vox_of) {
     const uint32_t n = rows > cols ? rows : cols;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (i < rows) G[(uint64_t)i * BT + b] = g[i];
-        if (i < cols) F[(uint64_t)i * BT + b] = f0 ? f0[i] : init;
+        if (i < rows) G[(uint64_t)i * BT + b] = g[lor_of ? lor_of[i] : i];
+        if (i < cols) F[(uint64_t)i * BT + b] = f0 ? f0[vox_of ? vox_of[i] : i] : init;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) remaining[b] = iters;
 }
 
 __global__ void k_slot_get(const float* __restrict__ F, uint32_t cols, uint32_t BT, uint32_t b,
-                           float* __restrict__ out) {
+                           float* __restrict__ out, const uint32_t* __restrict__ vox_of) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cols; i += gridDim.x * blockDim.x)
-        out[i] = F[(uint64_t)i * BT + b];
+        out[vox_of ? vox_of[i] : i] = F[(uint64_t)i * BT + b];
 }
 
 }  // namespace
 
 void launch_slot_put(int32_t* G, float* F, uint32_t rows, uint32_t cols, uint32_t BT, uint32_t b,
                      const int32_t* g, float init, const float* f0, uint32_t* remaining,
-                     uint32_t iters, cudaStream_t s) {
+                     uint32_t iters, const uint32_t* lor_of, const uint32_t* vox_of, cudaStream_t s) {
     const uint32_t n = std::max(rows, cols);
     const unsigned grid = std::max(1u, std::min<unsigned>(ceil_div_u(n, 256), 152u * 8u));
-    k_slot_put<<<grid, 256, 0, s>>>(G, F, rows, cols, BT, b, g, init, f0, remaining, iters);
+    k_slot_put<<<grid, 256, 0, s>>>(G, F, rows, cols, BT, b, g, init, f0, remaining, iters, lor_of, vox_of);
     MLEM_LAUNCHED();
 }
 
 void launch_slot_get(const float* F, uint32_t cols, uint32_t BT, uint32_t b, float* out,
-                     cudaStream_t s) {
+                     const uint32_t* vox_of, cudaStream_t s) {
     const unsigned grid = std::max(1u, std::min<unsigned>(ceil_div_u(cols, 256), 152u * 8u));
-    k_slot_get<<<grid, 256, 0, s>>>(F, cols, BT, b, out);
+    k_slot_get<<<grid, 256, 0, s>>>(F, cols, BT, b, out, vox_of);
     MLEM_LAUNCHED();
 }
 

@@ -299,6 +299,11 @@ mlem_status mlem_matrix_load_csr4(const char* path, const mlem_matrix_opts* opts
         if (opts) o = *opts;
         const Csr4Info info = parse_header(path);
         MLEM_REQUIRE(info.h.rows >= 1 && info.h.cols >= 1, MLEM_EINVAL, "matrix must have rows and columns");
+        if (o.layout != MLEM_LAYOUT_NATURAL && o.grid_nx == 0) {  // the file's scanner configuration
+            o.grid_nx = info.h.nx;
+            o.grid_ny = info.h.ny;
+            o.grid_nz = info.h.nz;
+        }
         *out = create_matrix_filled(o, [&](mlem_matrix* m) { csr4_ingest(path, info, m->A, m->stream); });
     });
 }

@@ -112,6 +112,19 @@ void scan_counts_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t
 // indices < cols).  Returns false when the CSR is malformed.
 bool validate_csr(const DevCsr& A, cudaStream_t s);
 
+// ------------------------------------------------------------- layout.cu
+// out[k] = in[map[k]] (natural -> internal order) / out[map[k]] = in[k]
+// (internal -> natural); map[k] = natural index of internal index k.
+void launch_gather_i32(int32_t* out, const int32_t* in, const uint32_t* map, uint64_t n, cudaStream_t s);
+void launch_gather_f32(float* out, const float* in, const uint32_t* map, uint64_t n, cudaStream_t s);
+void launch_scatter_f32(float* out, const float* in, const uint32_t* map, uint64_t n, cudaStream_t s);
+// inv[map[k]] = k
+void launch_invert_perm(const uint32_t* map, uint32_t n, uint32_t* inv, cudaStream_t s);
+// out row k = in row row_src[k] (NULL: k) with columns c -> col_map[c] (NULL:
+// unchanged), sorted; *keep_t (optional) receives the transpose of out.  f32.
+void remap_csr(const DevCsr& in, const uint32_t* row_src, const uint32_t* col_map, DevCsr& out, DevCsr* keep_t,
+               cudaStream_t s);
+
 // ------------------------------------------------------------- siddon.cu
 uint64_t siddon_rows(const mlem_geometry& geo);
 void siddon_count_host(const mlem_geometry& geo, uint64_t* rowptr);
@@ -120,7 +133,8 @@ void siddon_generate_device(const mlem_geometry& geo, DevCsr& A, cudaStream_t s)
 // Locality-friendly processing orders for a generated matrix: LORs in 4x4
 // detector tubes (rows of A) and voxels in 4x2x2 bricks (rows of Aᵀ).
 std::vector<uint32_t> siddon_lor_order(const mlem_geometry& geo);
-std::vector<uint32_t> voxel_brick_order(uint32_t nx, uint32_t ny, uint32_t nz);
+std::vector<uint32_t> voxel_brick_order(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t bx = 4, uint32_t by = 2,
+                                        uint32_t bz = 2);
 
 // ------------------------------------------------------------- batch.cu
 // Interleaved batch state: slot b of voxel c is f[c*tile + b]; g and ratio
@@ -145,11 +159,13 @@ void launch_batch_update_zero(const float* norm, uint32_t cols, const BatchArgs&
                               cudaStream_t s);
 // Slot b <- sinogram g (contiguous), image f0 (contiguous) or the constant init,
 // and its iteration count; slot b -> contiguous image.
+// lor_of / vox_of (may be NULL): natural index of each internal row / column
+// of a matrix in the locality layout; g, f0 and out are in natural order.
 void launch_slot_put(int32_t* G, float* F, uint32_t rows, uint32_t cols, uint32_t BT, uint32_t b,
                      const int32_t* g, float init, const float* f0, uint32_t* remaining,
-                     uint32_t iters, cudaStream_t s);
+                     uint32_t iters, const uint32_t* lor_of, const uint32_t* vox_of, cudaStream_t s);
 void launch_slot_get(const float* F, uint32_t cols, uint32_t BT, uint32_t b, float* out,
-                     cudaStream_t s);
+                     const uint32_t* vox_of, cudaStream_t s);
 
 }  // namespace mlem
 

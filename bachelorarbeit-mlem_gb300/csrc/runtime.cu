@@ -43,6 +43,8 @@ void Workspace::release() {
     cudaFree(ll_part);
     cudaFree(ll_vals);
     cudaFree(err);
+    cudaFree(tmp_rows);
+    cudaFree(tmp_cols);
     *this = Workspace();
 }
 
@@ -115,8 +117,43 @@ void ensure_workspace(mlem_matrix* m) {
     MLEM_CUDA(cudaMemsetAsync(w.err, 0, sizeof(uint32_t), m->stream));
     MLEM_CUDA(cudaMemsetAsync(w.bp, 0, sizeof(float) * C, m->stream));
     MLEM_CUDA(cudaMemsetAsync(w.ratio, 0, sizeof(float) * R, m->stream));
+    if (m->lor_of || m->vox_of) {
+        MLEM_CUDA(cudaMalloc(&w.tmp_rows, sizeof(float) * R));
+        MLEM_CUDA(cudaMalloc(&w.tmp_cols, sizeof(float) * C));
+    }
+    MLEM_CUDA(cudaStreamSynchronize(m->stream));
     w.ready = true;
 }
+
+// Entry-point permutations (identity copies when the matrix keeps its
+// natural layout).  *_in: natural -> internal, *_out: internal -> natural;
+// dst and src never alias.
+static void rows_in_i32(const mlem_matrix* m, int32_t* dst, const int32_t* src, cudaStream_t s) {
+    const uint64_t n = m->A.nrows;
+    if (m->lor_of) launch_gather_i32(dst, src, m->lor_of, n, s);
+    else MLEM_CUDA(cudaMemcpyAsync(dst, src, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
+}
+static void rows_in_f32(const mlem_matrix* m, float* dst, const float* src, cudaStream_t s) {
+    const uint64_t n = m->A.nrows;
+    if (m->lor_of) launch_gather_f32(dst, src, m->lor_of, n, s);
+    else MLEM_CUDA(cudaMemcpyAsync(dst, src, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+}
+static void rows_out(const mlem_matrix* m, float* dst, const float* src, cudaStream_t s) {
+    const uint64_t n = m->A.nrows;
+    if (m->lor_of) launch_scatter_f32(dst, src, m->lor_of, n, s);
+    else MLEM_CUDA(cudaMemcpyAsync(dst, src, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+}
+static void cols_in(const mlem_matrix* m, float* dst, const float* src, cudaStream_t s) {
+    const uint64_t n = m->A.ncols;
+    if (m->vox_of) launch_gather_f32(dst, src, m->vox_of, n, s);
+    else MLEM_CUDA(cudaMemcpyAsync(dst, src, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+}
+static void cols_out(const mlem_matrix* m, float* dst, const float* src, cudaStream_t s) {
+    const uint64_t n = m->A.ncols;
+    if (m->vox_of) launch_scatter_f32(dst, src, m->vox_of, n, s);
+    else MLEM_CUDA(cudaMemcpyAsync(dst, src, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+}
+static bool permuted(const mlem_matrix* m) { return m->lor_of || m->vox_of; }
 
 const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
     auto& plans = transposed ? m->plan_AT : m->plan_A;
@@ -306,7 +343,32 @@ void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, 
 }
 
 // One MLEM iteration on stream s using the matrix workspace.
-void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, double* ll_slot) {
+void StageTimer::record(cudaStream_t s) {
+    cudaEvent_t e = nullptr;
+    MLEM_CUDA(cudaEventCreate(&e));
+    ev.push_back(e);
+    MLEM_CUDA(cudaEventRecord(e, s));
+}
+
+void StageTimer::means(double& fp_ms, double& bp_ms) const {
+    double a = 0.0, b = 0.0;
+    const size_t n = ev.size() / 4;
+    for (size_t i = 0; i < n; ++i) {
+        float x = 0.f, y = 0.f;
+        MLEM_CUDA(cudaEventElapsedTime(&x, ev[4 * i], ev[4 * i + 1]));
+        MLEM_CUDA(cudaEventElapsedTime(&y, ev[4 * i + 2], ev[4 * i + 3]));
+        a += x;
+        b += y;
+    }
+    fp_ms = n ? a / n : std::numeric_limits<double>::quiet_NaN();
+    bp_ms = n ? b / n : std::numeric_limits<double>::quiet_NaN();
+}
+
+StageTimer::~StageTimer() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+}
+
+void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, double* ll_slot, StageTimer* timer) {
     Workspace& w = m->ws;
     const DevCsr& A = m->A;
     const bool want_ll = ll_slot != nullptr;
@@ -316,15 +378,26 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
         wr = {w.ratio, sizeof(float) * (size_t)A.nrows};
     }
     if (o.bp_mode == MLEM_BP_FUSED) {
+        if (timer) timer->record(s);
         launch_fused_fp_scatter(A, w.f, w.g, w.bp, want_ll ? w.fwproj : nullptr, wf, s);
+        if (timer) {
+            timer->record(s);
+            timer->record(s);
+        }
         launch_update_zero(w.f, w.bp, m->norm, A.ncols, s);
+        if (timer) timer->record(s);
     } else {
         EpiArgs fe;
         fe.kind = Epi::Correl;
         fe.g = w.g;
         fe.out = w.ratio;
         fe.fwproj = want_ll ? w.fwproj : nullptr;
+        if (timer) timer->record(s);
         project(m, false, w.f, fe, o, wf, s);
+        if (timer) {
+            timer->record(s);
+            timer->record(s);
+        }
         if (o.bp_mode == MLEM_BP_TRANS) {
             EpiArgs be;
             be.kind = Epi::Update;
@@ -335,6 +408,7 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
             launch_scatter(A, w.ratio, w.bp, pick_lanes(A.nnz, A.nrows), wr, s);
             launch_update_zero(w.f, w.bp, m->norm, A.ncols, s);
         }
+        if (timer) timer->record(s);
     }
     if (want_ll) launch_loglik(w.g, w.fwproj, A.nrows, w.ll_part, ll_slot, s);
 }
@@ -367,11 +441,11 @@ static void enable_l2_persisting(int dev) {
 
 // Runs `iters` iterations on the workspace (g and f already in place).
 static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
-                     double* ll_dev) {
-    if (o.loglik_every > 0 || !o.use_graph) {
+                     double* ll_dev, StageTimer* timer = nullptr) {
+    if (o.loglik_every > 0 || !o.use_graph || timer) {
         for (uint32_t it = 0; it < iters; ++it) {
             double* slot = (o.loglik_every > 0 && it % o.loglik_every == 0) ? ll_dev + it : nullptr;
-            enqueue_iteration(m, o, s, slot);
+            enqueue_iteration(m, o, s, slot, timer);
         }
         return;
     }
@@ -429,7 +503,7 @@ static void postprocess_matrix(mlem_matrix* m, const mlem_matrix_opts& o) {
     cudaStream_t s = m->stream;
     DevCsr& A = m->A;
     A.max_row = max_row_length(A.rowptr, A.nrows, s);
-    if (o.build_transpose) {
+    if (o.build_transpose && !m->has_t) {
         transpose_device(A, m->AT, s);
         m->has_t = true;
     }
@@ -458,24 +532,95 @@ static void postprocess_matrix(mlem_matrix* m, const mlem_matrix_opts& o) {
         if (m->has_t) build_ilv(m->AT, s);
     }
     MLEM_CUDA(cudaMalloc(&m->norm, sizeof(float) * std::max<uint32_t>(A.ncols, 1)));
-    if (o.norm) {
-        MLEM_CUDA(cudaMemcpyAsync(m->norm, o.norm, sizeof(float) * A.ncols, cudaMemcpyHostToDevice, s));
-    } else if (m->has_t) {
-        colsum_from_transpose(m->AT, m->norm, s);
-    } else {
-        colsum_scatter(A, m->norm, s);
-    }
     m->norm_host.resize(A.ncols);
-    if (A.ncols)
-        MLEM_CUDA(cudaMemcpyAsync(m->norm_host.data(), m->norm, sizeof(float) * A.ncols,
-                                  cudaMemcpyDeviceToHost, s));
+    if (o.norm) {
+        // given in natural column order
+        if (m->vox_of && A.ncols) {
+            float* nat = nullptr;
+            MLEM_CUDA(cudaMalloc(&nat, sizeof(float) * A.ncols));
+            MLEM_CUDA(cudaMemcpyAsync(nat, o.norm, sizeof(float) * A.ncols, cudaMemcpyHostToDevice, s));
+            launch_gather_f32(m->norm, nat, m->vox_of, A.ncols, s);
+            MLEM_CUDA(cudaStreamSynchronize(s));
+            cudaFree(nat);
+        } else {
+            MLEM_CUDA(cudaMemcpyAsync(m->norm, o.norm, sizeof(float) * A.ncols, cudaMemcpyHostToDevice, s));
+        }
+        std::copy(o.norm, o.norm + A.ncols, m->norm_host.begin());
+    } else {
+        if (m->has_t) colsum_from_transpose(m->AT, m->norm, s);
+        else colsum_scatter(A, m->norm, s);
+        if (A.ncols)
+            MLEM_CUDA(cudaMemcpyAsync(m->norm_host.data(), m->norm, sizeof(float) * A.ncols,
+                                      cudaMemcpyDeviceToHost, s));
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        if (m->vox_of) {  // back to natural order for the host copy
+            std::vector<float> internal(m->norm_host);
+            for (uint32_t p = 0; p < A.ncols; ++p) m->norm_host[m->vox_of_host[p]] = internal[p];
+        }
+    }
     MLEM_CUDA(cudaStreamSynchronize(s));
+}
+
+// Puts A (natural order, f32) into the locality layout.  lor: natural row of
+// every internal row (empty = keep the row order); vox: natural column of
+// every internal column.  keep_t: keep the transpose built on the way as Aᵀ.
+static void apply_layout(mlem_matrix* m, const std::vector<uint32_t>& lor, const std::vector<uint32_t>& vox,
+                         bool keep_t) {
+    cudaStream_t s = m->stream;
+    DevCsr& A = m->A;
+    MLEM_REQUIRE(A.vt == MLEM_VAL_F32, MLEM_EINVAL, "internal: layout before value conversion");
+    MLEM_REQUIRE(lor.empty() || lor.size() == A.nrows, MLEM_EINVAL, "internal: row order size");
+    MLEM_REQUIRE(vox.size() == A.ncols, MLEM_EINVAL,
+                 "locality layout: the voxel grid (nx*ny*nz) does not match the number of columns");
+    std::vector<uint32_t> pos(A.ncols, UINT32_MAX);
+    for (uint32_t p = 0; p < A.ncols; ++p) {
+        MLEM_REQUIRE(vox[p] < A.ncols && pos[vox[p]] == UINT32_MAX, MLEM_EINVAL, "internal: voxel order");
+        pos[vox[p]] = p;
+    }
+    uint32_t* d_pos = nullptr;
+    try {
+        if (!lor.empty()) {
+            MLEM_CUDA(cudaMalloc(&m->lor_of, sizeof(uint32_t) * lor.size()));
+            MLEM_CUDA(cudaMemcpy(m->lor_of, lor.data(), sizeof(uint32_t) * lor.size(), cudaMemcpyHostToDevice));
+        }
+        MLEM_CUDA(cudaMalloc(&m->vox_of, sizeof(uint32_t) * std::max<size_t>(vox.size(), 1)));
+        MLEM_CUDA(cudaMalloc(&d_pos, sizeof(uint32_t) * std::max<size_t>(pos.size(), 1)));
+        if (!vox.empty()) {
+            MLEM_CUDA(cudaMemcpy(m->vox_of, vox.data(), sizeof(uint32_t) * vox.size(), cudaMemcpyHostToDevice));
+            MLEM_CUDA(cudaMemcpy(d_pos, pos.data(), sizeof(uint32_t) * pos.size(), cudaMemcpyHostToDevice));
+        }
+        DevCsr An, Tn;
+        remap_csr(A, m->lor_of, d_pos, An, keep_t ? &Tn : nullptr, s);
+        free_csr(A);
+        A = An;
+        if (keep_t) {
+            m->AT = Tn;
+            m->has_t = true;
+        }
+    } catch (...) {
+        cudaFree(d_pos);
+        throw;
+    }
+    cudaFree(d_pos);
+    m->vox_of_host = vox;
+}
+
+// The layout the options ask for, given the voxel grid (and, for generated
+// matrices, the LOR order).
+static void maybe_apply_layout(mlem_matrix* m, const mlem_matrix_opts& o, uint32_t nx, uint32_t ny, uint32_t nz,
+                               const std::vector<uint32_t>& lor) {
+    if (o.layout == MLEM_LAYOUT_NATURAL) return;
+    MLEM_REQUIRE(nx && ny && nz && (uint64_t)nx * ny * nz == m->A.ncols, MLEM_EINVAL,
+                 "locality layout needs the voxel grid: nx*ny*nz must equal the number of columns");
+    apply_layout(m, lor, voxel_brick_order(nx, ny, nz, 4, 4, 2), o.build_transpose != 0);
 }
 
 static mlem_matrix* new_matrix(const mlem_matrix_opts& o) {
     MLEM_REQUIRE(o.value_type == MLEM_VAL_F32 || o.value_type == MLEM_VAL_F16 ||
                      o.value_type == MLEM_VAL_BF16,
                  MLEM_EINVAL, "value_type must be F32, F16 or BF16");
+    MLEM_REQUIRE(o.layout == MLEM_LAYOUT_NATURAL || o.layout == MLEM_LAYOUT_LOCALITY, MLEM_EINVAL,
+                 "layout must be 0 (natural) or 1 (locality)");
     int ndev = 0;
     MLEM_CUDA(cudaGetDeviceCount(&ndev));
     MLEM_REQUIRE(o.device >= 0 && o.device < ndev, MLEM_EINVAL, "device ordinal out of range");
@@ -496,6 +641,8 @@ static void destroy_matrix(mlem_matrix* m) {
     free_csr(m->A);
     free_csr(m->AT);
     cudaFree(m->norm);
+    cudaFree(m->lor_of);
+    cudaFree(m->vox_of);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
 }
@@ -539,6 +686,7 @@ mlem_matrix* create_matrix_filled(const mlem_matrix_opts& o, const std::function
         MLEM_CUDA(cudaStreamSynchronize(m->stream));
         MLEM_REQUIRE(validate_csr(m->A, m->stream), MLEM_EINVAL,
                      "csr column index >= cols or malformed row pointers");
+        maybe_apply_layout(m, o, o.grid_nx, o.grid_ny, o.grid_nz, {});
         postprocess_matrix(m, o);
     } catch (...) {
         destroy_matrix(m);
@@ -573,6 +721,8 @@ void mlem_matrix_opts_default(mlem_matrix_opts* o) {
     o->device = 0;
     o->compress_indices = 0;
     o->interleave = 0;
+    o->layout = MLEM_LAYOUT_NATURAL;
+    o->grid_nx = o->grid_ny = o->grid_nz = 0;
 }
 
 void mlem_run_opts_default(mlem_run_opts* o) {
@@ -589,6 +739,7 @@ void mlem_run_opts_default(mlem_run_opts* o) {
     o->unroll = 0;
     o->row_order = 0;
     o->pipeline = 0;
+    o->kernel_timing = 0;
 }
 
 mlem_status mlem_matrix_create(const mlem_csr_host* csr, const mlem_matrix_opts* opts, mlem_matrix** out) {
@@ -603,6 +754,7 @@ mlem_status mlem_matrix_create(const mlem_csr_host* csr, const mlem_matrix_opts*
         mlem_matrix* m = new_matrix(o);
         try {
             upload_csr(csr, m->A, m->stream);
+            maybe_apply_layout(m, o, o.grid_nx, o.grid_ny, o.grid_nz, {});
             postprocess_matrix(m, o);
         } catch (...) {
             destroy_matrix(m);
@@ -624,15 +776,20 @@ mlem_status mlem_matrix_generate(const mlem_geometry* geo, const mlem_matrix_opt
         try {
             siddon_generate_device(*geo, m->A, m->stream);
             MLEM_REQUIRE(m->A.nrows >= 1, MLEM_EINVAL, "geometry produced no rows");
+            maybe_apply_layout(m, o, geo->nx, geo->ny, geo->nz, siddon_lor_order(*geo));
             postprocess_matrix(m, o);
-            // locality orders of the rows: LOR tubes for A, voxel bricks for Aᵀ
-            auto upload = [&](DevCsr& op, const std::vector<uint32_t>& ord) {
-                if (ord.size() != op.nrows || op.nrows == 0) return;
-                MLEM_CUDA(cudaMalloc(&op.order, sizeof(uint32_t) * ord.size()));
-                MLEM_CUDA(cudaMemcpy(op.order, ord.data(), sizeof(uint32_t) * ord.size(), cudaMemcpyHostToDevice));
-            };
-            upload(m->A, siddon_lor_order(*geo));
-            if (m->has_t) upload(m->AT, voxel_brick_order(geo->nx, geo->ny, geo->nz));
+            if (o.layout == MLEM_LAYOUT_NATURAL) {
+                // locality orders of the rows (processing order only): LOR
+                // tubes for A, voxel bricks for Aᵀ
+                auto upload = [&](DevCsr& op, const std::vector<uint32_t>& ord) {
+                    if (ord.size() != op.nrows || op.nrows == 0) return;
+                    MLEM_CUDA(cudaMalloc(&op.order, sizeof(uint32_t) * ord.size()));
+                    MLEM_CUDA(cudaMemcpy(op.order, ord.data(), sizeof(uint32_t) * ord.size(),
+                                         cudaMemcpyHostToDevice));
+                };
+                upload(m->A, siddon_lor_order(*geo));
+                if (m->has_t) upload(m->AT, voxel_brick_order(geo->nx, geo->ny, geo->nz));
+            }
         } catch (...) {
             destroy_matrix(m);
             throw;
@@ -685,23 +842,72 @@ mlem_status mlem_matrix_get_norm(const mlem_matrix* m, float* norm_out) {
     });
 }
 
+namespace mlem {
+// Copies a device operand to host CSR arrays (values converted to f32).
+static void copy_csr_to_host(const DevCsr& c, uint64_t* rowptr, uint32_t* idx, float* val, cudaStream_t s) {
+    MLEM_CUDA(cudaMemcpy(rowptr, c.rowptr, sizeof(uint64_t) * ((uint64_t)c.nrows + 1), cudaMemcpyDeviceToHost));
+    if (!c.nnz) return;
+    MLEM_CUDA(cudaMemcpy(idx, c.idx, sizeof(uint32_t) * c.nnz, cudaMemcpyDeviceToHost));
+    float* tmp = nullptr;
+    MLEM_CUDA(cudaMalloc(&tmp, sizeof(float) * c.nnz));
+    convert_values_back(c.val, tmp, c.vt, c.nnz, s);
+    MLEM_CUDA(cudaStreamSynchronize(s));
+    const cudaError_t e = cudaMemcpy(val, tmp, sizeof(float) * c.nnz, cudaMemcpyDeviceToHost);
+    cudaFree(tmp);
+    MLEM_CUDA(e);
+}
+
+// A (transposed = false) or Aᵀ of a matrix in the locality layout, back in
+// natural order, as a new f32 device CSR.
+static DevCsr natural_operand(const mlem_matrix* m, bool transposed) {
+    cudaStream_t s = m->stream;
+    const DevCsr& src = transposed ? m->AT : m->A;
+    const uint32_t* perm_rows = transposed ? m->vox_of : m->lor_of;  // natural index of internal rows
+    const uint32_t* col_map = transposed ? m->lor_of : m->vox_of;    // internal column -> natural
+    DevCsr view = src, out;
+    float* v32 = nullptr;
+    uint32_t* inv = nullptr;
+    try {
+        if (src.vt != MLEM_VAL_F32) {
+            MLEM_CUDA(cudaMalloc(&v32, sizeof(float) * padded(src.nnz)));
+            convert_values_back(src.val, v32, src.vt, padded(src.nnz), s);
+            view.val = v32;
+            view.vt = MLEM_VAL_F32;
+        }
+        if (perm_rows) {
+            MLEM_CUDA(cudaMalloc(&inv, sizeof(uint32_t) * std::max<uint32_t>(src.nrows, 1)));
+            launch_invert_perm(perm_rows, src.nrows, inv, s);
+        }
+        remap_csr(view, inv, col_map, out, nullptr, s);
+    } catch (...) {
+        cudaStreamSynchronize(s);
+        cudaFree(v32);
+        cudaFree(inv);
+        throw;
+    }
+    cudaFree(v32);
+    cudaFree(inv);
+    return out;
+}
+}  // namespace mlem
+
 mlem_status mlem_matrix_get_transpose(const mlem_matrix* m, uint64_t* colptr, uint32_t* rowidx, float* val) {
     return guarded([&] {
         MLEM_REQUIRE(m && colptr && rowidx && val, MLEM_EINVAL, "NULL argument");
         MLEM_REQUIRE(m->has_t, MLEM_EINVAL, "matrix has no transpose");
         DeviceGuard dg(m->device);
-        const DevCsr& T = m->AT;
-        MLEM_CUDA(cudaMemcpy(colptr, T.rowptr, sizeof(uint64_t) * ((uint64_t)T.nrows + 1), cudaMemcpyDeviceToHost));
-        if (T.nnz) {
-            MLEM_CUDA(cudaMemcpy(rowidx, T.idx, sizeof(uint32_t) * T.nnz, cudaMemcpyDeviceToHost));
-            float* tmp = nullptr;
-            MLEM_CUDA(cudaMalloc(&tmp, sizeof(float) * T.nnz));
-            convert_values_back(T.val, tmp, T.vt, T.nnz, m->stream);
-            MLEM_CUDA(cudaStreamSynchronize(m->stream));
-            const cudaError_t e = cudaMemcpy(val, tmp, sizeof(float) * T.nnz, cudaMemcpyDeviceToHost);
-            cudaFree(tmp);
-            MLEM_CUDA(e);
+        if (!permuted(m)) {
+            copy_csr_to_host(m->AT, colptr, rowidx, val, m->stream);
+            return;
         }
+        DevCsr nat = natural_operand(m, true);
+        try {
+            copy_csr_to_host(nat, colptr, rowidx, val, m->stream);
+        } catch (...) {
+            free_csr(nat);
+            throw;
+        }
+        free_csr(nat);
     });
 }
 
@@ -709,18 +915,18 @@ mlem_status mlem_matrix_get_csr(const mlem_matrix* m, uint64_t* rowptr, uint32_t
     return guarded([&] {
         MLEM_REQUIRE(m && rowptr && col && val, MLEM_EINVAL, "NULL argument");
         DeviceGuard dg(m->device);
-        const DevCsr& A = m->A;
-        MLEM_CUDA(cudaMemcpy(rowptr, A.rowptr, sizeof(uint64_t) * ((uint64_t)A.nrows + 1), cudaMemcpyDeviceToHost));
-        if (A.nnz) {
-            MLEM_CUDA(cudaMemcpy(col, A.idx, sizeof(uint32_t) * A.nnz, cudaMemcpyDeviceToHost));
-            float* tmp = nullptr;
-            MLEM_CUDA(cudaMalloc(&tmp, sizeof(float) * A.nnz));
-            convert_values_back(A.val, tmp, A.vt, A.nnz, m->stream);
-            MLEM_CUDA(cudaStreamSynchronize(m->stream));
-            const cudaError_t e = cudaMemcpy(val, tmp, sizeof(float) * A.nnz, cudaMemcpyDeviceToHost);
-            cudaFree(tmp);
-            MLEM_CUDA(e);
+        if (!permuted(m)) {
+            copy_csr_to_host(m->A, rowptr, col, val, m->stream);
+            return;
         }
+        DevCsr nat = natural_operand(m, false);
+        try {
+            copy_csr_to_host(nat, rowptr, col, val, m->stream);
+        } catch (...) {
+            free_csr(nat);
+            throw;
+        }
+        free_csr(nat);
     });
 }
 
@@ -748,10 +954,22 @@ mlem_status mlem_run(mlem_matrix* m, const int32_t* g, const float* f0, uint32_t
         const uint32_t rows = m->A.nrows, cols = m->A.ncols;
         Workspace& w = m->ws;
         if (o.spmv == MLEM_SPMV_CSR_VECTOR) prepare_kernel(m, o);
-        MLEM_CUDA(cudaMemcpyAsync(w.g, g, sizeof(int32_t) * rows, cudaMemcpyHostToDevice, s));
+        const bool perm = permuted(m);
+        if (perm) {  // natural order staged, then permuted into the workspace
+            int32_t* gt = reinterpret_cast<int32_t*>(w.tmp_rows);
+            MLEM_CUDA(cudaMemcpyAsync(gt, g, sizeof(int32_t) * rows, cudaMemcpyHostToDevice, s));
+            rows_in_i32(m, w.g, gt, s);
+        } else {
+            MLEM_CUDA(cudaMemcpyAsync(w.g, g, sizeof(int32_t) * rows, cudaMemcpyHostToDevice, s));
+        }
         uint64_t h2d = sizeof(int32_t) * (uint64_t)rows;
         if (f0) {
-            MLEM_CUDA(cudaMemcpyAsync(w.f, f0, sizeof(float) * cols, cudaMemcpyHostToDevice, s));
+            if (perm) {
+                MLEM_CUDA(cudaMemcpyAsync(w.tmp_cols, f0, sizeof(float) * cols, cudaMemcpyHostToDevice, s));
+                cols_in(m, w.f, w.tmp_cols, s);
+            } else {
+                MLEM_CUDA(cudaMemcpyAsync(w.f, f0, sizeof(float) * cols, cudaMemcpyHostToDevice, s));
+            }
             h2d += sizeof(float) * (uint64_t)cols;
         } else {
             std::vector<float> init(cols, reference_initial_value(m, g));
@@ -774,11 +992,17 @@ mlem_status mlem_run(mlem_matrix* m, const int32_t* g, const float* f0, uint32_t
         MLEM_CUDA(cudaEventCreate(&e0));
         MLEM_CUDA(cudaEventCreate(&e1));
         const uint64_t l0 = g_launches.load();
+        StageTimer timer;
         MLEM_CUDA(cudaEventRecord(e0, s));
-        run_loop(m, o, iterations, s, w.ll_vals);
+        run_loop(m, o, iterations, s, w.ll_vals, o.kernel_timing ? &timer : nullptr);
         MLEM_CUDA(cudaEventRecord(e1, s));
         const uint64_t l1 = g_launches.load();
-        MLEM_CUDA(cudaMemcpyAsync(f_out, w.f, sizeof(float) * cols, cudaMemcpyDeviceToHost, s));
+        if (perm) {
+            cols_out(m, w.tmp_cols, w.f, s);
+            MLEM_CUDA(cudaMemcpyAsync(f_out, w.tmp_cols, sizeof(float) * cols, cudaMemcpyDeviceToHost, s));
+        } else {
+            MLEM_CUDA(cudaMemcpyAsync(f_out, w.f, sizeof(float) * cols, cudaMemcpyDeviceToHost, s));
+        }
         std::vector<double> ll;
         if (o.loglik_every > 0) {
             ll.resize(iterations);
@@ -803,6 +1027,7 @@ mlem_status mlem_run(mlem_matrix* m, const int32_t* g, const float* f0, uint32_t
             stats->bytes_h2d = h2d;
             stats->bytes_d2h = sizeof(float) * (uint64_t)cols;
             stats->loglik_last = std::numeric_limits<double>::quiet_NaN();
+            timer.means(stats->fp_ms, stats->bp_ms);
             for (uint32_t i = iterations; i-- > 0;)
                 if (!ll.empty() && !std::isnan(ll[i])) {
                     stats->loglik_last = ll[i];
@@ -829,10 +1054,12 @@ mlem_status mlem_run_device(mlem_matrix* m, const int32_t* g_dev, float* f_dev, 
         const uint32_t rows = m->A.nrows, cols = m->A.ncols;
         Workspace& w = m->ws;
         if (o.spmv == MLEM_SPMV_CSR_VECTOR) prepare_kernel(m, o);
-        MLEM_CUDA(cudaMemcpyAsync(w.g, g_dev, sizeof(int32_t) * rows, cudaMemcpyDeviceToDevice, s));
-        MLEM_CUDA(cudaMemcpyAsync(w.f, f_dev, sizeof(float) * cols, cudaMemcpyDeviceToDevice, s));
+        (void)rows;
+        (void)cols;
+        rows_in_i32(m, w.g, g_dev, s);
+        cols_in(m, w.f, f_dev, s);
         run_loop(m, o, iterations, s, nullptr);
-        MLEM_CUDA(cudaMemcpyAsync(f_dev, w.f, sizeof(float) * cols, cudaMemcpyDeviceToDevice, s));
+        cols_out(m, f_dev, w.f, s);
     });
 }
 
@@ -847,13 +1074,26 @@ mlem_status mlem_forward_project(mlem_matrix* m, const float* f_dev, const int32
         std::lock_guard<std::mutex> lk(m->mu);
         DeviceGuard dg(m->device);
         cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (o.spmv == MLEM_SPMV_CSR_VECTOR) prepare_kernel(m, o);
         EpiArgs fe;
         fe.kind = Epi::Correl;
-        fe.g = g_dev;
-        fe.out = ratio_dev;
-        fe.fwproj = fwproj_out_dev;
-        if (o.spmv == MLEM_SPMV_CSR_VECTOR) prepare_kernel(m, o);
-        project(m, false, f_dev, fe, o, {}, s);
+        if (!permuted(m)) {
+            fe.g = g_dev;
+            fe.out = ratio_dev;
+            fe.fwproj = fwproj_out_dev;
+            project(m, false, f_dev, fe, o, {}, s);
+        } else {  // internal order in the workspace, natural order at the boundary
+            ensure_workspace(m);
+            Workspace& w = m->ws;
+            cols_in(m, w.tmp_cols, f_dev, s);
+            rows_in_i32(m, w.g, g_dev, s);
+            fe.g = w.g;
+            fe.out = w.tmp_rows;
+            fe.fwproj = fwproj_out_dev ? w.fwproj : nullptr;
+            project(m, false, w.tmp_cols, fe, o, {}, s);
+            rows_out(m, ratio_dev, w.tmp_rows, s);
+            if (fwproj_out_dev) rows_out(m, fwproj_out_dev, w.fwproj, s);
+        }
     });
 }
 
@@ -868,16 +1108,26 @@ mlem_status mlem_back_project(mlem_matrix* m, const float* ratio_dev, float* bp_
         std::lock_guard<std::mutex> lk(m->mu);
         DeviceGuard dg(m->device);
         cudaStream_t s = static_cast<cudaStream_t>(stream);
+        const bool perm = permuted(m);
+        const float* r = ratio_dev;
+        float* out = bp_dev;
+        if (perm) {  // internal order in the workspace, natural order at the boundary
+            ensure_workspace(m);
+            rows_in_f32(m, m->ws.tmp_rows, ratio_dev, s);
+            r = m->ws.tmp_rows;
+            out = m->ws.tmp_cols;
+        }
         if (o.bp_mode == MLEM_BP_TRANS) {
             EpiArgs be;
             be.kind = Epi::Raw;
-            be.out = bp_dev;
+            be.out = out;
             if (o.spmv == MLEM_SPMV_CSR_VECTOR) prepare_kernel(m, o);
-            project(m, true, ratio_dev, be, o, {}, s);
+            project(m, true, r, be, o, {}, s);
         } else {
-            MLEM_CUDA(cudaMemsetAsync(bp_dev, 0, sizeof(float) * m->A.ncols, s));
-            launch_scatter(m->A, ratio_dev, bp_dev, pick_lanes(m->A.nnz, m->A.nrows), {}, s);
+            MLEM_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * m->A.ncols, s));
+            launch_scatter(m->A, r, out, pick_lanes(m->A.nnz, m->A.nrows), {}, s);
         }
+        if (perm) cols_out(m, bp_dev, out, s);
     });
 }
 

@@ -66,6 +66,8 @@ struct Workspace {
     double* ll_vals = nullptr; // [ll_cap]
     uint32_t ll_cap = 0;
     uint32_t* err = nullptr;   // set by kernels whose bounded waits expired
+    float* tmp_rows = nullptr; // [rows] staging in natural order (locality layout only)
+    float* tmp_cols = nullptr; // [cols] staging in natural order (locality layout only)
     std::map<RunKey, cudaGraphExec_t> graphs;
     std::map<RunKey, uint64_t> graph_nodes;
     void release();
@@ -116,7 +118,12 @@ struct mlem_matrix {
     mlem::DevCsr A, AT;
     bool has_t = false;
     float* norm = nullptr;
-    std::vector<float> norm_host;     // host copy (initial value computation)
+    std::vector<float> norm_host;     // host copy in natural column order (initial value)
+    // Locality layout: natural row / column of each internal row / column
+    // (NULL = natural order).
+    uint32_t* lor_of = nullptr;       // [rows]
+    uint32_t* vox_of = nullptr;       // [cols]
+    std::vector<uint32_t> vox_of_host;
     cudaStream_t stream = nullptr;
     mlem::Workspace ws;
     std::map<uint32_t, mlem::MergePlan> plan_A, plan_AT;
@@ -131,7 +138,16 @@ namespace mlem {
 // Shared by the single, batched and server paths.
 void ensure_workspace(mlem_matrix* m);
 const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize);
-void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, double* ll_slot);
+// CUDA events around the forward and back projection stages of eager
+// iterations (mlem_run_opts.kernel_timing).
+struct StageTimer {
+    std::vector<cudaEvent_t> ev;  // 4 per iteration: FP start/end, BP start/end
+    void record(cudaStream_t s);
+    void means(double& fp_ms, double& bp_ms) const;
+    ~StageTimer();
+};
+void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, double* ll_slot,
+                       StageTimer* timer = nullptr);
 void enqueue_batch_iteration(mlem_matrix* m, BatchState& b, cudaStream_t s);
 float reference_initial_value(const mlem_matrix* m, const int32_t* g);
 void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o);
@@ -142,10 +158,11 @@ void check_device_error(mlem_matrix* m, cudaStream_t s);
 // One projection of `op` (A or Aᵀ) with the kernel the options select.
 void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, const mlem_run_opts& o,
              L2Window win, cudaStream_t s);
-// Copies slot b of the interleaved batch state to/from contiguous device buffers.
-void batch_put_slot(BatchState& b, uint32_t rows, uint32_t cols, uint32_t slot, const int32_t* g_dev,
-                    float init, const float* f0_dev, uint32_t iters, cudaStream_t s);
-void batch_get_slot(const BatchState& b, uint32_t cols, uint32_t slot, float* f_dev, cudaStream_t s);
+// Copies slot b of the interleaved batch state to/from contiguous device
+// buffers in natural order (permuted for a matrix in the locality layout).
+void batch_put_slot(const mlem_matrix* m, BatchState& b, uint32_t slot, const int32_t* g_dev, float init,
+                    const float* f0_dev, uint32_t iters, cudaStream_t s);
+void batch_get_slot(const mlem_matrix* m, const BatchState& b, uint32_t slot, float* f_dev, cudaStream_t s);
 // A matrix whose operand A (FP32) is filled on the device by `fill` on the
 // matrix stream, then validated and post-processed like mlem_matrix_create
 // (transpose, value type, index copies, sensitivity image).

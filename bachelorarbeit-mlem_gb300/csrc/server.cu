@@ -40,13 +40,14 @@ void enqueue_batch_iteration(mlem_matrix* m, BatchState& b, cudaStream_t s) {
     launch_batch_tick(a, s);
 }
 
-void batch_put_slot(BatchState& b, uint32_t rows, uint32_t cols, uint32_t slot, const int32_t* g_dev,
-                    float init, const float* f0_dev, uint32_t iters, cudaStream_t s) {
-    launch_slot_put(b.g, b.f, rows, cols, b.tile, slot, g_dev, init, f0_dev, b.remaining, iters, s);
+void batch_put_slot(const mlem_matrix* m, BatchState& b, uint32_t slot, const int32_t* g_dev, float init,
+                    const float* f0_dev, uint32_t iters, cudaStream_t s) {
+    launch_slot_put(b.g, b.f, m->A.nrows, m->A.ncols, b.tile, slot, g_dev, init, f0_dev, b.remaining, iters,
+                    m->lor_of, m->vox_of, s);
 }
 
-void batch_get_slot(const BatchState& b, uint32_t cols, uint32_t slot, float* f_dev, cudaStream_t s) {
-    launch_slot_get(b.f, cols, b.tile, slot, f_dev, s);
+void batch_get_slot(const mlem_matrix* m, const BatchState& b, uint32_t slot, float* f_dev, cudaStream_t s) {
+    launch_slot_get(b.f, m->A.ncols, b.tile, slot, f_dev, m->vox_of, s);
 }
 
 static uint64_t batch_state_bytes(uint32_t rows, uint32_t cols, uint32_t tile, bool scatter) {
@@ -233,7 +234,7 @@ bool mlem_server::admit_locked() {
         MLEM_CUDA(cudaMemcpyAsync(ms.bs.stage_g, r.g.data(), sizeof(int32_t) * rows, cudaMemcpyHostToDevice,
                                   ms.stream));
         const float init = reference_initial_value(ms.m, r.g.data());
-        batch_put_slot(ms.bs, rows, cols, (uint32_t)slot, ms.bs.stage_g, init, nullptr, r.iters, ms.stream);
+        batch_put_slot(ms.m, ms.bs, (uint32_t)slot, ms.bs.stage_g, init, nullptr, r.iters, ms.stream);
         MLEM_CUDA(cudaStreamSynchronize(ms.stream));  // stage_g is reused by the next admission
         ms.slot_req[slot] = r.id;
         ms.slot_left[slot] = r.iters;
@@ -270,7 +271,7 @@ void mlem_server::run() {
                     ++st.iterations_done;
                     if (--ms.slot_left[b] > 0) continue;
                     Request& r = reqs[ms.slot_req[b]];
-                    batch_get_slot(ms.bs, cols, b, ms.bs.stage_f, ms.stream);
+                    batch_get_slot(ms.m, ms.bs, b, ms.bs.stage_f, ms.stream);
                     r.result.resize(cols);
                     MLEM_CUDA(cudaMemcpyAsync(r.result.data(), ms.bs.stage_f, sizeof(float) * cols,
                                               cudaMemcpyDeviceToHost, ms.stream));
@@ -360,7 +361,7 @@ mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, con
                     } else {
                         init = reference_initial_value(m, gi);
                     }
-                    batch_put_slot(bs, rows, cols, b, bs.stage_g, init, f0d, iterations[i], s);
+                    batch_put_slot(m, bs, b, bs.stage_g, init, f0d, iterations[i], s);
                     maxit = std::max(maxit, iterations[i]);
                     iters_total += iterations[i];
                 }
@@ -369,7 +370,7 @@ mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, con
                 MLEM_CUDA(cudaEventRecord(e1, s));
                 for (uint32_t b = 0; b < n; ++b) {
                     const uint32_t i = order[base + b];
-                    batch_get_slot(bs, cols, b, bs.stage_f, s);
+                    batch_get_slot(m, bs, b, bs.stage_f, s);
                     MLEM_CUDA(cudaMemcpyAsync(f_out + (uint64_t)i * cols, bs.stage_f, sizeof(float) * cols,
                                               cudaMemcpyDeviceToHost, s));
                     d2h += sizeof(float) * (uint64_t)cols;
@@ -397,6 +398,7 @@ mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, con
             stats->bytes_h2d = h2d;
             stats->bytes_d2h = d2h;
             stats->loglik_last = std::nan("");
+            stats->fp_ms = stats->bp_ms = std::nan("");
         }
     });
 }

@@ -412,10 +412,10 @@ std::vector<uint32_t> siddon_lor_order(const mlem_geometry& g) {
     return ord;
 }
 
-std::vector<uint32_t> voxel_brick_order(uint32_t nx, uint32_t ny, uint32_t nz) {
+std::vector<uint32_t> voxel_brick_order(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t bx, uint32_t by,
+                                        uint32_t bz) {
     std::vector<uint32_t> ord;
     ord.reserve((uint64_t)nx * ny * nz);
-    const uint32_t bx = 4, by = 2, bz = 2;
     for (uint32_t z0 = 0; z0 < nz; z0 += bz)
         for (uint32_t y0 = 0; y0 < ny; y0 += by)
             for (uint32_t x0 = 0; x0 < nx; x0 += bx)

@@ -153,12 +153,15 @@ def barrier(dist, torch=None):
             dist.barrier()
 
 
+LAYOUT = 1  # device layout of the generated matrices (set from --layout)
+
+
 def make_problem(pkg, name, torch, value_type=0, compress=False, interleave=True):
     from mlem_gb300 import synth
     cfg = WORKLOADS[name]
     geo = pkg.preset(name)
     t0 = time.time()
-    m = pkg.Matrix.generate(geo, value_type=value_type, compress=compress, interleave=interleave)
+    m = pkg.Matrix.generate(geo, value_type=value_type, compress=compress, interleave=interleave, layout=LAYOUT)
     t_gen = time.time() - t0
     xt = synth.phantom(geo, cfg["shapes"], seed=1).astype(np.float32)
     dx = torch.from_numpy(xt).cuda()
@@ -172,34 +175,13 @@ def make_problem(pkg, name, torch, value_type=0, compress=False, interleave=True
     return m, geo, g, t_gen
 
 
-def time_kernels(pkg, m, torch, g_dev, f_dev, reps=10, kernel=3, spmv=1):
-    """Average CUDA-event duration of the FP and BP kernels (launched alone)."""
-    s = torch.cuda.current_stream()
-    ratio = torch.zeros(m.rows, dtype=torch.float32, device="cuda")
-    bp = torch.zeros(m.cols, dtype=torch.float32, device="cuda")
-    out = {}
-    for kind in ("fp", "bp"):
-        for _ in range(2):
-            if kind == "fp":
-                m.forward_project(f_dev.data_ptr(), g_dev.data_ptr(), ratio.data_ptr(), 0, stream=s.cuda_stream,
-                                  kernel=kernel, spmv=spmv)
-            else:
-                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream, kernel=kernel, spmv=spmv)
-        times = []
-        for _ in range(reps):
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(s)
-            if kind == "fp":
-                m.forward_project(f_dev.data_ptr(), g_dev.data_ptr(), ratio.data_ptr(), 0, stream=s.cuda_stream,
-                                  kernel=kernel, spmv=spmv)
-            else:
-                m.back_project(ratio.data_ptr(), bp.data_ptr(), stream=s.cuda_stream, kernel=kernel, spmv=spmv)
-            b.record(s)
-            b.synchronize()
-            times.append(a.elapsed_time(b))
-        out[kind] = sum(times) / len(times)
-    return out
+def time_kernels(pkg, m, torch, g, f0, iters=20, **opts):
+    """Mean CUDA-event duration of the forward and back projection stages of a
+    real reconstruction (mlem_run with kernel_timing: events on the launching
+    stream around every stage, eager launches)."""
+    m.run(g, 3, f0=f0, **opts)  # tuning / plans / graphs settled
+    _, st = m.run(g, iters, f0=f0, stats=True, kernel_timing=True, **opts)
+    return {"fp": st["fp_ms"], "bp": st["bp_ms"]}
 
 
 def cpu_baseline(pkg, name, stride, iters=1):
@@ -345,7 +327,7 @@ def run_forms(pkg, torch, args):
     f0 = np.full(m16.cols, m16.initial_value(g), np.float32)
     f0_dev = torch.from_numpy(f0).cuda()
     f_dev = torch.empty_like(f0_dev)
-    kt16 = time_kernels(pkg, m16, torch, g_dev, f0_dev)
+    kt16 = time_kernels(pkg, m16, torch, g, f0)
     res["fp16_kernels"] = {"fp_ms": kt16["fp"], "bp_ms": kt16["bp"], "fp": m16.tuning(False), "bp": m16.tuning(True),
                            "device_bytes": m16.device_bytes}
     for bp_mode, label in ((0, "fp16_trans"), (2, "fp16_fused")):
@@ -395,7 +377,7 @@ def run_forms(pkg, torch, args):
             res["csr4_ingest_cyl3d_mid"] = time_csr4_ingest(pkg, msm)
         msm.close()
     # batched: the mid-size matrix with FP16 values, 64 sinograms, uneven iterations
-    mb = pkg.Matrix.generate(pkg.preset("cyl3d_mid"), value_type=pkg.VAL_F16)
+    mb = pkg.Matrix.generate(pkg.preset("cyl3d_mid"), value_type=pkg.VAL_F16, layout=LAYOUT)
     rng = np.random.Generator(np.random.PCG64(7))
     totals = np.exp(rng.uniform(np.log(1e5), np.log(1e9), 64))
     its = np.random.Generator(np.random.PCG64(8)).integers(10, 201, 64).astype(np.uint32)
@@ -429,7 +411,7 @@ def run_serving(pkg, torch, n_requests=300, rate=50.0, fp32_iter_s=None):
     mats, expect = [], []
     for name, vt, _ in specs:
         geo = pkg.preset(name)
-        m = pkg.Matrix.generate(geo, value_type=vt)
+        m = pkg.Matrix.generate(geo, value_type=vt, layout=LAYOUT)
         dz = torch.zeros(m.rows, dtype=torch.int32, device="cuda")
         ratio = torch.zeros(m.rows, dtype=torch.float32, device="cuda")
         fp = torch.zeros(m.rows, dtype=torch.float32, device="cuda")
@@ -505,6 +487,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--spmv", default="csr-vector", choices=["csr-vector", "merge"],
                     help="SpMV of the timed reconstruction (the reference's argv[8])")
+    ap.add_argument("--layout", default="locality", choices=["natural", "locality"],
+                    help="device layout of the generated matrices (rows in LOR tubes, columns in voxel bricks)")
     ap.add_argument("--bp", default="trans", choices=["trans", "scatter", "fused"],
                     help="back projection of the timed reconstruction (argv[7]; fused: single pass)")
     ap.add_argument("--no-ref-cuda", action="store_true",
@@ -512,6 +496,8 @@ def main():
     ap.add_argument("--no-interleave", action="store_true",
                     help="skip the lane-interleaved matrix copy (halves device memory)")
     args = ap.parse_args()
+    global LAYOUT
+    LAYOUT = 1 if args.layout == "locality" else 0
     if args.impl == "reference":
         return run_reference(args)
 
@@ -586,10 +572,10 @@ def main():
     e2e_value = world * args.steps * iters / float(te.item())
 
     # roofline of the dominant kernel
-    kt = time_kernels(pkg, m, torch, g_dev, f0_dev, spmv=SPMV)
-    kt_direct = time_kernels(pkg, m, torch, g_dev, f0_dev, kernel=0)
-    kt_tma = time_kernels(pkg, m, torch, g_dev, f0_dev, kernel=1)
-    kt_pers = time_kernels(pkg, m, torch, g_dev, f0_dev, kernel=2)
+    kt = time_kernels(pkg, m, torch, g, f0, spmv=SPMV, bp_mode=BP)
+    kt_direct = time_kernels(pkg, m, torch, g, f0, kernel=0)
+    kt_tma = time_kernels(pkg, m, torch, g, f0, kernel=1)
+    kt_pers = time_kernels(pkg, m, torch, g, f0, kernel=2)
     fp_b, bp_b = algorithmic_bytes(m.rows, m.cols, m.nnz, 4)
     dom = "fp" if kt["fp"] >= kt["bp"] else "bp"
     dom_bytes = fp_b if dom == "fp" else bp_b
@@ -599,7 +585,8 @@ def main():
     traffic = None
     tf = PROFILES / "dram_traffic.json"
     if tf.exists() and default_form:
-        traffic = json.loads(tf.read_text()).get(f"{name}/{dom}")
+        key = f"{name}/{dom}" + ("/locality" if LAYOUT else "")
+        traffic = json.loads(tf.read_text()).get(key)
 
     line = {
         "metric": "MLEM iterations/s", "value": value, "unit": "iter/s", "n_gpus": world,
@@ -607,7 +594,8 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded multi-ray Siddon matrix, ellipsoid phantom, Poisson sinogram)",
         "config": {"workload": name, "rows": m.rows, "cols": m.cols, "nnz": m.nnz, "iterations_per_step": iters,
-                   "form": f"fp32 plain: {args.spmv} SpMV, {args.bp} BP", "l2": "inputs larger than L2 "
+                   "form": f"fp32 plain: {args.spmv} SpMV, {args.bp} BP, {args.layout} layout",
+                   "l2": "inputs larger than L2 "
                    f"({(m.device_bytes) / 1e9:.1f} GB resident matrix)", "replicas": world,
                    "matrix_generation_s": round(t_gen, 2)},
         "e2e": {"value": e2e_value, "unit": "iter/s", "h2d_bytes_per_step": int(4 * m.rows + 4 * m.cols),

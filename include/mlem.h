@@ -84,7 +84,20 @@ typedef struct {
                                    nonzero instead of 4) for the csr-vector projections */
     uint32_t interleave;        /* 1: also keep a lane-interleaved copy (16-byte loads whose
                                    gathers cover consecutive columns) for the projections */
+    uint32_t layout;            /* mlem_layout: device order of rows and columns */
+    uint32_t grid_nx, grid_ny, grid_nz; /* voxel grid of the columns (column = x + nx*(y + ny*z),
+                                   scannerconfig.cpp:30-35) for the locality layout of
+                                   mlem_matrix_create; csr4 files and geometries carry their own */
 } mlem_matrix_opts;
+
+/* Device layout of a matrix.  LOCALITY stores A' = P_L A P_Vᵀ: columns
+ * (voxels) in 4x4x2 bricks, rows (LORs) in 4x4 detector tubes for generated
+ * matrices (natural row order otherwise), each row's columns ascending.  The
+ * gathers of both projections then hit fewer cache lines.  Every entry point
+ * still takes and returns natural order (sinograms, images, projections,
+ * mlem_matrix_get_csr / _transpose / _norm); results agree with the natural
+ * layout to FP32 rounding (the order of each row's additions changes). */
+typedef enum { MLEM_LAYOUT_NATURAL = 0, MLEM_LAYOUT_LOCALITY = 1 } mlem_layout;
 
 /* Fills *o with the defaults: F32 values, transpose built, norm computed, device 0. */
 void mlem_matrix_opts_default(mlem_matrix_opts* o);
@@ -149,6 +162,9 @@ typedef struct {
                                    the locality order of a generated matrix */
     uint32_t pipeline;          /* DIRECT / ORDERED with 16 or 32 lanes: 1 = load a row's next vectors
                                    before the gathers of the current ones (same results) */
+    uint32_t kernel_timing;     /* mlem_run only: 1 = CUDA events around the forward and back
+                                   projection stages of every iteration (eager launches, no graph
+                                   replay); their means go to mlem_stats.fp_ms / bp_ms */
 } mlem_run_opts;
 
 /* Kernel variants of the csr-vector projections (same arithmetic; the order of
@@ -181,6 +197,7 @@ typedef struct {
     uint32_t kernel_launches;   /* kernels launched by the iteration loop */
     uint64_t bytes_h2d, bytes_d2h;
     double loglik_last;         /* last computed log-likelihood (NaN if none) */
+    double fp_ms, bp_ms;        /* mean forward / back projection stage (kernel_timing), else NaN */
 } mlem_stats;
 
 /* Runs `iterations` MLEM iterations on host buffers: g i32[rows] (sinogram),
