@@ -330,6 +330,12 @@ def run_forms(pkg, torch, args):
     kt16 = time_kernels(pkg, m16, torch, g, f0)
     res["fp16_kernels"] = {"fp_ms": kt16["fp"], "bp_ms": kt16["bp"], "fp": m16.tuning(False), "bp": m16.tuning(True),
                            "device_bytes": m16.device_bytes}
+    # each variant with its default lanes / vectors in flight (the tuned choice is above)
+    variants = {}
+    for label, kern in (("direct", pkg.KERNEL_DIRECT), ("ilv", pkg.KERNEL_ILV), ("d16", pkg.KERNEL_D16)):
+        t = time_kernels(pkg, m16, torch, g, f0, iters=10, kernel=kern)
+        variants[label] = {"fp_ms": t["fp"], "bp_ms": t["bp"]}
+    res["fp16_kernels"]["variants_ms"] = variants
     for bp_mode, label in ((0, "fp16_trans"), (2, "fp16_fused")):
         f_dev.copy_(f0_dev)
         m16.run_device(g_dev.data_ptr(), f_dev.data_ptr(), 5, stream=s.cuda_stream, bp_mode=bp_mode)
