@@ -87,6 +87,9 @@ struct MergePlan {
     uint32_t* carry_row = nullptr;// [ntiles]
     float* head = nullptr;        // [ntiles]
     size_t smem = 0;
+    // true: the row-parallel tile kernel (library-owned, padded operands);
+    // false: the per-thread walk over shared-memory products (any arrays)
+    bool rows_kernel = false;
     void release();
 };
 // Builds the tile partition of `op` for a section size (device allocations).

@@ -3,16 +3,21 @@
 // (kernel.cu:52-105), merge_based_start (kernel.cu:190-241) and
 // merge_based_work (kernel.cu:257-286).
 //
-// Work decomposition is the reference's: global thread t consumes secsize
-// items of the merged list (row ends ∪ nonzeros) starting at diagonal
-// t*secsize, with the coordinates the reference search finds.  What differs
-// is how the row fragments are combined: the reference adds every fragment
-// with a global atomicAdd (order nondeterministic); here a CTA of T threads
-// stages its tile of values and gathered x in shared memory, combines the
-// per-thread carries with a segmented scan in a fixed order, applies the
-// fused epilogue (correlation or update) to rows that end inside the tile,
-// and leaves the first row of every tile to a small fix-up kernel that adds
-// the carries of earlier tiles in tile order.  Results are deterministic.
+// The merged list (row ends ∪ nonzeros) is cut into tiles whose start
+// coordinates come from the reference search.  Library matrices use
+// row-parallel tiles (k_merge_rows): a tile spans at least the stretch one
+// 1024-thread block of the reference covers (1024 * secsize items) and about
+// 32 average rows; its rows are shared out to 16-lane groups that read their
+// part of the row with 16-byte vector loads.  Caller-owned arrays (the
+// allocation-free entry point) use the per-thread form (k_merge_tile): thread
+// t consumes secsize items from diagonal t*secsize, the tile's products are
+// staged in shared memory and the per-thread carries are combined with a
+// segmented scan in a fixed order.  Both apply the fused epilogue
+// (correlation or update) to rows that end inside the tile and leave the
+// first row of every tile to a small fix-up kernel that adds the carries of
+// earlier tiles in tile order.  The reference instead adds every row fragment
+// with a global atomicAdd (order nondeterministic); results here are
+// deterministic.
 #include "kernels.cuh"
 
 #include <algorithm>
@@ -250,12 +255,85 @@ __global__ void k_merge_fixup(const uint32_t* __restrict__ ti, const float* __re
     }
 }
 
+// Row-parallel tile: the tile is the same stretch of the merge path as above
+// (row ends and nonzeros from the reference search), but its rows are shared
+// out to the CTA's warps.  A warp sums its row's part of the tile with
+// 16-byte vector loads (the operand's arrays are padded and 16-byte aligned)
+// and a fixed xor reduction; rows that end inside the tile get their
+// epilogue here, the tile's first row (which began in an earlier tile) goes
+// to head[k] and the row still open at the tile's end to carry[k], for the
+// same fix-up kernel.  Deterministic.
+template <typename V, int LPR>
+__device__ __forceinline__ float group_part_dot(const uint32_t* __restrict__ idx, const V* __restrict__ val,
+                                                const float* __restrict__ x, uint64_t s, uint64_t t, int sub) {
+    const uint4* idx4 = reinterpret_cast<const uint4*>(idx);
+    const uint64_t v1 = (t + 3) >> 2;
+    float acc = 0.f;
+    for (uint64_t v = (s >> 2) + sub; v < v1; v += LPR) {
+        const uint4 c = __ldcs(idx4 + v);
+        float a[4];
+        Val4<V>::load(val, v, a);
+        const uint32_t cs[4] = {c.x, c.y, c.z, c.w};
+        // element 4v+k lies in [s, t) unless it is a masked head or tail element
+        const uint32_t lo = (uint32_t)(s > 4 * v ? s - 4 * v : 0), hi = (uint32_t)(t - 4 * v);
+        float g[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) g[k] = (k >= (int)lo && k < (int)hi) ? __ldg(x + cs[k]) : 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k >= (int)lo && k < (int)hi) acc = fmaf(a[k], g[k], acc);
+    }
+    return acc;
+}
+
+template <typename V, int LPR>
+__global__ void __launch_bounds__(256, 8)
+k_merge_rows(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx, const V* __restrict__ val,
+             const float* __restrict__ x, uint32_t rows, const uint32_t* __restrict__ ti,
+             const uint64_t* __restrict__ tj, float* __restrict__ carry, uint32_t* __restrict__ carry_row,
+             float* __restrict__ head, EpiDev epi) {
+    const uint64_t k = blockIdx.x;
+    const uint32_t I0 = ti[k], I1 = ti[k + 1];
+    const uint64_t J0 = tj[k], J1 = tj[k + 1];
+    const uint32_t nrow_l = I1 - I0;  // rows that end inside the tile
+    constexpr uint32_t NG = 256 / LPR;  // lane groups of the CTA
+    const uint32_t grp = threadIdx.x / LPR;
+    const int sub = threadIdx.x & (LPR - 1);
+    const unsigned mask = LPR == 32 ? 0xffffffffu : (((1u << LPR) - 1u) << ((threadIdx.x & 31) & ~(LPR - 1)));
+    for (uint32_t i = grp; i <= nrow_l; i += NG) {
+        const uint32_t r = I0 + i;
+        float acc = 0.f;
+        if (r < rows) {
+            uint64_t s = rowptr[r], t = rowptr[r + 1];
+            s = s < J0 ? J0 : s;
+            t = t > J1 ? J1 : t;
+            if (s < t) acc = group_part_dot<V, LPR>(idx, val, x, s, t, sub);
+        }
+#pragma unroll
+        for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(mask, acc, o);
+        if (sub == 0) {
+            if (i == nrow_l) {  // still open at the tile's end (or past the last row)
+                carry[k] = acc;
+                carry_row[k] = r;
+            } else if (i == 0) {
+                head[k] = acc;  // began in an earlier tile: the fix-up adds their carries
+            } else {
+                epi(r, acc);
+            }
+        }
+    }
+}
+
 template <typename V>
 void merge_launch_t(const DevCsr& op, const MergePlan& p, const float* x, const EpiDev& e,
                     L2Window win, cudaStream_t s) {
-    launch_ex(k_merge_tile<V>, dim3((unsigned)p.ntiles), dim3(p.threads), p.smem, s, win,
-              op.rowptr, op.idx, static_cast<const V*>(op.val), x, op.nrows, p.secsize,
-              p.tile_i, p.tile_j, p.carry, p.carry_row, p.head, e);
+    if (p.rows_kernel)
+        launch_ex(k_merge_rows<V, 16>, dim3((unsigned)p.ntiles), dim3(256), 0, s, win, op.rowptr, op.idx,
+                  static_cast<const V*>(op.val), x, op.nrows, p.tile_i, p.tile_j, p.carry, p.carry_row, p.head, e);
+    else
+        launch_ex(k_merge_tile<V>, dim3((unsigned)p.ntiles), dim3(p.threads), p.smem, s, win,
+                  op.rowptr, op.idx, static_cast<const V*>(op.val), x, op.nrows, p.secsize,
+                  p.tile_i, p.tile_j, p.carry, p.carry_row, p.head, e);
     const unsigned fg = std::max(1u, std::min<unsigned>(ceil_div_u(p.ntiles, 256), 152u * 8u));
     launch_ex(k_merge_fixup, dim3(fg), dim3(256), 0, s, L2Window{}, p.tile_i, p.carry,
               p.carry_row, p.head, p.ntiles, e);
@@ -292,14 +370,18 @@ void merge_plan_build(const DevCsr& op, uint32_t secsize, MergePlan& plan, cudaS
                  "merge section size must be in 1..512");
     plan.release();
     plan.secsize = secsize;
-    uint32_t T = 4096 / secsize;
-    T = std::max(32u, std::min(256u, T & ~31u));
-    plan.threads = T;
-    const uint64_t TS = (uint64_t)T * secsize;
+    // Row-parallel tiles of the merge path, 256 threads: at least the stretch
+    // one 1024-thread block of the reference covers (1024 * secsize items),
+    // and enough items for about 32 average rows so that the CTA's 8 warps
+    // share the tile's rows evenly; at most 65536 items.
+    plan.rows_kernel = true;
+    plan.threads = 256;
     const uint64_t items = (uint64_t)op.nrows + op.nnz;
+    const uint64_t per_row = op.nrows ? (items + op.nrows - 1) / op.nrows : 1;
+    const uint64_t TS = std::min<uint64_t>(std::max<uint64_t>(1024ull * secsize, 32 * per_row), 65536ull);
     plan.ntiles = (items + TS - 1) / TS;
     MLEM_REQUIRE(plan.ntiles < (1ull << 31), MLEM_EUNSUPPORTED, "merge path: too many tiles");
-    plan.smem = sizeof(uint32_t) * (TS + 4) + sizeof(float) * TS;
+    plan.smem = 0;
     const uint64_t nt = std::max<uint64_t>(plan.ntiles, 1);
     MLEM_CUDA(cudaMalloc(&plan.tile_i, sizeof(uint32_t) * (nt + 1)));
     MLEM_CUDA(cudaMalloc(&plan.tile_j, sizeof(uint64_t) * (nt + 1)));
