@@ -314,6 +314,26 @@ def time_csr4_ingest(pkg, m):
         shutil.rmtree(d, ignore_errors=True)
 
 
+def run_modes(pkg, torch, name):
+    """The reference's switch combinations (argv[8] merge / csr-vector x argv[7]
+    transposed / scatter), the fused single pass and a batched run (16
+    sinograms, 10 iterations) on one workload: every projection kernel runs."""
+    m, _, g, _ = make_problem(pkg, name, torch, interleave=False)
+    f0 = np.full(m.cols, m.initial_value(g), np.float32)
+    its = 10
+    out = {}
+    for label, spmv, bp in (("csr_vector_trans", 1, 0), ("merge_trans", 0, 0), ("csr_vector_scatter", 1, 1),
+                            ("merge_scatter", 0, 1), ("fused", 1, 2)):
+        m.run(g, 3, f0=f0, spmv=spmv, bp_mode=bp)
+        _, st = m.run(g, its, f0=f0, spmv=spmv, bp_mode=bp, stats=True)
+        out[label] = {"iterations_per_s": its / st["seconds_iterations"]}
+    G = np.stack([np.roll(g, 17 * k) for k in range(16)]).astype(np.int32)
+    _, st = m.batch_run(G, np.full(16, its, np.uint32), stats=True)
+    out["batched_16"] = {"images_iterations_per_s": 16 * its / st["seconds_iterations"]}
+    m.close()
+    return out
+
+
 def run_forms(pkg, torch, args):
     """FP16-value and batched forms (images*iterations/s)."""
     from mlem_gb300 import synth
@@ -489,7 +509,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cyl3d_12gb", choices=sorted(WORKLOADS))
-    ap.add_argument("--forms", default="all", choices=["all", "none"])
+    ap.add_argument("--forms", default="all", choices=["all", "none", "modes"],
+                    help="all: FP16, batched, serving and the modes on the smaller matrices; modes: only the "
+                         "reference's switch combinations, the fused pass and a batched run on --workload")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--spmv", default="csr-vector", choices=["csr-vector", "merge"],
                     help="SpMV of the timed reconstruction (the reference's argv[8])")
@@ -620,6 +642,8 @@ def main():
         "clocks": clk.summary(),
     }
     m.close()
+    if args.forms == "modes":
+        line["forms"] = run_modes(pkg, torch, name)
     if args.forms == "all":
         line["forms"] = run_forms(pkg, torch, args)
         line["forms"]["fp32_plain"] = {"images_iterations_per_s": value / world}
