@@ -25,7 +25,7 @@ LIB_PATH = PKG / "lib" / "libmlem_gb300.so"
 CLI_PATH = PKG / "bin" / "mlem_gb300"
 
 SPMV_MERGE, SPMV_CSR_VECTOR = 0, 1
-KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO, KERNEL_D16, KERNEL_ILV, KERNEL_ORDERED = 0, 1, 2, 3, 4, 5, 6
+KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO, KERNEL_D16, KERNEL_ILV, KERNEL_ORDERED, KERNEL_SYM = range(8)
 LAYOUT_NATURAL, LAYOUT_LOCALITY = 0, 1
 VAL_F32, VAL_F16, VAL_BF16 = 0, 1, 2
 BP_TRANS, BP_SCATTER, BP_FUSED = 0, 1, 2
@@ -50,7 +50,8 @@ class CsrHost(C.Structure):
 class MatrixOpts(C.Structure):
     _fields_ = [("value_type", C.c_int), ("build_transpose", C.c_uint32), ("norm", C.c_void_p),
                 ("device", C.c_int), ("compress_indices", C.c_uint32), ("interleave", C.c_uint32),
-                ("layout", C.c_uint32), ("grid_nx", C.c_uint32), ("grid_ny", C.c_uint32), ("grid_nz", C.c_uint32)]
+                ("layout", C.c_uint32), ("grid_nx", C.c_uint32), ("grid_ny", C.c_uint32), ("grid_nz", C.c_uint32),
+                ("symmetry", C.c_uint32)]
 
 
 class MatrixInfo(C.Structure):
@@ -282,7 +283,7 @@ class Matrix:
     # construction ---------------------------------------------------------
     @staticmethod
     def _opts(value_type=VAL_F32, build_transpose=True, norm=None, device=0, compress=False, interleave=False,
-              layout=0, grid=None):
+              layout=0, grid=None, symmetry=False):
         o = MatrixOpts()
         load_library().mlem_matrix_opts_default(C.byref(o))
         o.value_type = value_type
@@ -290,6 +291,7 @@ class Matrix:
         o.compress_indices = 1 if compress else 0
         o.interleave = 1 if interleave else 0
         o.layout = int(layout)
+        o.symmetry = 1 if symmetry else 0
         if grid is not None:
             o.grid_nx, o.grid_ny, o.grid_nz = (int(v) for v in grid)
         keep = None
@@ -322,8 +324,8 @@ class Matrix:
 
     @classmethod
     def generate(cls, geo: Geometry, value_type=VAL_F32, build_transpose=True, device=0,
-                 compress=False, interleave=False, layout=LAYOUT_NATURAL) -> "Matrix":
-        o, _ = cls._opts(value_type, build_transpose, None, device, compress, interleave, layout)
+                 compress=False, interleave=False, layout=LAYOUT_NATURAL, symmetry=False) -> "Matrix":
+        o, _ = cls._opts(value_type, build_transpose, None, device, compress, interleave, layout, symmetry=symmetry)
         h = C.c_void_p()
         _check(load_library().mlem_matrix_generate(C.byref(geo), C.byref(o), C.byref(h)))
         return cls(h.value)
@@ -360,7 +362,7 @@ class Matrix:
         k, ln, u, od, pp, ms = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_float()
         _check(load_library().mlem_matrix_get_tuning(self._h, int(transposed), C.byref(k), C.byref(ln),
                                                      C.byref(u), C.byref(od), C.byref(pp), C.byref(ms)))
-        names = {0: "direct", 1: "tma", 2: "persistent", 4: "d16", 5: "ilv"}
+        names = {0: "direct", 1: "tma", 2: "persistent", 4: "d16", 5: "ilv", 7: "sym"}
         return {"kernel": names.get(k.value, k.value), "lanes_per_row": ln.value, "vectors_in_flight": u.value,
                 "locality_order": bool(od.value), "pipelined": bool(pp.value), "ms": ms.value}
 

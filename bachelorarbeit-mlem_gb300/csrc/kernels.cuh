@@ -128,11 +128,55 @@ void launch_invert_perm(const uint32_t* map, uint32_t n, uint32_t* inv, cudaStre
 void remap_csr(const DevCsr& in, const uint32_t* row_src, const uint32_t* col_map, DevCsr& out, DevCsr* keep_t,
                cudaStream_t s);
 
+// ------------------------------------------------------------- symmetry.cu
+// s(x, y, z) of a voxel as an index: ax*x + ay*y + az*z + c0
+struct SymVoxMap {
+    int32_t ax, ay, az, c0;
+};
+struct SymMapsArg {
+    SymVoxMap m[16];
+};
+// Symmetry-compressed projection operands of a generated cylindrical scanner
+// (see symmetry.cu): canonical LOR rows for the forward projection, canonical
+// voxel rows of A^T for the back projection.
+struct SymOps {
+    uint32_t n = 0, nz = 0;          // square voxel grid n x n x nz
+    uint32_t K = 0, J = 0;           // canonical LOR rows / canonical voxel rows
+    uint64_t fp_nnz = 0, bp_nnz = 0;
+    uint64_t* fp_rowptr = nullptr;   // [K+1]
+    uint32_t* fp_key = nullptr;      // [fp_nnz] x | y << 11 | z << 22
+    void* fp_val = nullptr;          // [fp_nnz]
+    uint32_t* img = nullptr;         // [16 K] LOR s(r_k)
+    uint32_t* fp_mask = nullptr;     // [K] transformations giving distinct LORs
+    uint64_t* bp_rowptr = nullptr;   // [J+1]
+    uint32_t* bp_key = nullptr;      // [bp_nnz] canonical row << 4 | transformation
+    void* bp_val = nullptr;          // [bp_nnz]
+    uint32_t* vxyz = nullptr;        // [J] packed canonical voxel
+    uint32_t* vmask = nullptr;       // [J] transformations giving distinct voxels
+    uint8_t* comp = nullptr;         // [256] composition table: comp[16 s + t] = s after t
+    SymMapsArg maps{};               // voxel maps of the 16 transformations
+    mlem_value_type vt = MLEM_VAL_F32;
+    void release();
+    uint64_t bytes() const;
+};
+// Geometry requirements of the symmetric form (errors otherwise).
+void check_symmetric_geometry(const mlem_geometry& geo);
+// A^ (symmetrised from the canonical rows), its transpose, and the compact
+// operands; A and AT must be empty.
+void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y, cudaStream_t s);
+void lower_symmetric_values(SymOps& y, mlem_value_type vt, cudaStream_t s);
+// Forward (transposed = false: Correl or Raw epilogue) or back projection
+// (true: Update or Raw) through the compact operands; natural order in and out.
+void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s);
+
 // ------------------------------------------------------------- siddon.cu
 uint64_t siddon_rows(const mlem_geometry& geo);
 void siddon_count_host(const mlem_geometry& geo, uint64_t* rowptr);
 void siddon_fill_host(const mlem_geometry& geo, const uint64_t* rowptr, uint32_t* col, float* val);
 void siddon_generate_device(const mlem_geometry& geo, DevCsr& A, cudaStream_t s);
+// Rows of the given LOR indices (row_stride 1), generated on the host.
+void siddon_rows_of_lors(const mlem_geometry& geo, const std::vector<uint64_t>& lors, std::vector<uint64_t>& rowptr,
+                         std::vector<uint32_t>& col, std::vector<float>& val);
 // Locality-friendly processing orders for a generated matrix: LORs in 4x4
 // detector tubes (rows of A) and voxels in 4x2x2 bricks (rows of Aᵀ).
 std::vector<uint32_t> siddon_lor_order(const mlem_geometry& geo);

@@ -167,8 +167,10 @@ const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
 
 
 void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o) {
-    MLEM_REQUIRE(o.kernel <= MLEM_KERNEL_ORDERED, MLEM_EINVAL,
-                 "kernel must be 0 direct, 1 tma, 2 persistent, 3 auto, 4 d16, 5 ilv or 6 ordered");
+    MLEM_REQUIRE(o.kernel <= MLEM_KERNEL_SYM, MLEM_EINVAL,
+                 "kernel must be 0 direct, 1 tma, 2 persistent, 3 auto, 4 d16, 5 ilv, 6 ordered or 7 sym");
+    MLEM_REQUIRE(o.kernel != MLEM_KERNEL_SYM || m->sym.fp_rowptr != nullptr, MLEM_EINVAL,
+                 "kernel SYM needs a matrix generated with symmetry = 1");
     MLEM_REQUIRE(o.lanes == 0 || o.lanes == 4 || o.lanes == 8 || o.lanes == 16 || o.lanes == 32, MLEM_EINVAL,
                  "lanes must be 0, 4, 8, 16 or 32");
     MLEM_REQUIRE(o.unroll == 0 || o.unroll == 1 || o.unroll == 2 || o.unroll == 4, MLEM_EINVAL,
@@ -213,6 +215,8 @@ static void launch_cfg(mlem_matrix* m, const DevCsr& op, const float* x, const E
         launch_csr_tma(op, x, e, m->ws.err, win, s);
     } else if (c.kind == MLEM_KERNEL_D16) {
         launch_csr_d16(op, x, e, win, s);
+    } else if (c.kind == MLEM_KERNEL_SYM) {
+        launch_sym(m->sym, &op == &m->AT, x, e, win, s);
     } else if (c.kind == MLEM_KERNEL_ILV) {
         launch_csr_ilv(op, x, e, c.unroll, win, s);
     } else if (c.kind == MLEM_KERNEL_PERSISTENT) {
@@ -246,6 +250,7 @@ static void tune_projection(mlem_matrix* m, bool transposed) {
     if (op.d16) cand.push_back(ProjCfg{MLEM_KERNEL_D16, 32, 1, 0.f});
     if (op.idx_ilv)
         for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_ILV, 32, u, 0.f});
+    if (m->sym.fp_rowptr) cand.push_back(ProjCfg{MLEM_KERNEL_SYM, 32, 1, 0.f});
     prepare_csrvec_pipe(op.vt);
     prepare_csr_tma(op.vt);
     ensure_workspace(m);
@@ -332,6 +337,8 @@ void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, 
         MLEM_REQUIRE(op.idx_ilv != nullptr, MLEM_EINVAL, "kernel ILV needs a matrix created with interleave = 1");
         c.kind = MLEM_KERNEL_ILV;
         c.unroll = 2;
+    } else if (o.kernel == MLEM_KERNEL_SYM) {
+        c.kind = MLEM_KERNEL_SYM;
     } else {
         c.kind = MLEM_KERNEL_DIRECT;
         c.lanes = o.lanes ? (int)o.lanes : pick_lanes(op.nnz, op.nrows);
@@ -640,6 +647,7 @@ static void destroy_matrix(mlem_matrix* m) {
     for (auto& kv : m->plan_AT) kv.second.release();
     free_csr(m->A);
     free_csr(m->AT);
+    m->sym.release();
     cudaFree(m->norm);
     cudaFree(m->lor_of);
     cudaFree(m->vox_of);
@@ -700,7 +708,7 @@ mlem_matrix* create_matrix_filled(const mlem_matrix_opts& o, const std::function
 using namespace mlem;
 
 uint64_t mlem_matrix::bytes() const {
-    uint64_t b = csr_bytes(A) + csr_bytes(AT) + sizeof(float) * (uint64_t)A.ncols;
+    uint64_t b = csr_bytes(A) + csr_bytes(AT) + sizeof(float) * (uint64_t)A.ncols + sym.bytes();
     for (auto& kv : plan_A) b += kv.second.ntiles * 24;
     for (auto& kv : plan_AT) b += kv.second.ntiles * 24;
     if (ws.ready) b += (uint64_t)A.nrows * 12 + (uint64_t)A.ncols * 8;
@@ -723,6 +731,7 @@ void mlem_matrix_opts_default(mlem_matrix_opts* o) {
     o->interleave = 0;
     o->layout = MLEM_LAYOUT_NATURAL;
     o->grid_nx = o->grid_ny = o->grid_nz = 0;
+    o->symmetry = 0;
 }
 
 void mlem_run_opts_default(mlem_run_opts* o) {
@@ -774,10 +783,19 @@ mlem_status mlem_matrix_generate(const mlem_geometry* geo, const mlem_matrix_opt
         DeviceGuard dg(o.device);
         mlem_matrix* m = new_matrix(o);
         try {
-            siddon_generate_device(*geo, m->A, m->stream);
-            MLEM_REQUIRE(m->A.nrows >= 1, MLEM_EINVAL, "geometry produced no rows");
-            maybe_apply_layout(m, o, geo->nx, geo->ny, geo->nz, siddon_lor_order(*geo));
-            postprocess_matrix(m, o);
+            if (o.symmetry) {
+                MLEM_REQUIRE(o.layout == MLEM_LAYOUT_NATURAL, MLEM_EUNSUPPORTED,
+                             "symmetry keeps the natural layout (the symmetric operands are compact already)");
+                build_symmetric(*geo, m->A, m->AT, m->sym, m->stream);
+                m->has_t = true;
+                postprocess_matrix(m, o);
+                lower_symmetric_values(m->sym, o.value_type, m->stream);
+            } else {
+                siddon_generate_device(*geo, m->A, m->stream);
+                MLEM_REQUIRE(m->A.nrows >= 1, MLEM_EINVAL, "geometry produced no rows");
+                maybe_apply_layout(m, o, geo->nx, geo->ny, geo->nz, siddon_lor_order(*geo));
+                postprocess_matrix(m, o);
+            }
             if (o.layout == MLEM_LAYOUT_NATURAL) {
                 // locality orders of the rows (processing order only): LOR
                 // tubes for A, voxel bricks for Aᵀ

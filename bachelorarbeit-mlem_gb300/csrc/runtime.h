@@ -121,6 +121,7 @@ struct mlem_matrix {
     std::vector<float> norm_host;     // host copy in natural column order (initial value)
     // Locality layout: natural row / column of each internal row / column
     // (NULL = natural order).
+    mlem::SymOps sym;                 // symmetry-compressed operands (symmetry = 1)
     uint32_t* lor_of = nullptr;       // [rows]
     uint32_t* vox_of = nullptr;       // [cols]
     std::vector<uint32_t> vox_of_host;

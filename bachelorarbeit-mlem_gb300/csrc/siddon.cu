@@ -393,6 +393,40 @@ void siddon_fill_host(const mlem_geometry& g, const uint64_t* rowptr, uint32_t* 
     }
 }
 
+void siddon_rows_of_lors(const mlem_geometry& g, const std::vector<uint64_t>& lors, std::vector<uint64_t>& rowptr,
+                         std::vector<uint32_t>& col, std::vector<float>& val) {
+    check_geo(g);
+    Geo G = make_geo(g);
+    MLEM_REQUIRE(G.stride == 1, MLEM_EINVAL, "rows of a LOR list need row_stride 1");
+    std::vector<double> ct, st;
+    angle_tables(G, ct, st);
+    const int64_t n = (int64_t)lors.size();
+    rowptr.assign(lors.size() + 1, 0);
+#pragma omp parallel
+    {
+        std::vector<HostEntry> buf;
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t q = 0; q < n; ++q)
+            rowptr[q + 1] = row_host(G, ct.data(), st.data(), lors[q], buf, [](uint32_t, float) {});
+    }
+    for (int64_t q = 0; q < n; ++q) rowptr[q + 1] += rowptr[q];
+    col.resize(rowptr[n]);
+    val.resize(rowptr[n]);
+#pragma omp parallel
+    {
+        std::vector<HostEntry> buf;
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t q = 0; q < n; ++q) {
+            uint64_t pos = rowptr[q];
+            row_host(G, ct.data(), st.data(), lors[q], buf, [&](uint32_t c, float v) {
+                col[pos] = c;
+                val[pos] = v;
+                ++pos;
+            });
+        }
+    }
+}
+
 std::vector<uint32_t> siddon_lor_order(const mlem_geometry& g) {
     check_geo(g);
     const Geo G = make_geo(g);

@@ -1,0 +1,600 @@
+// symmetry.cu — symmetry-compressed projections for generated cylindrical
+// scanners.
+//
+// A ring scanner with dpr % 4 == 0 detectors per ring (detector k at angle
+// 2*pi*k/dpr), rings placed symmetrically about z = 0 and a square voxel grid
+// centred on the axis is invariant under 16 transformations s = q + 4m + 8f:
+// a mirror y -> -y (m), a rotation by q * 90 degrees, and the axial flip
+// z -> -z (f), applied in that order.  On a voxel (x, y, z) of an n x n x nz
+// grid: y -> n-1-y; (x, y) -> (n-1-y, x) q times; z -> nz-1-z.  On a
+// detector (ring, k): k -> (dpr-k) % dpr; k -> (k + q*dpr/4) % dpr;
+// ring -> rings-1-ring.  A LOR (a, b) maps to the sorted pair of images.
+//
+// The symmetric matrix A^ is built from the rows of the canonical LORs (the
+// smallest index of every orbit), generated as usual and, where a LOR is
+// fixed by some transformations, averaged over them so that
+// A^[s(r), s(c)] = A^[r, c] holds exactly.  A^ and its transpose stay the
+// matrix of the handle (every mode and getter uses them); beside them this
+// file keeps two compact operands:
+//   forward projection: the canonical rows (1/16 of the nonzeros), columns
+//     packed as x | y << 11 | z << 22, and img[16 k + s] = s(r_k) for each
+//     canonical row k;
+//   back projection over A^T: the rows of the canonical voxels (1/16 of the
+//     nonzeros), each entry a LOR r' = t(r_k) stored as k << 4 | t.
+// A warp handles one compact row; a lane takes consecutive elements and keeps
+// 16 accumulators, one per transformation, so the gathers of one instruction
+// follow one transformed ray (32 consecutive voxels / LORs).  The FP gathers
+// f[s(c)]; the BP gathers ratio[img[16 k + s*t]].  Each distinct image row
+// (LOR s(r_k), voxel s(v)) is written by the first s that produces it.
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <map>
+#include <vector>
+
+namespace mlem {
+
+namespace {
+
+struct SymMaps {
+    uint32_t n, nz, dpr, rings, D;
+    void vox(int s, uint32_t& x, uint32_t& y, uint32_t& z) const {
+        if ((s >> 2) & 1) y = n - 1 - y;
+        for (int q = 0; q < (s & 3); ++q) {
+            const uint32_t t = x;
+            x = n - 1 - y;
+            y = t;
+        }
+        if (s >> 3) z = nz - 1 - z;
+    }
+    uint32_t vox_index(int s, uint32_t c) const {
+        uint32_t x = c % n, y = (c / n) % n, z = c / (n * n);
+        vox(s, x, y, z);
+        return x + n * (y + n * z);
+    }
+    uint32_t det(int s, uint32_t d) const {
+        uint32_t ring = d / dpr, k = d % dpr;
+        if ((s >> 2) & 1) k = (dpr - k) % dpr;
+        k = (k + (uint32_t)(s & 3) * (dpr / 4)) % dpr;
+        if (s >> 3) ring = rings - 1 - ring;
+        return ring * dpr + k;
+    }
+    uint64_t lor(uint64_t a, uint64_t b) const {
+        if (a > b) std::swap(a, b);
+        return a * D - a * (a + 1) / 2 + (b - a - 1);
+    }
+};
+
+// comp[s][t]: the transformation "t, then s", found on probe voxels.
+void composition(const SymMaps& M, uint8_t comp[16][16], uint8_t inv[16]) {
+    SymMaps P = M;
+    P.n = 7;
+    P.nz = 5;
+    const uint32_t probe[3][3] = {{0, 1, 0}, {2, 5, 1}, {3, 0, 4}};
+    auto image = [&](int s, const uint32_t p[3], uint32_t out[3]) {
+        out[0] = p[0];
+        out[1] = p[1];
+        out[2] = p[2];
+        P.vox(s, out[0], out[1], out[2]);
+    };
+    for (int s = 0; s < 16; ++s)
+        for (int t = 0; t < 16; ++t) {
+            int found = -1;
+            for (int u = 0; u < 16 && found < 0; ++u) {
+                bool same = true;
+                for (int k = 0; k < 3 && same; ++k) {
+                    uint32_t a[3], b[3], c[3];
+                    image(t, probe[k], a);
+                    image(s, a, b);
+                    image(u, probe[k], c);
+                    same = b[0] == c[0] && b[1] == c[1] && b[2] == c[2];
+                }
+                if (same) found = u;
+            }
+            MLEM_REQUIRE(found >= 0, MLEM_EINVAL, "internal: symmetry group not closed");
+            comp[s][t] = (uint8_t)found;
+        }
+    for (int s = 0; s < 16; ++s)
+        for (int t = 0; t < 16; ++t)
+            if (comp[s][t] == 0) inv[s] = (uint8_t)t;
+}
+
+// ---------------------------------------------------------------- device maps
+using VoxMap = SymVoxMap;
+
+__host__ __device__ __forceinline__ VoxMap vox_map(int s, int32_t n, int32_t nz) {
+    // images of the origin and of the three unit steps (the map is affine)
+    auto img = [&](int32_t x, int32_t y, int32_t z) -> int32_t {
+        if ((s >> 2) & 1) y = n - 1 - y;
+        for (int q = 0; q < (s & 3); ++q) {
+            const int32_t t = x;
+            x = n - 1 - y;
+            y = t;
+        }
+        if (s >> 3) z = nz - 1 - z;
+        return x + n * (y + n * z);
+    };
+    VoxMap m;
+    m.c0 = img(0, 0, 0);
+    m.ax = img(1, 0, 0) - m.c0;
+    m.ay = img(0, 1, 0) - m.c0;
+    m.az = img(0, 0, 1) - m.c0;
+    return m;
+}
+
+template <typename V>
+__device__ __forceinline__ float ld_val(const V* p, uint64_t e) {
+    return Val4<V>::one(p, e);
+}
+
+template <typename V, int EPI>
+__global__ void __launch_bounds__(256)
+k_sym_fp(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ key, const V* __restrict__ val,
+         const uint32_t* __restrict__ img, const uint32_t* __restrict__ mask, uint32_t K,
+         const float* __restrict__ x, const int32_t* __restrict__ g, float* __restrict__ out,
+         float* __restrict__ fwproj, SymMapsArg vm) {
+    const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (k >= K) return;  // warp-uniform
+    float acc[16];
+#pragma unroll
+    for (int s = 0; s < 16; ++s) acc[s] = 0.f;
+    const uint64_t s0 = rowptr[k], s1 = rowptr[k + 1];
+    for (uint64_t e = s0 + lane; e < s1; e += 32) {
+        const uint32_t kk = __ldcs(key + e);
+        const float v = ld_val<V>(val, e);
+        const int32_t xx = (int32_t)(kk & 2047u), yy = (int32_t)((kk >> 11) & 2047u), zz = (int32_t)(kk >> 22);
+        float gx[16];
+#pragma unroll
+        for (int s = 0; s < 16; ++s) {
+            const VoxMap m = vm.m[s];
+            gx[s] = __ldg(x + (m.ax * xx + m.ay * yy + m.az * zz + m.c0));
+        }
+#pragma unroll
+        for (int s = 0; s < 16; ++s) acc[s] = fmaf(v, gx[s], acc[s]);
+    }
+    float mine = 0.f;
+#pragma unroll
+    for (int s = 0; s < 16; ++s) {
+        float a = acc[s];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == s) mine = a;
+    }
+    if (lane < 16 && ((mask[k] >> lane) & 1u)) {
+        const uint32_t r = img[16 * (uint64_t)k + lane];
+        if (EPI == (int)Epi::Correl) {
+            out[r] = (mine != 0.0f) ? __fdiv_rn((float)g[r], mine) : 0.0f;
+            if (fwproj) fwproj[r] = mine;
+        } else {
+            out[r] = mine;
+        }
+    }
+}
+
+template <typename V, int EPI>
+__global__ void __launch_bounds__(256)
+k_sym_bp(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ key, const V* __restrict__ val,
+         const uint32_t* __restrict__ vxyz, const uint32_t* __restrict__ vmask, uint32_t J,
+         const uint32_t* __restrict__ img, const uint8_t* __restrict__ comp, const float* __restrict__ ratio,
+         float* __restrict__ out, float* __restrict__ f, const float* __restrict__ norm, SymMapsArg vm) {
+    __shared__ uint8_t s_comp[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_comp[i] = comp[i];
+    __syncthreads();
+    const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (j >= J) return;  // warp-uniform, after the block barrier
+    float acc[16];
+#pragma unroll
+    for (int s = 0; s < 16; ++s) acc[s] = 0.f;
+    const uint64_t s0 = rowptr[j], s1 = rowptr[j + 1];
+    for (uint64_t e = s0 + lane; e < s1; e += 32) {
+        const uint32_t kk = __ldcs(key + e);
+        const float v = ld_val<V>(val, e);
+        const uint64_t base = 16 * (uint64_t)(kk >> 4);
+        const uint32_t t = kk & 15u;
+        uint32_t idx[16];
+#pragma unroll
+        for (int s = 0; s < 16; ++s) idx[s] = __ldg(img + base + s_comp[16 * s + t]);
+        float gr[16];
+#pragma unroll
+        for (int s = 0; s < 16; ++s) gr[s] = __ldg(ratio + idx[s]);
+#pragma unroll
+        for (int s = 0; s < 16; ++s) acc[s] = fmaf(v, gr[s], acc[s]);
+    }
+    float mine = 0.f;
+#pragma unroll
+    for (int s = 0; s < 16; ++s) {
+        float a = acc[s];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == s) mine = a;
+    }
+    if (lane < 16 && ((vmask[j] >> lane) & 1u)) {
+        const uint32_t p = vxyz[j];
+        const VoxMap m = vm.m[lane];
+        const uint32_t c = (uint32_t)(m.ax * (int32_t)(p & 2047u) + m.ay * (int32_t)((p >> 11) & 2047u) +
+                                      m.az * (int32_t)(p >> 22) + m.c0);
+        if (EPI == (int)Epi::Update) {
+            const float tt = __fmul_rn(f[c], mine);
+            const float nn = norm[c];
+            f[c] = (nn == 0.0f) ? tt : __fdiv_rn(tt, nn);
+        } else {
+            out[c] = mine;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- build kernels
+// Row lengths of A^ (natural LOR order): every row has its canonical row's length.
+__global__ void k_sym_lens(const uint64_t* __restrict__ crp, const uint32_t* __restrict__ can_row, uint64_t nlor,
+                           uint32_t* __restrict__ len) {
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < nlor; r += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = can_row[r];
+        len[r] = (uint32_t)(crp[k + 1] - crp[k]);
+    }
+}
+
+// Row r of A^ (unsorted) = canonical row can_row[r] with columns mapped by sym_of[r].
+__global__ void k_sym_expand(const uint64_t* __restrict__ crp, const uint32_t* __restrict__ ccol,
+                             const float* __restrict__ cval, const uint32_t* __restrict__ can_row,
+                             const uint8_t* __restrict__ sym_of, uint64_t nlor, uint32_t n, uint32_t nz,
+                             const uint64_t* __restrict__ orp, uint32_t* __restrict__ ocol, float* __restrict__ oval) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint64_t r = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; r < nlor;
+         r += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+        const uint32_t k = can_row[r];
+        const VoxMap m = vox_map(sym_of[r], (int32_t)n, (int32_t)nz);
+        const uint64_t s = crp[k], len = crp[k + 1] - s, o = orp[r];
+        for (uint64_t t = lane; t < len; t += 32) {
+            const uint32_t c = ccol[s + t];
+            const uint32_t xx = c % n, yy = (c / n) % n, zz = c / (n * n);
+            ocol[o + t] = (uint32_t)(m.ax * (int32_t)xx + m.ay * (int32_t)yy + m.az * (int32_t)zz + m.c0);
+            oval[o + t] = cval[s + t];
+        }
+    }
+}
+
+__global__ void k_pack_xyz(const uint32_t* __restrict__ col, uint64_t nnz, uint32_t n, uint32_t* __restrict__ key) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nnz; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = col[e];
+        key[e] = (c % n) | (((c / n) % n) << 11) | ((c / (n * n)) << 22);
+    }
+}
+
+// Rows of A^T for the canonical voxels, entries r' -> can_row[r'] << 4 | sym_of[r'].
+__global__ void k_sym_bp_lens(const uint64_t* __restrict__ trp, const uint32_t* __restrict__ vrow, uint32_t J,
+                              uint32_t* __restrict__ len) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < J; j += gridDim.x * blockDim.x)
+        len[j] = (uint32_t)(trp[vrow[j] + 1] - trp[vrow[j]]);
+}
+
+__global__ void k_sym_bp_fill(const uint64_t* __restrict__ trp, const uint32_t* __restrict__ tidx,
+                              const float* __restrict__ tval, const uint32_t* __restrict__ vrow, uint32_t J,
+                              const uint32_t* __restrict__ can_row, const uint8_t* __restrict__ sym_of,
+                              const uint64_t* __restrict__ brp, uint32_t* __restrict__ bkey,
+                              float* __restrict__ bval) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint64_t j = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; j < J;
+         j += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+        const uint64_t s = trp[vrow[j]], len = trp[vrow[j] + 1] - s, o = brp[j];
+        for (uint64_t t = lane; t < len; t += 32) {
+            const uint32_t r = tidx[s + t];
+            bkey[o + t] = (can_row[r] << 4) | sym_of[r];
+            bval[o + t] = tval[s + t];
+        }
+    }
+}
+
+unsigned grid_of(uint64_t n) { return std::max(1u, std::min<unsigned>(ceil_div_u(n, 256), 152u * 32u)); }
+
+template <typename T>
+T* upload(const std::vector<T>& h, size_t min_elems = 1) {
+    T* d = nullptr;
+    MLEM_CUDA(cudaMalloc(&d, sizeof(T) * std::max(h.size(), min_elems)));
+    if (!h.empty()) MLEM_CUDA(cudaMemcpy(d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+    return d;
+}
+
+template <typename V, int EPI>
+void fp_launch(const SymOps& y, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+    launch_ex(k_sym_fp<V, EPI>, dim3(ceil_div_u((uint64_t)y.K * 32, 256)), dim3(256), 0, s, win, y.fp_rowptr,
+              y.fp_key, static_cast<const V*>(y.fp_val), y.img, y.fp_mask, y.K, x, e.g, e.out, e.fwproj, y.maps);
+}
+
+template <typename V, int EPI>
+void bp_launch(const SymOps& y, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+    launch_ex(k_sym_bp<V, EPI>, dim3(ceil_div_u((uint64_t)y.J * 32, 256)), dim3(256), 0, s, win, y.bp_rowptr,
+              y.bp_key, static_cast<const V*>(y.bp_val), y.vxyz, y.vmask, y.J, y.img, y.comp, x, e.out, e.f, e.norm,
+              y.maps);
+}
+
+template <typename V>
+void sym_dispatch(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+    if (!transposed) {
+        if (e.kind == Epi::Correl) fp_launch<V, (int)Epi::Correl>(y, x, e, win, s);
+        else fp_launch<V, (int)Epi::Raw>(y, x, e, win, s);
+    } else {
+        if (e.kind == Epi::Update) bp_launch<V, (int)Epi::Update>(y, x, e, win, s);
+        else bp_launch<V, (int)Epi::Raw>(y, x, e, win, s);
+    }
+}
+
+}  // namespace
+
+void SymOps::release() {
+    cudaFree(fp_rowptr);
+    cudaFree(fp_key);
+    cudaFree(fp_val);
+    cudaFree(img);
+    cudaFree(fp_mask);
+    cudaFree(bp_rowptr);
+    cudaFree(bp_key);
+    cudaFree(bp_val);
+    cudaFree(vxyz);
+    cudaFree(vmask);
+    cudaFree(comp);
+    *this = SymOps();
+}
+
+uint64_t SymOps::bytes() const {
+    if (!fp_rowptr) return 0;
+    const size_t vb = val_bytes(vt);
+    return sizeof(uint64_t) * (K + 1 + J + 1) + (4 + vb) * (fp_nnz + bp_nnz) + 4 * (17 * (uint64_t)K + 2 * J) + 256;
+}
+
+void check_symmetric_geometry(const mlem_geometry& g) {
+    MLEM_REQUIRE(g.nx == g.ny, MLEM_EUNSUPPORTED, "symmetry needs a square voxel grid (nx == ny)");
+    MLEM_REQUIRE(g.det_per_ring % 4 == 0, MLEM_EUNSUPPORTED, "symmetry needs a multiple of 4 detectors per ring");
+    MLEM_REQUIRE(g.row_stride <= 1, MLEM_EUNSUPPORTED, "symmetry needs every LOR (row_stride 1)");
+    MLEM_REQUIRE(g.nx < 2048 && g.nz < 1024, MLEM_EUNSUPPORTED, "symmetry: voxel grid too large for packed indices");
+    MLEM_REQUIRE(g.vx == g.vy, MLEM_EUNSUPPORTED, "symmetry needs square voxels in the transaxial plane");
+}
+
+void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y, cudaStream_t s) {
+    check_symmetric_geometry(geo);
+    SymMaps M;
+    M.n = geo.nx;
+    M.nz = geo.nz;
+    M.dpr = geo.det_per_ring;
+    M.rings = geo.n_rings;
+    M.D = M.dpr * M.rings;
+    const uint64_t D = M.D, nlor = D * (D - 1) / 2, cols = (uint64_t)M.n * M.n * M.nz;
+    MLEM_REQUIRE(nlor < (1ull << 32), MLEM_EUNSUPPORTED, "symmetry: too many LORs");
+    uint8_t comp[16][16], inv[16];
+    composition(M, comp, inv);
+
+    // LOR orbits: canonical rows (smallest index of each orbit) and, for every
+    // LOR, its canonical row and the first transformation that produces it
+    std::vector<uint8_t> canon_flag(nlor, 0);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t a = 0; a < (int64_t)D - 1; ++a) {
+        for (uint64_t b = (uint64_t)a + 1; b < D; ++b) {
+            const uint64_t r = M.lor((uint64_t)a, b);
+            uint64_t mn = r;
+            for (int t = 1; t < 16; ++t) mn = std::min<uint64_t>(mn, M.lor(M.det(t, (uint32_t)a), M.det(t, (uint32_t)b)));
+            canon_flag[r] = mn == r;
+        }
+    }
+    std::vector<uint64_t> canon;
+    std::vector<uint32_t> pair_a;
+    for (uint64_t a = 0; a + 1 < D; ++a)
+        for (uint64_t b = a + 1; b < D; ++b)
+            if (canon_flag[M.lor(a, b)]) {
+                canon.push_back(M.lor(a, b));
+                pair_a.push_back((uint32_t)a);
+            }
+    std::vector<uint8_t>().swap(canon_flag);
+    const uint64_t K = canon.size();
+    MLEM_REQUIRE(K < (1ull << 28), MLEM_EUNSUPPORTED, "symmetry: too many canonical rows");
+    std::vector<uint32_t> img(16 * K), mask(K, 0), can_row(nlor);
+    std::vector<uint8_t> sym_of(nlor);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < (int64_t)K; ++k) {
+        const uint64_t r = canon[k];
+        const uint32_t a = pair_a[k], b = (uint32_t)(r - M.lor(a, a + 1) + a + 1);
+        for (int t = 0; t < 16; ++t) {
+            const uint64_t im = M.lor(M.det(t, a), M.det(t, b));
+            img[16 * k + t] = (uint32_t)im;
+            bool first = true;
+            for (int u = 0; u < t && first; ++u) first = img[16 * k + u] != im;
+            if (first) {
+                mask[k] |= 1u << t;
+                can_row[im] = (uint32_t)k;
+                sym_of[im] = (uint8_t)t;
+            }
+        }
+    }
+    // voxel orbits
+    std::vector<uint32_t> vrow, vxyz, vmask;
+    for (uint32_t c = 0; c < cols; ++c) {
+        uint32_t mn = c;
+        for (int t = 1; t < 16; ++t) mn = std::min(mn, M.vox_index(t, c));
+        if (mn != c) continue;
+        uint32_t msk = 0;
+        uint32_t seen[16];
+        for (int t = 0; t < 16; ++t) {
+            seen[t] = M.vox_index(t, c);
+            bool first = true;
+            for (int u = 0; u < t && first; ++u) first = seen[u] != seen[t];
+            if (first) msk |= 1u << t;
+        }
+        vrow.push_back(c);
+        vxyz.push_back((c % M.n) | (((c / M.n) % M.n) << 11) | ((c / (M.n * M.n)) << 22));
+        vmask.push_back(msk);
+    }
+
+    // canonical rows, averaged over the transformations that fix their LOR
+    std::vector<uint64_t> crp;
+    std::vector<uint32_t> ccol;
+    std::vector<float> cval;
+    siddon_rows_of_lors(geo, canon, crp, ccol, cval);
+    {
+        std::vector<uint64_t> nrp(K + 1, 0);
+        std::vector<uint32_t> ncol;
+        std::vector<float> nval;
+        ncol.reserve(ccol.size());
+        nval.reserve(cval.size());
+        for (uint64_t k = 0; k < K; ++k) {
+            const uint64_t r = canon[k];
+            int H[16], nh = 0;
+            for (int t = 0; t < 16; ++t)
+                if (img[16 * k + t] == r) H[nh++] = t;
+            if (nh == 1) {
+                for (uint64_t e = crp[k]; e < crp[k + 1]; ++e) {
+                    ncol.push_back(ccol[e]);
+                    nval.push_back(cval[e]);
+                }
+            } else {
+                std::map<uint32_t, float> orig;
+                for (uint64_t e = crp[k]; e < crp[k + 1]; ++e) orig[ccol[e]] = cval[e];
+                std::map<uint32_t, double> sym;
+                for (const auto& kv : orig)
+                    for (int h = 0; h < nh; ++h) sym[M.vox_index(H[h], kv.first)] = 0.0;
+                for (auto& kv : sym) {
+                    double acc = 0.0;
+                    for (int h = 0; h < nh; ++h) {
+                        auto it = orig.find(M.vox_index(inv[H[h]], kv.first));
+                        if (it != orig.end()) acc += it->second;
+                    }
+                    kv.second = acc / nh;
+                }
+                for (const auto& kv : sym) {
+                    ncol.push_back(kv.first);
+                    nval.push_back((float)kv.second);
+                }
+            }
+            nrp[k + 1] = ncol.size();
+        }
+        crp.swap(nrp);
+        ccol.swap(ncol);
+        cval.swap(nval);
+    }
+    const uint64_t cnnz = crp[K];
+
+    // device: canonical rows, then A^ (every LOR) by expansion and two stable transposes
+    uint64_t* d_crp = nullptr;
+    uint32_t *d_ccol = nullptr, *d_can = nullptr, *len = nullptr;
+    float* d_cval = nullptr;
+    uint8_t* d_sym = nullptr;
+    DevCsr R;
+    try {
+        d_crp = upload(crp);
+        d_ccol = upload(ccol);
+        d_cval = upload(cval);
+        d_can = upload(can_row);
+        d_sym = upload(sym_of);
+        R.nrows = (uint32_t)nlor;
+        R.ncols = (uint32_t)cols;
+        R.vt = MLEM_VAL_F32;
+        MLEM_CUDA(cudaMalloc(&len, sizeof(uint32_t) * std::max<uint64_t>(nlor, 1)));
+        k_sym_lens<<<grid_of(nlor), 256, 0, s>>>(d_crp, d_can, nlor, len);
+        MLEM_LAUNCHED();
+        MLEM_CUDA(cudaMalloc(&R.rowptr, sizeof(uint64_t) * (nlor + 1)));
+        scan_counts_u64(len, R.rowptr, nlor, s);
+        MLEM_CUDA(cudaMemcpyAsync(&R.nnz, R.rowptr + nlor, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        MLEM_CUDA(cudaMalloc(&R.idx, sizeof(uint32_t) * padded(R.nnz)));
+        MLEM_CUDA(cudaMalloc(&R.val, sizeof(float) * padded(R.nnz)));
+        MLEM_CUDA(cudaMemsetAsync(R.idx, 0, sizeof(uint32_t) * padded(R.nnz), s));
+        MLEM_CUDA(cudaMemsetAsync(R.val, 0, sizeof(float) * padded(R.nnz), s));
+        k_sym_expand<<<grid_of(nlor * 32), 256, 0, s>>>(d_crp, d_ccol, d_cval, d_can, d_sym, nlor, M.n, M.nz,
+                                                         R.rowptr, R.idx, static_cast<float*>(R.val));
+        MLEM_LAUNCHED();
+        transpose_device(R, AT, s);  // voxel rows, LORs ascending: the transpose of A^
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        cudaFree(R.rowptr);
+        cudaFree(R.idx);
+        cudaFree(R.val);
+        R = DevCsr();
+        transpose_device(AT, A, s);  // A^, columns ascending in every row
+        A.max_row = max_row_length(A.rowptr, A.nrows, s);
+
+        // forward-projection operand: canonical rows with packed columns
+        y.n = M.n;
+        y.nz = M.nz;
+        y.K = (uint32_t)K;
+        y.fp_nnz = cnnz;
+        y.fp_rowptr = d_crp;
+        d_crp = nullptr;
+        MLEM_CUDA(cudaMalloc(&y.fp_key, sizeof(uint32_t) * std::max<uint64_t>(cnnz, 1)));
+        if (cnnz) {
+            k_pack_xyz<<<grid_of(cnnz), 256, 0, s>>>(d_ccol, cnnz, M.n, y.fp_key);
+            MLEM_LAUNCHED();
+        }
+        y.fp_val = d_cval;
+        d_cval = nullptr;
+        y.img = upload(img);
+        y.fp_mask = upload(mask);
+        // back-projection operand: rows of A^T for the canonical voxels
+        y.J = (uint32_t)vrow.size();
+        uint32_t* d_vrow = upload(vrow);
+        uint32_t* blen = nullptr;
+        MLEM_CUDA(cudaMalloc(&blen, sizeof(uint32_t) * std::max<uint32_t>(y.J, 1)));
+        MLEM_CUDA(cudaMalloc(&y.bp_rowptr, sizeof(uint64_t) * ((uint64_t)y.J + 1)));
+        k_sym_bp_lens<<<grid_of(y.J), 256, 0, s>>>(AT.rowptr, d_vrow, y.J, blen);
+        MLEM_LAUNCHED();
+        scan_counts_u64(blen, y.bp_rowptr, y.J, s);
+        MLEM_CUDA(cudaMemcpyAsync(&y.bp_nnz, y.bp_rowptr + y.J, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        MLEM_CUDA(cudaMalloc(&y.bp_key, sizeof(uint32_t) * std::max<uint64_t>(y.bp_nnz, 1)));
+        MLEM_CUDA(cudaMalloc(&y.bp_val, sizeof(float) * std::max<uint64_t>(y.bp_nnz, 1)));
+        k_sym_bp_fill<<<grid_of((uint64_t)y.J * 32), 256, 0, s>>>(AT.rowptr, AT.idx, static_cast<const float*>(AT.val),
+                                                                   d_vrow, y.J, d_can, d_sym, y.bp_rowptr, y.bp_key,
+                                                                   static_cast<float*>(y.bp_val));
+        MLEM_LAUNCHED();
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        cudaFree(d_vrow);
+        cudaFree(blen);
+        y.vxyz = upload(vxyz);
+        y.vmask = upload(vmask);
+        std::vector<uint8_t> comp_flat(256);
+        for (int a = 0; a < 16; ++a)
+            for (int b = 0; b < 16; ++b) comp_flat[16 * a + b] = comp[a][b];
+        y.comp = upload(comp_flat);
+        y.vt = MLEM_VAL_F32;
+        for (int t = 0; t < 16; ++t) y.maps.m[t] = vox_map(t, (int32_t)M.n, (int32_t)M.nz);
+    } catch (...) {
+        cudaStreamSynchronize(s);
+        cudaFree(d_crp);
+        cudaFree(d_ccol);
+        cudaFree(d_cval);
+        cudaFree(d_can);
+        cudaFree(d_sym);
+        cudaFree(len);
+        cudaFree(R.rowptr);
+        cudaFree(R.idx);
+        cudaFree(R.val);
+        throw;
+    }
+    cudaFree(d_ccol);
+    cudaFree(d_can);
+    cudaFree(d_sym);
+    cudaFree(len);
+}
+
+void lower_symmetric_values(SymOps& y, mlem_value_type vt, cudaStream_t s) {
+    if (vt == MLEM_VAL_F32 || !y.fp_rowptr) return;
+    auto lower = [&](void*& v, uint64_t n) {
+        void* nv = nullptr;
+        MLEM_CUDA(cudaMalloc(&nv, 2 * std::max<uint64_t>(n, 1)));
+        convert_values(static_cast<const float*>(v), nv, vt, n, s);
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        cudaFree(v);
+        v = nv;
+    };
+    lower(y.fp_val, y.fp_nnz);
+    lower(y.bp_val, y.bp_nnz);
+    y.vt = vt;
+}
+
+void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+    MLEM_REQUIRE(y.fp_rowptr != nullptr, MLEM_EINVAL, "matrix has no symmetry operands");
+    switch (y.vt) {
+        case MLEM_VAL_F32: sym_dispatch<float>(y, transposed, x, e, win, s); break;
+        case MLEM_VAL_F16: sym_dispatch<__half>(y, transposed, x, e, win, s); break;
+        default: sym_dispatch<__nv_bfloat16>(y, transposed, x, e, win, s);
+    }
+}
+
+}  // namespace mlem

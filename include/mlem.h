@@ -88,6 +88,16 @@ typedef struct {
     uint32_t grid_nx, grid_ny, grid_nz; /* voxel grid of the columns (column = x + nx*(y + ny*z),
                                    scannerconfig.cpp:30-35) for the locality layout of
                                    mlem_matrix_create; csr4 files and geometries carry their own */
+    uint32_t symmetry;          /* mlem_matrix_generate only: 1 = use the 16 symmetries of the scanner
+                                   (mirror y -> -y, rotations by 90 degrees, axial flip; needs
+                                   det_per_ring % 4 == 0, nx == ny, vx == vy, row_stride 1, natural
+                                   layout).  The matrix becomes A^, built from the canonical LOR rows
+                                   (averaged over the symmetries that fix their LOR) so that it is
+                                   exactly symmetric; it stays the matrix of every mode and getter.
+                                   Beside it: compact operands holding 1/16 of the nonzeros for the
+                                   csr-vector projections (kernel SYM, an autotuner candidate).  No
+                                   counterpart in the reference (its csr4 symmetry flags are not
+                                   expanded, csr4matrix.cpp:72-75). */
 } mlem_matrix_opts;
 
 /* Device layout of a matrix.  LOCALITY stores A' = P_L A P_Vᵀ: columns
@@ -182,8 +192,9 @@ typedef enum {
     MLEM_KERNEL_AUTO = 3, /* autotuned per matrix operand (lanes per row, vectors in flight, variant) */
     MLEM_KERNEL_D16 = 4,  /* delta-compressed indices (matrix created with compress_indices = 1) */
     MLEM_KERNEL_ILV = 5,  /* lane-interleaved copy (matrix created with interleave = 1) */
-    MLEM_KERNEL_ORDERED = 6 /* DIRECT with rows in locality order (generated matrices:
+    MLEM_KERNEL_ORDERED = 6, /* DIRECT with rows in locality order (generated matrices:
                                LORs in 4x4 detector tubes, voxels in 4x2x2 bricks) */
+    MLEM_KERNEL_SYM = 7   /* symmetry-compressed operands (generated with symmetry = 1) */
 } mlem_kernel;
 
 /* Defaults: CSR_VECTOR, BP_TRANS, secsize 5/5, graphs on, no log-likelihood, L2 window on,
