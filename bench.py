@@ -427,6 +427,57 @@ def run_forms(pkg, torch, args):
     return res
 
 
+def run_symmetry(pkg, torch, name):
+    """Symmetry-compressed operands on the workload's scanner: the symmetric
+    matrix A^ (16 symmetries), MLEM iterations/s with the autotuned kernels and
+    with each of the compact (SYM) and full csr-vector (DIRECT) kernels on the
+    same A^, the stage times and the device bytes; and how far the A^ image is
+    from the image of the plain generated matrix on the same sinogram."""
+    from mlem_gb300 import synth
+    s = torch.cuda.current_stream()
+    cfg = WORKLOADS[name]
+    geo = pkg.preset(name)
+    its = cfg["iters"]
+    out = {"workload": f"{name}, natural layout, 16 symmetries"}
+    plain = pkg.Matrix.generate(geo)
+    xt = torch.from_numpy(synth.phantom(geo, cfg["shapes"], seed=1).astype(np.float32)).cuda()
+    dz = torch.zeros(plain.rows, dtype=torch.int32, device="cuda")
+    ratio = torch.zeros(plain.rows, dtype=torch.float32, device="cuda")
+    fp = torch.zeros(plain.rows, dtype=torch.float32, device="cuda")
+    plain.forward_project(xt.data_ptr(), dz.data_ptr(), ratio.data_ptr(), fp.data_ptr(), stream=s.cuda_stream)
+    torch.cuda.synchronize()
+    g = synth.poisson_sinogram(fp.cpu().numpy().astype(np.float64), cfg["total"], seed=2)
+    f0 = np.full(plain.cols, plain.initial_value(g), np.float32)
+    img_plain = plain.run(g, its, f0=f0)
+    plain_bytes = plain.device_bytes
+    plain.close()
+    for vt, label in ((pkg.VAL_F32, "fp32"), (pkg.VAL_F16, "fp16")):
+        t0 = time.time()
+        m = pkg.Matrix.generate(geo, value_type=vt, symmetry=True)
+        r = {"build_s": time.time() - t0, "device_bytes": m.device_bytes, "plain_fp32_device_bytes": plain_bytes}
+        g_dev = torch.from_numpy(g).cuda()
+        f0_dev = torch.from_numpy(f0).cuda()
+        f_dev = torch.empty_like(f0_dev)
+        for klabel, kern in (("autotuned", pkg.KERNEL_AUTO), ("sym", pkg.KERNEL_SYM), ("direct", pkg.KERNEL_DIRECT)):
+            f_dev.copy_(f0_dev)
+            m.run_device(g_dev.data_ptr(), f_dev.data_ptr(), 5, stream=s.cuda_stream, kernel=kern)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f_dev.copy_(f0_dev)
+            a.record(s)
+            m.run_device(g_dev.data_ptr(), f_dev.data_ptr(), its, stream=s.cuda_stream, kernel=kern)
+            b.record(s)
+            b.synchronize()
+            kt = time_kernels(pkg, m, torch, g, f0, iters=10, kernel=kern)
+            r[klabel] = {"iterations_per_s": its / (a.elapsed_time(b) * 1e-3), "fp_ms": kt["fp"], "bp_ms": kt["bp"]}
+        r["tuning"] = {"fp": m.tuning(False), "bp": m.tuning(True)}
+        img = m.run(g, its, f0=f0)
+        r["image_rel_l2_vs_plain_matrix"] = float(np.linalg.norm(img.astype(np.float64) - img_plain)
+                                                  / np.linalg.norm(img_plain.astype(np.float64)))
+        m.close()
+        out[label] = r
+    return out
+
+
 def run_serving(pkg, torch, n_requests=300, rate=50.0, fp32_iter_s=None):
     """Serving form: three resident matrices (2-D ring FP32, 3-D mid FP32,
     12 GB class FP16), Poisson arrivals, continuous batching in the server."""
@@ -509,9 +560,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cyl3d_12gb", choices=sorted(WORKLOADS))
-    ap.add_argument("--forms", default="all", choices=["all", "none", "modes"],
-                    help="all: FP16, batched, serving and the modes on the smaller matrices; modes: only the "
-                         "reference's switch combinations, the fused pass and a batched run on --workload")
+    ap.add_argument("--forms", default="all", choices=["all", "none", "modes", "symmetry"],
+                    help="all: FP16, batched, serving, symmetry and the modes on the smaller matrices; modes: only "
+                         "the reference's switch combinations, the fused pass and a batched run on --workload; "
+                         "symmetry: only the symmetry-compressed operands on --workload")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--spmv", default="csr-vector", choices=["csr-vector", "merge"],
                     help="SpMV of the timed reconstruction (the reference's argv[8])")
@@ -644,6 +696,8 @@ def main():
     m.close()
     if args.forms == "modes":
         line["forms"] = run_modes(pkg, torch, name)
+    if args.forms == "symmetry":
+        line["forms"] = {"symmetry": run_symmetry(pkg, torch, name)}
     if args.forms == "all":
         line["forms"] = run_forms(pkg, torch, args)
         line["forms"]["fp32_plain"] = {"images_iterations_per_s": value / world}
@@ -652,6 +706,7 @@ def main():
             "images_iterations_per_s")}
         if all(rates.values()):
             line["forms"]["serving"] = run_serving(pkg, torch, fp32_iter_s=rates)
+        line["forms"]["symmetry"] = run_symmetry(pkg, torch, name)
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(pkg, name, WORKLOADS[name]["cpu_stride"])
         full_nnz = line["config"]["nnz"]
