@@ -129,32 +129,27 @@ void remap_csr(const DevCsr& in, const uint32_t* row_src, const uint32_t* col_ma
                cudaStream_t s);
 
 // ------------------------------------------------------------- symmetry.cu
-// s(x, y, z) of a voxel as an index: ax*x + ay*y + az*z + c0
-struct SymVoxMap {
-    int32_t ax, ay, az, c0;
-};
-struct SymMapsArg {
-    SymVoxMap m[16];
-};
 // Symmetry-compressed projection operands of a generated cylindrical scanner
-// (see symmetry.cu): canonical LOR rows for the forward projection, canonical
-// voxel rows of A^T for the back projection.
+// (see symmetry.cu).  Rows: canonical LORs (forward projection) and canonical
+// voxels (back projection over A^T); an entry names its column as an orbit
+// row and a transformation, key = orbit << 4 | t.  The orbit arrays hold the
+// input vector in orbit order (16 floats per canonical voxel / LOR) and are
+// per-handle scratch, refilled before every projection.
 struct SymOps {
-    uint32_t n = 0, nz = 0;          // square voxel grid n x n x nz
     uint32_t K = 0, J = 0;           // canonical LOR rows / canonical voxel rows
     uint64_t fp_nnz = 0, bp_nnz = 0;
     uint64_t* fp_rowptr = nullptr;   // [K+1]
-    uint32_t* fp_key = nullptr;      // [fp_nnz] x | y << 11 | z << 22
+    uint32_t* fp_key = nullptr;      // [fp_nnz] canonical voxel << 4 | t
     void* fp_val = nullptr;          // [fp_nnz]
     uint32_t* img = nullptr;         // [16 K] LOR s(r_k)
-    uint32_t* fp_mask = nullptr;     // [K] transformations giving distinct LORs
+    uint32_t* mask = nullptr;        // [K] transformations giving distinct LORs
     uint64_t* bp_rowptr = nullptr;   // [J+1]
-    uint32_t* bp_key = nullptr;      // [bp_nnz] canonical row << 4 | transformation
+    uint32_t* bp_key = nullptr;      // [bp_nnz] canonical LOR << 4 | t
     void* bp_val = nullptr;          // [bp_nnz]
-    uint32_t* vxyz = nullptr;        // [J] packed canonical voxel
+    uint32_t* vimg = nullptr;        // [16 J] voxel s(v_j)
     uint32_t* vmask = nullptr;       // [J] transformations giving distinct voxels
-    uint8_t* comp = nullptr;         // [256] composition table: comp[16 s + t] = s after t
-    SymMapsArg maps{};               // voxel maps of the 16 transformations
+    float* orb_x = nullptr;          // [16 J] image in orbit order (forward projection input)
+    float* orb_r = nullptr;          // [16 K] ratio in orbit order (back projection input)
     mlem_value_type vt = MLEM_VAL_F32;
     void release();
     uint64_t bytes() const;

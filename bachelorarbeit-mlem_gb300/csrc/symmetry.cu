@@ -15,17 +15,25 @@
 // fixed by some transformations, averaged over them so that
 // A^[s(r), s(c)] = A^[r, c] holds exactly.  A^ and its transpose stay the
 // matrix of the handle (every mode and getter uses them); beside them this
-// file keeps two compact operands:
-//   forward projection: the canonical rows (1/16 of the nonzeros), columns
-//     packed as x | y << 11 | z << 22, and img[16 k + s] = s(r_k) for each
-//     canonical row k;
-//   back projection over A^T: the rows of the canonical voxels (1/16 of the
-//     nonzeros), each entry a LOR r' = t(r_k) stored as k << 4 | t.
-// A warp handles one compact row; a lane takes consecutive elements and keeps
-// 16 accumulators, one per transformation, so the gathers of one instruction
-// follow one transformed ray (32 consecutive voxels / LORs).  The FP gathers
-// f[s(c)]; the BP gathers ratio[img[16 k + s*t]].  Each distinct image row
-// (LOR s(r_k), voxel s(v)) is written by the first s that produces it.
+// file keeps two compact operands with 1/16 of the nonzeros each:
+//   forward projection: the canonical LOR rows r_k; an entry for voxel
+//     c = t(v_j) is stored as j << 4 | t (v_j the canonical voxel of c);
+//   back projection over A^T: the canonical voxel rows v_j; an entry for
+//     LOR r = t(r_k) is stored as k << 4 | t.
+// Row k of the product for transformation s needs the input at s(t(v_j)):
+// with the input laid out in orbit order, O[16 j + u] = x[u(v_j)], that is
+// O[16 j + (s o t)].  Writing s = F^f R^q M^m (mirror M first, then q
+// rotations R, then the axial flip F; M R = R^-1 M, F central),
+//   s o t = F^(f_s ^ f_t) R^(q_s + (m_s ? -q_t : q_t)) M^(m_s ^ m_t),
+// so for the four s sharing (m_s, f_s) the needed values are one aligned
+// float4 of the 64-byte orbit row (chunk (m_s ^ m_t) + 2 (f_s ^ f_t)),
+// rotated by q_t or -q_t.  A warp handles one compact row: 8 entries per
+// step, 4 lanes per entry (one per (m_s, f_s)), each lane one 16-byte load
+// and 4 accumulators; the 64 bytes an entry needs come in one coalesced
+// piece.  The orbit arrays (16 floats per canonical voxel / LOR, L2-resident)
+// are gathered from the natural-order input by a small kernel before each
+// projection; each distinct output row (LOR s(r_k), voxel s(v_j)) is written
+// by the first s that produces it.
 #include "kernels.cuh"
 
 #include <algorithm>
@@ -92,6 +100,10 @@ void composition(const SymMaps& M, uint8_t comp[16][16], uint8_t inv[16]) {
                 if (same) found = u;
             }
             MLEM_REQUIRE(found >= 0, MLEM_EINVAL, "internal: symmetry group not closed");
+            // the closed form the compact kernels use (orbit_chunk / orbit_fma)
+            const int d = ((s >> 2) & 1) ? (4 - (t & 3)) & 3 : (t & 3);
+            const int closed = ((s + d) & 3) + 4 * (((s >> 2) ^ (t >> 2)) & 1) + 8 * ((s >> 3) ^ (t >> 3));
+            MLEM_REQUIRE(found == closed, MLEM_EINVAL, "internal: symmetry composition differs from its closed form");
             comp[s][t] = (uint8_t)found;
         }
     for (int s = 0; s < 16; ++s)
@@ -100,10 +112,12 @@ void composition(const SymMaps& M, uint8_t comp[16][16], uint8_t inv[16]) {
 }
 
 // ---------------------------------------------------------------- device maps
-using VoxMap = SymVoxMap;
+// s(x, y, z) of a voxel as an index: ax*x + ay*y + az*z + c0 (the map is affine)
+struct VoxMap {
+    int32_t ax, ay, az, c0;
+};
 
 __host__ __device__ __forceinline__ VoxMap vox_map(int s, int32_t n, int32_t nz) {
-    // images of the origin and of the three unit steps (the map is affine)
     auto img = [&](int32_t x, int32_t y, int32_t z) -> int32_t {
         if ((s >> 2) & 1) y = n - 1 - y;
         for (int q = 0; q < (s & 3); ++q) {
@@ -127,102 +141,103 @@ __device__ __forceinline__ float ld_val(const V* p, uint64_t e) {
     return Val4<V>::one(p, e);
 }
 
-template <typename V, int EPI>
+// One entry of a compact row for the lane of group (mg, fg): the orbit row
+// float4 holding s o t for the four s = 4 (mg + 2 fg) + q.
+__device__ __forceinline__ uint32_t orbit_chunk(uint32_t kk, uint32_t mg, uint32_t fg) {
+    const uint32_t t = kk & 15u;
+    return ((kk >> 4) << 2) | ((mg ^ ((t >> 2) & 1u)) | ((fg ^ (t >> 3)) << 1));
+}
+
+// acc[q] += v * o[(q + d) & 3], d = q_t (mg = 0) or -q_t (mg = 1)
+__device__ __forceinline__ void orbit_fma(float4 o, float v, uint32_t kk, uint32_t mg, float (&acc)[4]) {
+    const uint32_t qt = kk & 3u;
+    const uint32_t d = (mg ? (4u - qt) : qt) & 3u;
+    float r0 = o.x, r1 = o.y, r2 = o.z, r3 = o.w;
+    if (d & 1u) {
+        const float t0 = r0;
+        r0 = r1;
+        r1 = r2;
+        r2 = r3;
+        r3 = t0;
+    }
+    if (d & 2u) {
+        float t0 = r0;
+        r0 = r2;
+        r2 = t0;
+        t0 = r1;
+        r1 = r3;
+        r3 = t0;
+    }
+    acc[0] = fmaf(v, r0, acc[0]);
+    acc[1] = fmaf(v, r1, acc[1]);
+    acc[2] = fmaf(v, r2, acc[2]);
+    acc[3] = fmaf(v, r3, acc[3]);
+}
+
+// Compact product with epilogue: out row oimg[16 row + s] for every s with
+// bit s of omask[row].  EPI Correl / Raw (forward projection: rows are
+// canonical LORs) or Update / Raw (back projection: canonical voxels).
+template <typename V, int EPI, int U>
 __global__ void __launch_bounds__(256)
-k_sym_fp(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ key, const V* __restrict__ val,
-         const uint32_t* __restrict__ img, const uint32_t* __restrict__ mask, uint32_t K,
-         const float* __restrict__ x, const int32_t* __restrict__ g, float* __restrict__ out,
-         float* __restrict__ fwproj, SymMapsArg vm) {
-    const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (k >= K) return;  // warp-uniform
-    float acc[16];
+k_sym_orbit(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ key, const V* __restrict__ val,
+            uint32_t nrows, const float4* __restrict__ orb, const uint32_t* __restrict__ oimg,
+            const uint32_t* __restrict__ omask, const int32_t* __restrict__ g, float* __restrict__ out,
+            float* __restrict__ fwproj, float* __restrict__ f, const float* __restrict__ norm) {
+    const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
+    if (row >= nrows) return;  // warp-uniform
+    const uint32_t mg = lane & 1u, fg = (lane >> 1) & 1u, slot = lane >> 2;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    const uint64_t s0 = rowptr[row], s1 = rowptr[row + 1];
+    uint64_t e = s0 + slot;
+    for (; e + 8 * (U - 1) < s1; e += 8 * U) {
+        uint32_t kk[U];
+        float v[U];
+        float4 o[U];
 #pragma unroll
-    for (int s = 0; s < 16; ++s) acc[s] = 0.f;
-    const uint64_t s0 = rowptr[k], s1 = rowptr[k + 1];
-    for (uint64_t e = s0 + lane; e < s1; e += 32) {
-        const uint32_t kk = __ldcs(key + e);
-        const float v = ld_val<V>(val, e);
-        const int32_t xx = (int32_t)(kk & 2047u), yy = (int32_t)((kk >> 11) & 2047u), zz = (int32_t)(kk >> 22);
-        float gx[16];
-#pragma unroll
-        for (int s = 0; s < 16; ++s) {
-            const VoxMap m = vm.m[s];
-            gx[s] = __ldg(x + (m.ax * xx + m.ay * yy + m.az * zz + m.c0));
+        for (int u = 0; u < U; ++u) {
+            kk[u] = __ldcs(key + e + 8 * u);
+            v[u] = ld_val<V>(val, e + 8 * u);
         }
 #pragma unroll
-        for (int s = 0; s < 16; ++s) acc[s] = fmaf(v, gx[s], acc[s]);
-    }
-    float mine = 0.f;
+        for (int u = 0; u < U; ++u) o[u] = __ldg(orb + orbit_chunk(kk[u], mg, fg));
 #pragma unroll
-    for (int s = 0; s < 16; ++s) {
-        float a = acc[s];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if (lane == s) mine = a;
+        for (int u = 0; u < U; ++u) orbit_fma(o[u], v[u], kk[u], mg, acc);
     }
-    if (lane < 16 && ((mask[k] >> lane) & 1u)) {
-        const uint32_t r = img[16 * (uint64_t)k + lane];
+    for (; e < s1; e += 8) {
+        const uint32_t kk = __ldcs(key + e);
+        const float v = ld_val<V>(val, e);
+        orbit_fma(__ldg(orb + orbit_chunk(kk, mg, fg)), v, kk, mg, acc);
+    }
+#pragma unroll
+    for (int o = 4; o < 32; o <<= 1)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+    // lane s (< 16) takes the total of s = 4 (mg + 2 fg) + q from lane s >> 2
+    const uint32_t sl = lane & 15u, src = sl >> 2, q = sl & 3u;
+    const float b0 = __shfl_sync(0xffffffffu, acc[0], src), b1 = __shfl_sync(0xffffffffu, acc[1], src);
+    const float b2 = __shfl_sync(0xffffffffu, acc[2], src), b3 = __shfl_sync(0xffffffffu, acc[3], src);
+    const float mine = q == 0 ? b0 : (q == 1 ? b1 : (q == 2 ? b2 : b3));
+    if (lane < 16 && ((omask[row] >> lane) & 1u)) {
+        const uint32_t r = oimg[16 * (uint64_t)row + lane];
         if (EPI == (int)Epi::Correl) {
             out[r] = (mine != 0.0f) ? __fdiv_rn((float)g[r], mine) : 0.0f;
             if (fwproj) fwproj[r] = mine;
+        } else if (EPI == (int)Epi::Update) {
+            const float tt = __fmul_rn(f[r], mine);
+            const float nn = norm[r];
+            f[r] = (nn == 0.0f) ? tt : __fdiv_rn(tt, nn);
         } else {
             out[r] = mine;
         }
     }
 }
 
-template <typename V, int EPI>
-__global__ void __launch_bounds__(256)
-k_sym_bp(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ key, const V* __restrict__ val,
-         const uint32_t* __restrict__ vxyz, const uint32_t* __restrict__ vmask, uint32_t J,
-         const uint32_t* __restrict__ img, const uint8_t* __restrict__ comp, const float* __restrict__ ratio,
-         float* __restrict__ out, float* __restrict__ f, const float* __restrict__ norm, SymMapsArg vm) {
-    __shared__ uint8_t s_comp[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_comp[i] = comp[i];
-    __syncthreads();
-    const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (j >= J) return;  // warp-uniform, after the block barrier
-    float acc[16];
-#pragma unroll
-    for (int s = 0; s < 16; ++s) acc[s] = 0.f;
-    const uint64_t s0 = rowptr[j], s1 = rowptr[j + 1];
-    for (uint64_t e = s0 + lane; e < s1; e += 32) {
-        const uint32_t kk = __ldcs(key + e);
-        const float v = ld_val<V>(val, e);
-        const uint64_t base = 16 * (uint64_t)(kk >> 4);
-        const uint32_t t = kk & 15u;
-        uint32_t idx[16];
-#pragma unroll
-        for (int s = 0; s < 16; ++s) idx[s] = __ldg(img + base + s_comp[16 * s + t]);
-        float gr[16];
-#pragma unroll
-        for (int s = 0; s < 16; ++s) gr[s] = __ldg(ratio + idx[s]);
-#pragma unroll
-        for (int s = 0; s < 16; ++s) acc[s] = fmaf(v, gr[s], acc[s]);
-    }
-    float mine = 0.f;
-#pragma unroll
-    for (int s = 0; s < 16; ++s) {
-        float a = acc[s];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if (lane == s) mine = a;
-    }
-    if (lane < 16 && ((vmask[j] >> lane) & 1u)) {
-        const uint32_t p = vxyz[j];
-        const VoxMap m = vm.m[lane];
-        const uint32_t c = (uint32_t)(m.ax * (int32_t)(p & 2047u) + m.ay * (int32_t)((p >> 11) & 2047u) +
-                                      m.az * (int32_t)(p >> 22) + m.c0);
-        if (EPI == (int)Epi::Update) {
-            const float tt = __fmul_rn(f[c], mine);
-            const float nn = norm[c];
-            f[c] = (nn == 0.0f) ? tt : __fdiv_rn(tt, nn);
-        } else {
-            out[c] = mine;
-        }
-    }
+// orb[i] = src[table[i]]: the input vector in orbit order.
+__global__ void k_orbit_gather(float* __restrict__ orb, const float* __restrict__ src,
+                               const uint32_t* __restrict__ table, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        orb[i] = __ldg(src + __ldg(table + i));
 }
 
 // ---------------------------------------------------------------- build kernels
@@ -255,10 +270,12 @@ __global__ void k_sym_expand(const uint64_t* __restrict__ crp, const uint32_t* _
     }
 }
 
-__global__ void k_pack_xyz(const uint32_t* __restrict__ col, uint64_t nnz, uint32_t n, uint32_t* __restrict__ key) {
+// Columns of the canonical rows as canonical voxel << 4 | transformation.
+__global__ void k_sym_fp_keys(const uint32_t* __restrict__ col, uint64_t nnz, const uint32_t* __restrict__ vorb,
+                              const uint8_t* __restrict__ vsym, uint32_t* __restrict__ key) {
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nnz; e += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t c = col[e];
-        key[e] = (c % n) | (((c / n) % n) << 11) | ((c / (n * n)) << 22);
+        key[e] = (vorb[c] << 4) | vsym[c];
     }
 }
 
@@ -296,27 +313,30 @@ T* upload(const std::vector<T>& h, size_t min_elems = 1) {
     return d;
 }
 
-template <typename V, int EPI>
-void fp_launch(const SymOps& y, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
-    launch_ex(k_sym_fp<V, EPI>, dim3(ceil_div_u((uint64_t)y.K * 32, 256)), dim3(256), 0, s, win, y.fp_rowptr,
-              y.fp_key, static_cast<const V*>(y.fp_val), y.img, y.fp_mask, y.K, x, e.g, e.out, e.fwproj, y.maps);
-}
+constexpr int kOrbitUnroll = 4;
 
 template <typename V, int EPI>
-void bp_launch(const SymOps& y, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
-    launch_ex(k_sym_bp<V, EPI>, dim3(ceil_div_u((uint64_t)y.J * 32, 256)), dim3(256), 0, s, win, y.bp_rowptr,
-              y.bp_key, static_cast<const V*>(y.bp_val), y.vxyz, y.vmask, y.J, y.img, y.comp, x, e.out, e.f, e.norm,
-              y.maps);
+void orbit_launch(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+    const uint32_t rows = transposed ? y.J : y.K;
+    float* orb = transposed ? y.orb_r : y.orb_x;
+    const uint32_t* table = transposed ? y.img : y.vimg;  // input orbits: LORs for BP, voxels for FP
+    const uint64_t n_orb = 16ull * (transposed ? y.K : y.J);
+    k_orbit_gather<<<grid_of(n_orb), 256, 0, s>>>(orb, x, table, n_orb);
+    MLEM_LAUNCHED();
+    launch_ex(k_sym_orbit<V, EPI, kOrbitUnroll>, dim3(ceil_div_u((uint64_t)rows * 32, 256)), dim3(256), 0, s, win,
+              transposed ? y.bp_rowptr : y.fp_rowptr, transposed ? y.bp_key : y.fp_key,
+              static_cast<const V*>(transposed ? y.bp_val : y.fp_val), rows, reinterpret_cast<const float4*>(orb),
+              transposed ? y.vimg : y.img, transposed ? y.vmask : y.mask, e.g, e.out, e.fwproj, e.f, e.norm);
 }
 
 template <typename V>
 void sym_dispatch(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
     if (!transposed) {
-        if (e.kind == Epi::Correl) fp_launch<V, (int)Epi::Correl>(y, x, e, win, s);
-        else fp_launch<V, (int)Epi::Raw>(y, x, e, win, s);
+        if (e.kind == Epi::Correl) orbit_launch<V, (int)Epi::Correl>(y, false, x, e, win, s);
+        else orbit_launch<V, (int)Epi::Raw>(y, false, x, e, win, s);
     } else {
-        if (e.kind == Epi::Update) bp_launch<V, (int)Epi::Update>(y, x, e, win, s);
-        else bp_launch<V, (int)Epi::Raw>(y, x, e, win, s);
+        if (e.kind == Epi::Update) orbit_launch<V, (int)Epi::Update>(y, true, x, e, win, s);
+        else orbit_launch<V, (int)Epi::Raw>(y, true, x, e, win, s);
     }
 }
 
@@ -327,27 +347,27 @@ void SymOps::release() {
     cudaFree(fp_key);
     cudaFree(fp_val);
     cudaFree(img);
-    cudaFree(fp_mask);
+    cudaFree(mask);
     cudaFree(bp_rowptr);
     cudaFree(bp_key);
     cudaFree(bp_val);
-    cudaFree(vxyz);
+    cudaFree(vimg);
     cudaFree(vmask);
-    cudaFree(comp);
+    cudaFree(orb_x);
+    cudaFree(orb_r);
     *this = SymOps();
 }
 
 uint64_t SymOps::bytes() const {
     if (!fp_rowptr) return 0;
     const size_t vb = val_bytes(vt);
-    return sizeof(uint64_t) * (K + 1 + J + 1) + (4 + vb) * (fp_nnz + bp_nnz) + 4 * (17 * (uint64_t)K + 2 * J) + 256;
+    return sizeof(uint64_t) * (K + 1 + J + 1) + (4 + vb) * (fp_nnz + bp_nnz) + 4 * 33 * ((uint64_t)K + J);
 }
 
 void check_symmetric_geometry(const mlem_geometry& g) {
     MLEM_REQUIRE(g.nx == g.ny, MLEM_EUNSUPPORTED, "symmetry needs a square voxel grid (nx == ny)");
     MLEM_REQUIRE(g.det_per_ring % 4 == 0, MLEM_EUNSUPPORTED, "symmetry needs a multiple of 4 detectors per ring");
     MLEM_REQUIRE(g.row_stride <= 1, MLEM_EUNSUPPORTED, "symmetry needs every LOR (row_stride 1)");
-    MLEM_REQUIRE(g.nx < 2048 && g.nz < 1024, MLEM_EUNSUPPORTED, "symmetry: voxel grid too large for packed indices");
     MLEM_REQUIRE(g.vx == g.vy, MLEM_EUNSUPPORTED, "symmetry needs square voxels in the transaxial plane");
 }
 
@@ -405,24 +425,32 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
             }
         }
     }
-    // voxel orbits
-    std::vector<uint32_t> vrow, vxyz, vmask;
+    // voxel orbits: canonical voxels (smallest index of each orbit), their 16
+    // images, and for every voxel its canonical voxel and the first
+    // transformation that produces it
+    std::vector<uint32_t> vrow, vimg, vmask, vorb(cols);
+    std::vector<uint8_t> vsym(cols);
     for (uint32_t c = 0; c < cols; ++c) {
-        uint32_t mn = c;
-        for (int t = 1; t < 16; ++t) mn = std::min(mn, M.vox_index(t, c));
-        if (mn != c) continue;
-        uint32_t msk = 0;
         uint32_t seen[16];
+        uint32_t mn = c;
+        for (int t = 0; t < 16; ++t) mn = std::min(mn, seen[t] = M.vox_index(t, c));
+        if (mn != c) continue;
+        const uint32_t j = (uint32_t)vrow.size();
+        uint32_t msk = 0;
         for (int t = 0; t < 16; ++t) {
-            seen[t] = M.vox_index(t, c);
             bool first = true;
             for (int u = 0; u < t && first; ++u) first = seen[u] != seen[t];
-            if (first) msk |= 1u << t;
+            if (first) {
+                msk |= 1u << t;
+                vorb[seen[t]] = j;
+                vsym[seen[t]] = (uint8_t)t;
+            }
+            vimg.push_back(seen[t]);
         }
         vrow.push_back(c);
-        vxyz.push_back((c % M.n) | (((c / M.n) % M.n) << 11) | ((c / (M.n * M.n)) << 22));
         vmask.push_back(msk);
     }
+    MLEM_REQUIRE(vrow.size() < (1ull << 28), MLEM_EUNSUPPORTED, "symmetry: too many canonical voxels");
 
     // canonical rows, averaged over the transformations that fix their LOR
     std::vector<uint64_t> crp;
@@ -511,21 +539,24 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
         A.max_row = max_row_length(A.rowptr, A.nrows, s);
 
         // forward-projection operand: canonical rows with packed columns
-        y.n = M.n;
-        y.nz = M.nz;
         y.K = (uint32_t)K;
         y.fp_nnz = cnnz;
         y.fp_rowptr = d_crp;
         d_crp = nullptr;
         MLEM_CUDA(cudaMalloc(&y.fp_key, sizeof(uint32_t) * std::max<uint64_t>(cnnz, 1)));
         if (cnnz) {
-            k_pack_xyz<<<grid_of(cnnz), 256, 0, s>>>(d_ccol, cnnz, M.n, y.fp_key);
+            uint32_t* d_vorb = upload(vorb);
+            uint8_t* d_vsym = upload(vsym);
+            k_sym_fp_keys<<<grid_of(cnnz), 256, 0, s>>>(d_ccol, cnnz, d_vorb, d_vsym, y.fp_key);
             MLEM_LAUNCHED();
+            MLEM_CUDA(cudaStreamSynchronize(s));
+            cudaFree(d_vorb);
+            cudaFree(d_vsym);
         }
         y.fp_val = d_cval;
         d_cval = nullptr;
         y.img = upload(img);
-        y.fp_mask = upload(mask);
+        y.mask = upload(mask);
         // back-projection operand: rows of A^T for the canonical voxels
         y.J = (uint32_t)vrow.size();
         uint32_t* d_vrow = upload(vrow);
@@ -546,14 +577,11 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
         MLEM_CUDA(cudaStreamSynchronize(s));
         cudaFree(d_vrow);
         cudaFree(blen);
-        y.vxyz = upload(vxyz);
+        y.vimg = upload(vimg);
         y.vmask = upload(vmask);
-        std::vector<uint8_t> comp_flat(256);
-        for (int a = 0; a < 16; ++a)
-            for (int b = 0; b < 16; ++b) comp_flat[16 * a + b] = comp[a][b];
-        y.comp = upload(comp_flat);
+        MLEM_CUDA(cudaMalloc(&y.orb_x, sizeof(float) * 16 * std::max<uint64_t>(y.J, 1)));
+        MLEM_CUDA(cudaMalloc(&y.orb_r, sizeof(float) * 16 * std::max<uint64_t>(y.K, 1)));
         y.vt = MLEM_VAL_F32;
-        for (int t = 0; t < 16; ++t) y.maps.m[t] = vox_map(t, (int32_t)M.n, (int32_t)M.nz);
     } catch (...) {
         cudaStreamSynchronize(s);
         cudaFree(d_crp);
