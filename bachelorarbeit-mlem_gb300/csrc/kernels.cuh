@@ -138,12 +138,12 @@ void remap_csr(const DevCsr& in, const uint32_t* row_src, const uint32_t* col_ma
 struct SymOps {
     uint32_t K = 0, J = 0;           // canonical LOR rows / canonical voxel rows
     uint64_t fp_nnz = 0, bp_nnz = 0;
-    uint64_t* fp_rowptr = nullptr;   // [K+1]
+    uint64_t* fp_rowptr = nullptr;   // [4 K + 1] row k, segment q (entries with t & 3 == q): 4 k + q
     uint32_t* fp_key = nullptr;      // [fp_nnz] canonical voxel << 4 | t
     void* fp_val = nullptr;          // [fp_nnz]
     uint32_t* img = nullptr;         // [16 K] LOR s(r_k)
     uint32_t* mask = nullptr;        // [K] transformations giving distinct LORs
-    uint64_t* bp_rowptr = nullptr;   // [J+1]
+    uint64_t* bp_rowptr = nullptr;   // [4 J + 1]
     uint32_t* bp_key = nullptr;      // [bp_nnz] canonical LOR << 4 | t
     void* bp_val = nullptr;          // [bp_nnz]
     uint32_t* vimg = nullptr;        // [16 J] voxel s(v_j)
@@ -162,7 +162,9 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
 void lower_symmetric_values(SymOps& y, mlem_value_type vt, cudaStream_t s);
 // Forward (transposed = false: Correl or Raw epilogue) or back projection
 // (true: Update or Raw) through the compact operands; natural order in and out.
-void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s);
+// unroll: entries per lane in flight (2, 4 or 8).
+void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, L2Window win,
+                cudaStream_t s);
 
 // ------------------------------------------------------------- siddon.cu
 uint64_t siddon_rows(const mlem_geometry& geo);

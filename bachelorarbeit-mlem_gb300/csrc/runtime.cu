@@ -173,8 +173,9 @@ void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o) {
                  "kernel SYM needs a matrix generated with symmetry = 1");
     MLEM_REQUIRE(o.lanes == 0 || o.lanes == 4 || o.lanes == 8 || o.lanes == 16 || o.lanes == 32, MLEM_EINVAL,
                  "lanes must be 0, 4, 8, 16 or 32");
-    MLEM_REQUIRE(o.unroll == 0 || o.unroll == 1 || o.unroll == 2 || o.unroll == 4, MLEM_EINVAL,
-                 "unroll must be 0, 1, 2 or 4");
+    MLEM_REQUIRE(o.unroll == 0 || o.unroll == 1 || o.unroll == 2 || o.unroll == 4 ||
+                     (o.unroll == 8 && o.kernel == MLEM_KERNEL_SYM),
+                 MLEM_EINVAL, "unroll must be 0, 1, 2 or 4 (or 8 with kernel SYM)");
     MLEM_REQUIRE(o.kernel != MLEM_KERNEL_PERSISTENT || (o.lanes != 4 && o.lanes != 8 && o.unroll != 4),
                  MLEM_EINVAL, "the persistent kernel takes 16 or 32 lanes and unroll 1 or 2");
     MLEM_REQUIRE(o.row_order <= 1, MLEM_EINVAL, "row_order must be 0 or 1");
@@ -216,7 +217,7 @@ static void launch_cfg(mlem_matrix* m, const DevCsr& op, const float* x, const E
     } else if (c.kind == MLEM_KERNEL_D16) {
         launch_csr_d16(op, x, e, win, s);
     } else if (c.kind == MLEM_KERNEL_SYM) {
-        launch_sym(m->sym, &op == &m->AT, x, e, win, s);
+        launch_sym(m->sym, &op == &m->AT, x, e, c.unroll, win, s);
     } else if (c.kind == MLEM_KERNEL_ILV) {
         launch_csr_ilv(op, x, e, c.unroll, win, s);
     } else if (c.kind == MLEM_KERNEL_PERSISTENT) {
@@ -250,7 +251,8 @@ static void tune_projection(mlem_matrix* m, bool transposed) {
     if (op.d16) cand.push_back(ProjCfg{MLEM_KERNEL_D16, 32, 1, 0.f});
     if (op.idx_ilv)
         for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_ILV, 32, u, 0.f});
-    if (m->sym.fp_rowptr) cand.push_back(ProjCfg{MLEM_KERNEL_SYM, 32, 1, 0.f});
+    if (m->sym.fp_rowptr)
+        for (int u : {2, 4, 8}) cand.push_back(ProjCfg{MLEM_KERNEL_SYM, 32, u, 0.f});
     prepare_csrvec_pipe(op.vt);
     prepare_csr_tma(op.vt);
     ensure_workspace(m);
@@ -339,6 +341,7 @@ void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, 
         c.unroll = 2;
     } else if (o.kernel == MLEM_KERNEL_SYM) {
         c.kind = MLEM_KERNEL_SYM;
+        c.unroll = o.unroll >= 8 ? 8 : (o.unroll == 0 || o.unroll == 4 ? 4 : 2);
     } else {
         c.kind = MLEM_KERNEL_DIRECT;
         c.lanes = o.lanes ? (int)o.lanes : pick_lanes(op.nnz, op.nrows);

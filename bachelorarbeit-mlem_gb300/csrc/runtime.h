@@ -103,12 +103,12 @@ struct BatchState {
 namespace mlem {
 // Launch configuration of a csr-vector projection.
 struct ProjCfg {
-    int kind = 0;    // mlem_kernel: DIRECT, TMA or PERSISTENT
+    int kind = 0;    // mlem_kernel: DIRECT, TMA, PERSISTENT, D16, ILV or SYM
     int lanes = 32;  // DIRECT: lanes per row
-    int unroll = 2;  // DIRECT: 4-element vectors in flight per lane
+    int unroll = 2;  // DIRECT: 4-element vectors in flight per lane; SYM: entries in flight per lane
     float ms = 0.f;  // measured time of one launch
     bool ordered = false;    // DIRECT / PERSISTENT: rows in the operand's locality order
-    bool pipelined = false;  // DIRECT: next vectors loaded before the current gathers
+    bool pipelined = false;  // DIRECT: next vectors loaded before the current gathers; SYM: next keys
 };
 }  // namespace mlem
 

@@ -26,14 +26,16 @@
 // rotations R, then the axial flip F; M R = R^-1 M, F central),
 //   s o t = F^(f_s ^ f_t) R^(q_s + (m_s ? -q_t : q_t)) M^(m_s ^ m_t),
 // so for the four s sharing (m_s, f_s) the needed values are one aligned
-// float4 of the 64-byte orbit row (chunk (m_s ^ m_t) + 2 (f_s ^ f_t)),
-// rotated by q_t or -q_t.  A warp handles one compact row: 8 entries per
-// step, 4 lanes per entry (one per (m_s, f_s)), each lane one 16-byte load
-// and 4 accumulators; the 64 bytes an entry needs come in one coalesced
-// piece.  The orbit arrays (16 floats per canonical voxel / LOR, L2-resident)
-// are gathered from the natural-order input by a small kernel before each
-// projection; each distinct output row (LOR s(r_k), voxel s(v_j)) is written
-// by the first s that produces it.
+// float4 of the 64-byte orbit row (chunk (m_s ^ m_t) + 2 (f_s ^ f_t), which
+// is (key >> 2) ^ (m_s + 2 f_s) in units of float4), rotated by q_t or -q_t.
+// The entries of a row are kept in 4 segments by q_t, so a lane adds the
+// float4 unrotated and rotates its sums once per segment.  A warp handles
+// one compact row: 8 entries per step, 4 lanes per entry (one per
+// (m_s, f_s)), each lane one 16-byte load and 4 sums; the 64 bytes an entry
+// needs come in one coalesced piece.  The orbit arrays (16 floats per
+// canonical voxel / LOR, L2-resident) are gathered from the natural-order
+// input by a small kernel before each projection; each distinct output row
+// (LOR s(r_k), voxel s(v_j)) is written by the first s that produces it.
 #include "kernels.cuh"
 
 #include <algorithm>
@@ -100,7 +102,7 @@ void composition(const SymMaps& M, uint8_t comp[16][16], uint8_t inv[16]) {
                 if (same) found = u;
             }
             MLEM_REQUIRE(found >= 0, MLEM_EINVAL, "internal: symmetry group not closed");
-            // the closed form the compact kernels use (orbit_chunk / orbit_fma)
+            // the closed form the compact kernels use (k_sym_orbit)
             const int d = ((s >> 2) & 1) ? (4 - (t & 3)) & 3 : (t & 3);
             const int closed = ((s + d) & 3) + 4 * (((s >> 2) ^ (t >> 2)) & 1) + 8 * ((s >> 3) ^ (t >> 3));
             MLEM_REQUIRE(found == closed, MLEM_EINVAL, "internal: symmetry composition differs from its closed form");
@@ -141,74 +143,111 @@ __device__ __forceinline__ float ld_val(const V* p, uint64_t e) {
     return Val4<V>::one(p, e);
 }
 
-// One entry of a compact row for the lane of group (mg, fg): the orbit row
-// float4 holding s o t for the four s = 4 (mg + 2 fg) + q.
-__device__ __forceinline__ uint32_t orbit_chunk(uint32_t kk, uint32_t mg, uint32_t fg) {
-    const uint32_t t = kk & 15u;
-    return ((kk >> 4) << 2) | ((mg ^ ((t >> 2) & 1u)) | ((fg ^ (t >> 3)) << 1));
+// cp.async.bulk.prefetch.L2 of [p, p + bytes) widened to 16-byte granules.
+__device__ __forceinline__ void l2_prefetch_range(const void* p, uint64_t bytes) {
+    const uint64_t a = reinterpret_cast<uint64_t>(p);
+    const uint64_t lo = a & ~15ull, hi = (a + bytes + 15) & ~15ull;
+    for (uint64_t q = lo; q < hi; q += 65536) {
+        const uint32_t n = (uint32_t)(hi - q < 65536 ? hi - q : 65536);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q), "r"(n) : "memory");
+    }
 }
 
-// acc[q] += v * o[(q + d) & 3], d = q_t (mg = 0) or -q_t (mg = 1)
-__device__ __forceinline__ void orbit_fma(float4 o, float v, uint32_t kk, uint32_t mg, float (&acc)[4]) {
-    const uint32_t qt = kk & 3u;
-    const uint32_t d = (mg ? (4u - qt) : qt) & 3u;
-    float r0 = o.x, r1 = o.y, r2 = o.z, r3 = o.w;
-    if (d & 1u) {
-        const float t0 = r0;
-        r0 = r1;
-        r1 = r2;
-        r2 = r3;
-        r3 = t0;
+__device__ __forceinline__ float comp4(const float4& v, int i) {
+    return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+// Segment Q of a compact row (entries with q_t = Q): unrotated sums, then
+// acc[p] += sums[(p + d) & 3] with d = Q (m_s = 0) or -Q (m_s = 1).
+template <typename V, int U, int Q>
+__device__ __forceinline__ void orbit_segment(const uint32_t* __restrict__ key, const V* __restrict__ val,
+                                              const float4* __restrict__ orb, uint64_t s0, uint64_t s1,
+                                              uint32_t slot, uint32_t lb, uint32_t mg, float (&acc)[4]) {
+    float4 sa = make_float4(0.f, 0.f, 0.f, 0.f);
+    // row-local 32-bit offsets; full steps of U entries per lane, then one
+    // predicated step
+    const uint32_t* kp = key + s0;
+    const V* vp = val + s0;
+    const uint32_t n = (uint32_t)(s1 - s0);
+    uint32_t i = slot;
+    for (; i + 8 * (U - 1) < n; i += 8 * U) {
+        uint32_t kk[U];
+        float v[U];
+        float4 o[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            kk[u] = __ldcs(kp + i + 8 * u);
+            v[u] = ld_val<V>(vp, i + 8 * u);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) o[u] = __ldg(orb + ((kk[u] >> 2) ^ lb));
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            sa.x = fmaf(v[u], o[u].x, sa.x);
+            sa.y = fmaf(v[u], o[u].y, sa.y);
+            sa.z = fmaf(v[u], o[u].z, sa.z);
+            sa.w = fmaf(v[u], o[u].w, sa.w);
+        }
     }
-    if (d & 2u) {
-        float t0 = r0;
-        r0 = r2;
-        r2 = t0;
-        t0 = r1;
-        r1 = r3;
-        r3 = t0;
+    if (i < n) {
+        uint32_t kk[U];
+        float v[U];
+        float4 o[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const bool ok = i + 8 * u < n;
+            kk[u] = ok ? __ldcs(kp + i + 8 * u) : 0u;
+            v[u] = ok ? ld_val<V>(vp, i + 8 * u) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            o[u] = (i + 8 * u < n) ? __ldg(orb + ((kk[u] >> 2) ^ lb)) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            sa.x = fmaf(v[u], o[u].x, sa.x);
+            sa.y = fmaf(v[u], o[u].y, sa.y);
+            sa.z = fmaf(v[u], o[u].z, sa.z);
+            sa.w = fmaf(v[u], o[u].w, sa.w);
+        }
     }
-    acc[0] = fmaf(v, r0, acc[0]);
-    acc[1] = fmaf(v, r1, acc[1]);
-    acc[2] = fmaf(v, r2, acc[2]);
-    acc[3] = fmaf(v, r3, acc[3]);
+    constexpr int D0 = Q, D1 = (4 - Q) & 3;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) acc[p] += mg ? comp4(sa, (p + D1) & 3) : comp4(sa, (p + D0) & 3);
 }
 
 // Compact product with epilogue: out row oimg[16 row + s] for every s with
 // bit s of omask[row].  EPI Correl / Raw (forward projection: rows are
 // canonical LORs) or Update / Raw (back projection: canonical voxels).
+// Segment q of a row holds the entries with q_t = q; lane l of an entry
+// loads chunk (key >> 2) ^ (l & 3) of the orbit row (key >> 4).  U entries
+// per lane in flight.
+// register budget per unroll: U = 2 or 4 -> 6 blocks of 256 threads per SM
+// (40 registers), 8 -> 4 (64)
+constexpr int orbit_min_blocks(int U) { return U <= 4 ? 6 : 4; }
+
 template <typename V, int EPI, int U>
-__global__ void __launch_bounds__(256)
-k_sym_orbit(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ key, const V* __restrict__ val,
+__global__ void __launch_bounds__(256, orbit_min_blocks(U))
+k_sym_orbit(const uint64_t* __restrict__ rowptr4, const uint32_t* __restrict__ key, const V* __restrict__ val,
             uint32_t nrows, const float4* __restrict__ orb, const uint32_t* __restrict__ oimg,
             const uint32_t* __restrict__ omask, const int32_t* __restrict__ g, float* __restrict__ out,
             float* __restrict__ fwproj, float* __restrict__ f, const float* __restrict__ norm) {
     const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
     if (row >= nrows) return;  // warp-uniform
-    const uint32_t mg = lane & 1u, fg = (lane >> 1) & 1u, slot = lane >> 2;
+    const uint32_t lb = lane & 3u, mg = lane & 1u, slot = lane >> 2;
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    const uint64_t s0 = rowptr[row], s1 = rowptr[row + 1];
-    uint64_t e = s0 + slot;
-    for (; e + 8 * (U - 1) < s1; e += 8 * U) {
-        uint32_t kk[U];
-        float v[U];
-        float4 o[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            kk[u] = __ldcs(key + e + 8 * u);
-            v[u] = ld_val<V>(val, e + 8 * u);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) o[u] = __ldg(orb + orbit_chunk(kk[u], mg, fg));
-#pragma unroll
-        for (int u = 0; u < U; ++u) orbit_fma(o[u], v[u], kk[u], mg, acc);
+    const uint64_t* rp = rowptr4 + 4 * (uint64_t)row;
+    const uint64_t r0 = rp[0], r1 = rp[1], r2 = rp[2], r3 = rp[3], r4 = rp[4];
+    if (lane == 0 && r4 > r0) {
+        // the row's keys and values into L2 ahead of the loads (16-byte
+        // granules; the arrays are padded by 16 elements past their end)
+        l2_prefetch_range(key + r0, (r4 - r0) * sizeof(uint32_t));
+        l2_prefetch_range(val + r0, (r4 - r0) * sizeof(V));
     }
-    for (; e < s1; e += 8) {
-        const uint32_t kk = __ldcs(key + e);
-        const float v = ld_val<V>(val, e);
-        orbit_fma(__ldg(orb + orbit_chunk(kk, mg, fg)), v, kk, mg, acc);
-    }
+    orbit_segment<V, U, 0>(key, val, orb, r0, r1, slot, lb, mg, acc);
+    orbit_segment<V, U, 1>(key, val, orb, r1, r2, slot, lb, mg, acc);
+    orbit_segment<V, U, 2>(key, val, orb, r2, r3, slot, lb, mg, acc);
+    orbit_segment<V, U, 3>(key, val, orb, r3, r4, slot, lb, mg, acc);
 #pragma unroll
     for (int o = 4; o < 32; o <<= 1)
 #pragma unroll
@@ -270,38 +309,69 @@ __global__ void k_sym_expand(const uint64_t* __restrict__ crp, const uint32_t* _
     }
 }
 
-// Columns of the canonical rows as canonical voxel << 4 | transformation.
-__global__ void k_sym_fp_keys(const uint32_t* __restrict__ col, uint64_t nnz, const uint32_t* __restrict__ vorb,
-                              const uint8_t* __restrict__ vsym, uint32_t* __restrict__ key) {
-    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nnz; e += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t c = col[e];
-        key[e] = (vorb[c] << 4) | vsym[c];
+// Compact operands from CSR rows (row j of the output = input row rowsel[j],
+// or j without a selection): an entry with column c becomes
+// orb_of[c] << 4 | sym[c], and every output row is split into 4 segments by
+// the rotation class sym[c] & 3 (stable inside a segment).  One warp per row.
+__global__ void k_seg_counts(const uint64_t* __restrict__ rp, const uint32_t* __restrict__ idx,
+                             const uint32_t* __restrict__ rowsel, uint32_t nrows, const uint8_t* __restrict__ sym,
+                             uint32_t* __restrict__ counts) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint64_t j = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; j < nrows;
+         j += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+        const uint32_t r = rowsel ? rowsel[j] : (uint32_t)j;
+        uint32_t c[4] = {0, 0, 0, 0};
+        for (uint64_t e = rp[r] + lane; e < rp[r + 1]; e += 32) {
+            const uint32_t q = sym[idx[e]] & 3u;
+            c[0] += q == 0;
+            c[1] += q == 1;
+            c[2] += q == 2;
+            c[3] += q == 3;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) c[q] += __shfl_xor_sync(0xffffffffu, c[q], o);
+        if (lane < 4) counts[4 * j + lane] = c[0] * (lane == 0) + c[1] * (lane == 1) + c[2] * (lane == 2) + c[3] * (lane == 3);
     }
 }
 
-// Rows of A^T for the canonical voxels, entries r' -> can_row[r'] << 4 | sym_of[r'].
-__global__ void k_sym_bp_lens(const uint64_t* __restrict__ trp, const uint32_t* __restrict__ vrow, uint32_t J,
-                              uint32_t* __restrict__ len) {
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < J; j += gridDim.x * blockDim.x)
-        len[j] = (uint32_t)(trp[vrow[j] + 1] - trp[vrow[j]]);
-}
-
-__global__ void k_sym_bp_fill(const uint64_t* __restrict__ trp, const uint32_t* __restrict__ tidx,
-                              const float* __restrict__ tval, const uint32_t* __restrict__ vrow, uint32_t J,
-                              const uint32_t* __restrict__ can_row, const uint8_t* __restrict__ sym_of,
-                              const uint64_t* __restrict__ brp, uint32_t* __restrict__ bkey,
-                              float* __restrict__ bval) {
-    const uint32_t lane = threadIdx.x & 31;
-    for (uint64_t j = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; j < J;
+__global__ void k_seg_fill(const uint64_t* __restrict__ rp, const uint32_t* __restrict__ idx,
+                           const float* __restrict__ val, const uint32_t* __restrict__ rowsel, uint32_t nrows,
+                           const uint32_t* __restrict__ orb_of, const uint8_t* __restrict__ sym,
+                           const uint64_t* __restrict__ orp, uint32_t* __restrict__ okey, float* __restrict__ oval) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint64_t j = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; j < nrows;
          j += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
-        const uint64_t s = trp[vrow[j]], len = trp[vrow[j] + 1] - s, o = brp[j];
-        for (uint64_t t = lane; t < len; t += 32) {
-            const uint32_t r = tidx[s + t];
-            bkey[o + t] = (can_row[r] << 4) | sym_of[r];
-            bval[o + t] = tval[s + t];
+        const uint32_t r = rowsel ? rowsel[j] : (uint32_t)j;
+        const uint64_t s0 = rp[r], s1 = rp[r + 1];
+        for (uint32_t q = 0; q < 4; ++q) {
+            uint64_t o = orp[4 * j + q];
+            for (uint64_t base = s0; base < s1; base += 32) {
+                const uint64_t e = base + lane;
+                uint32_t c = 0, t = 0;
+                bool take = false;
+                if (e < s1) {
+                    c = idx[e];
+                    t = sym[c];
+                    take = (t & 3u) == q;
+                }
+                const uint32_t b = __ballot_sync(0xffffffffu, take);
+                if (take) {
+                    const uint64_t pos = o + __popc(b & ((1u << lane) - 1u));
+                    okey[pos] = (orb_of[c] << 4) | t;
+                    oval[pos] = val[e];
+                }
+                o += __popc(b);
+            }
         }
     }
 }
+
+// Builds one compact operand (segmented row pointers [4 nrows + 1], keys, FP32 values).
+void build_segmented(const uint64_t* rp, const uint32_t* idx, const float* val, const uint32_t* rowsel, uint32_t nrows,
+                     const uint32_t* orb_of, const uint8_t* sym, uint64_t*& orp, uint32_t*& okey, void*& oval,
+                     uint64_t& onnz, cudaStream_t s);
 
 unsigned grid_of(uint64_t n) { return std::max(1u, std::min<unsigned>(ceil_div_u(n, 256), 152u * 32u)); }
 
@@ -313,9 +383,34 @@ T* upload(const std::vector<T>& h, size_t min_elems = 1) {
     return d;
 }
 
-constexpr int kOrbitUnroll = 4;
+void build_segmented(const uint64_t* rp, const uint32_t* idx, const float* val, const uint32_t* rowsel, uint32_t nrows,
+                     const uint32_t* orb_of, const uint8_t* sym, uint64_t*& orp, uint32_t*& okey, void*& oval,
+                     uint64_t& onnz, cudaStream_t s) {
+    const uint64_t nseg = 4ull * nrows;
+    uint32_t* counts = nullptr;
+    MLEM_CUDA(cudaMalloc(&counts, sizeof(uint32_t) * std::max<uint64_t>(nseg, 1)));
+    try {
+        MLEM_CUDA(cudaMalloc(&orp, sizeof(uint64_t) * (nseg + 1)));
+        k_seg_counts<<<grid_of((uint64_t)nrows * 32), 256, 0, s>>>(rp, idx, rowsel, nrows, sym, counts);
+        MLEM_LAUNCHED();
+        scan_counts_u64(counts, orp, nseg, s);
+        MLEM_CUDA(cudaMemcpyAsync(&onnz, orp + nseg, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        // 16 elements of padding: the kernels prefetch whole 16-byte granules
+        MLEM_CUDA(cudaMalloc(&okey, sizeof(uint32_t) * (onnz + 16)));
+        MLEM_CUDA(cudaMalloc(&oval, sizeof(float) * (onnz + 16)));
+        k_seg_fill<<<grid_of((uint64_t)nrows * 32), 256, 0, s>>>(rp, idx, val, rowsel, nrows, orb_of, sym, orp, okey,
+                                                                   static_cast<float*>(oval));
+        MLEM_LAUNCHED();
+        MLEM_CUDA(cudaStreamSynchronize(s));
+    } catch (...) {
+        cudaFree(counts);
+        throw;
+    }
+    cudaFree(counts);
+}
 
-template <typename V, int EPI>
+template <typename V, int EPI, int U>
 void orbit_launch(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
     const uint32_t rows = transposed ? y.J : y.K;
     float* orb = transposed ? y.orb_r : y.orb_x;
@@ -323,20 +418,29 @@ void orbit_launch(const SymOps& y, bool transposed, const float* x, const EpiArg
     const uint64_t n_orb = 16ull * (transposed ? y.K : y.J);
     k_orbit_gather<<<grid_of(n_orb), 256, 0, s>>>(orb, x, table, n_orb);
     MLEM_LAUNCHED();
-    launch_ex(k_sym_orbit<V, EPI, kOrbitUnroll>, dim3(ceil_div_u((uint64_t)rows * 32, 256)), dim3(256), 0, s, win,
+    launch_ex(k_sym_orbit<V, EPI, U>, dim3(ceil_div_u((uint64_t)rows * 32, 256)), dim3(256), 0, s, win,
               transposed ? y.bp_rowptr : y.fp_rowptr, transposed ? y.bp_key : y.fp_key,
               static_cast<const V*>(transposed ? y.bp_val : y.fp_val), rows, reinterpret_cast<const float4*>(orb),
               transposed ? y.vimg : y.img, transposed ? y.vmask : y.mask, e.g, e.out, e.fwproj, e.f, e.norm);
 }
 
+template <typename V, int EPI>
+void orbit_variant(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, L2Window win,
+                   cudaStream_t s) {
+    if (unroll >= 8) orbit_launch<V, EPI, 8>(y, transposed, x, e, win, s);
+    else if (unroll >= 4) orbit_launch<V, EPI, 4>(y, transposed, x, e, win, s);
+    else orbit_launch<V, EPI, 2>(y, transposed, x, e, win, s);
+}
+
 template <typename V>
-void sym_dispatch(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+void sym_dispatch(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, L2Window win,
+                  cudaStream_t s) {
     if (!transposed) {
-        if (e.kind == Epi::Correl) orbit_launch<V, (int)Epi::Correl>(y, false, x, e, win, s);
-        else orbit_launch<V, (int)Epi::Raw>(y, false, x, e, win, s);
+        if (e.kind == Epi::Correl) orbit_variant<V, (int)Epi::Correl>(y, false, x, e, unroll, win, s);
+        else orbit_variant<V, (int)Epi::Raw>(y, false, x, e, unroll, win, s);
     } else {
-        if (e.kind == Epi::Update) orbit_launch<V, (int)Epi::Update>(y, true, x, e, win, s);
-        else orbit_launch<V, (int)Epi::Raw>(y, true, x, e, win, s);
+        if (e.kind == Epi::Update) orbit_variant<V, (int)Epi::Update>(y, true, x, e, unroll, win, s);
+        else orbit_variant<V, (int)Epi::Raw>(y, true, x, e, unroll, win, s);
     }
 }
 
@@ -361,7 +465,7 @@ void SymOps::release() {
 uint64_t SymOps::bytes() const {
     if (!fp_rowptr) return 0;
     const size_t vb = val_bytes(vt);
-    return sizeof(uint64_t) * (K + 1 + J + 1) + (4 + vb) * (fp_nnz + bp_nnz) + 4 * 33 * ((uint64_t)K + J);
+    return sizeof(uint64_t) * (4 * ((uint64_t)K + J) + 2) + (4 + vb) * (fp_nnz + bp_nnz) + 4 * 33 * ((uint64_t)K + J);
 }
 
 void check_symmetric_geometry(const mlem_geometry& g) {
@@ -538,45 +642,37 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
         transpose_device(AT, A, s);  // A^, columns ascending in every row
         A.max_row = max_row_length(A.rowptr, A.nrows, s);
 
-        // forward-projection operand: canonical rows with packed columns
+        // forward-projection operand: the canonical rows, columns as canonical voxel << 4 | t
         y.K = (uint32_t)K;
-        y.fp_nnz = cnnz;
-        y.fp_rowptr = d_crp;
-        d_crp = nullptr;
-        MLEM_CUDA(cudaMalloc(&y.fp_key, sizeof(uint32_t) * std::max<uint64_t>(cnnz, 1)));
-        if (cnnz) {
+        y.J = (uint32_t)vrow.size();
+        {
             uint32_t* d_vorb = upload(vorb);
             uint8_t* d_vsym = upload(vsym);
-            k_sym_fp_keys<<<grid_of(cnnz), 256, 0, s>>>(d_ccol, cnnz, d_vorb, d_vsym, y.fp_key);
-            MLEM_LAUNCHED();
-            MLEM_CUDA(cudaStreamSynchronize(s));
+            try {
+                build_segmented(d_crp, d_ccol, d_cval, nullptr, y.K, d_vorb, d_vsym, y.fp_rowptr, y.fp_key, y.fp_val,
+                                y.fp_nnz, s);
+            } catch (...) {
+                cudaFree(d_vorb);
+                cudaFree(d_vsym);
+                throw;
+            }
             cudaFree(d_vorb);
             cudaFree(d_vsym);
         }
-        y.fp_val = d_cval;
-        d_cval = nullptr;
         y.img = upload(img);
         y.mask = upload(mask);
-        // back-projection operand: rows of A^T for the canonical voxels
-        y.J = (uint32_t)vrow.size();
-        uint32_t* d_vrow = upload(vrow);
-        uint32_t* blen = nullptr;
-        MLEM_CUDA(cudaMalloc(&blen, sizeof(uint32_t) * std::max<uint32_t>(y.J, 1)));
-        MLEM_CUDA(cudaMalloc(&y.bp_rowptr, sizeof(uint64_t) * ((uint64_t)y.J + 1)));
-        k_sym_bp_lens<<<grid_of(y.J), 256, 0, s>>>(AT.rowptr, d_vrow, y.J, blen);
-        MLEM_LAUNCHED();
-        scan_counts_u64(blen, y.bp_rowptr, y.J, s);
-        MLEM_CUDA(cudaMemcpyAsync(&y.bp_nnz, y.bp_rowptr + y.J, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-        MLEM_CUDA(cudaStreamSynchronize(s));
-        MLEM_CUDA(cudaMalloc(&y.bp_key, sizeof(uint32_t) * std::max<uint64_t>(y.bp_nnz, 1)));
-        MLEM_CUDA(cudaMalloc(&y.bp_val, sizeof(float) * std::max<uint64_t>(y.bp_nnz, 1)));
-        k_sym_bp_fill<<<grid_of((uint64_t)y.J * 32), 256, 0, s>>>(AT.rowptr, AT.idx, static_cast<const float*>(AT.val),
-                                                                   d_vrow, y.J, d_can, d_sym, y.bp_rowptr, y.bp_key,
-                                                                   static_cast<float*>(y.bp_val));
-        MLEM_LAUNCHED();
-        MLEM_CUDA(cudaStreamSynchronize(s));
-        cudaFree(d_vrow);
-        cudaFree(blen);
+        // back-projection operand: rows of A^T for the canonical voxels, LORs as canonical row << 4 | t
+        {
+            uint32_t* d_vrow = upload(vrow);
+            try {
+                build_segmented(AT.rowptr, AT.idx, static_cast<const float*>(AT.val), d_vrow, y.J, d_can, d_sym,
+                                y.bp_rowptr, y.bp_key, y.bp_val, y.bp_nnz, s);
+            } catch (...) {
+                cudaFree(d_vrow);
+                throw;
+            }
+            cudaFree(d_vrow);
+        }
         y.vimg = upload(vimg);
         y.vmask = upload(vmask);
         MLEM_CUDA(cudaMalloc(&y.orb_x, sizeof(float) * 16 * std::max<uint64_t>(y.J, 1)));
@@ -595,7 +691,9 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
         cudaFree(R.val);
         throw;
     }
+    cudaFree(d_crp);
     cudaFree(d_ccol);
+    cudaFree(d_cval);
     cudaFree(d_can);
     cudaFree(d_sym);
     cudaFree(len);
@@ -605,7 +703,7 @@ void lower_symmetric_values(SymOps& y, mlem_value_type vt, cudaStream_t s) {
     if (vt == MLEM_VAL_F32 || !y.fp_rowptr) return;
     auto lower = [&](void*& v, uint64_t n) {
         void* nv = nullptr;
-        MLEM_CUDA(cudaMalloc(&nv, 2 * std::max<uint64_t>(n, 1)));
+        MLEM_CUDA(cudaMalloc(&nv, 2 * (n + 16)));
         convert_values(static_cast<const float*>(v), nv, vt, n, s);
         MLEM_CUDA(cudaStreamSynchronize(s));
         cudaFree(v);
@@ -616,12 +714,13 @@ void lower_symmetric_values(SymOps& y, mlem_value_type vt, cudaStream_t s) {
     y.vt = vt;
 }
 
-void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, L2Window win,
+                cudaStream_t s) {
     MLEM_REQUIRE(y.fp_rowptr != nullptr, MLEM_EINVAL, "matrix has no symmetry operands");
     switch (y.vt) {
-        case MLEM_VAL_F32: sym_dispatch<float>(y, transposed, x, e, win, s); break;
-        case MLEM_VAL_F16: sym_dispatch<__half>(y, transposed, x, e, win, s); break;
-        default: sym_dispatch<__nv_bfloat16>(y, transposed, x, e, win, s);
+        case MLEM_VAL_F32: sym_dispatch<float>(y, transposed, x, e, unroll, win, s); break;
+        case MLEM_VAL_F16: sym_dispatch<__half>(y, transposed, x, e, unroll, win, s); break;
+        default: sym_dispatch<__nv_bfloat16>(y, transposed, x, e, unroll, win, s);
     }
 }
 

@@ -167,7 +167,8 @@ typedef struct {
     uint32_t lanes;             /* DIRECT / PERSISTENT / ORDERED: lanes per row (4, 8, 16, 32;
                                    PERSISTENT 16 or 32); 0 = chosen from the mean row length */
     uint32_t unroll;            /* same kernels: vectors of 4 elements in flight per lane
-                                   (1, 2, 4; PERSISTENT 1 or 2); 0 = 2 */
+                                   (1, 2, 4; PERSISTENT 1 or 2); 0 = 2.  SYM: entries in flight
+                                   per lane, 2 (1, 2), 4 (0, 4) or 8 */
     uint32_t row_order;         /* DIRECT / PERSISTENT with 16 or 32 lanes: 1 = process the rows in
                                    the locality order of a generated matrix */
     uint32_t pipeline;          /* DIRECT / ORDERED with 16 or 32 lanes: 1 = load a row's next vectors
