@@ -29,6 +29,11 @@ struct EpiArgs {
     float* fwproj = nullptr;      // Correl: optional copy of the projection
     float* f = nullptr;           // Update: image, updated in place
     const float* norm = nullptr;  // Update
+    // symmetry-compressed kernels only: also write the results in orbit
+    // order (Correl: ratio into SymOps::orb_r; Update: image into orb_x), and
+    // take the input's orbit array as current instead of gathering it
+    float* orbit_out = nullptr;
+    bool orbit_ready = false;
 };
 
 // Rows of `op` times x, one group of `lanes` (4/8/16/32) threads per row,
@@ -162,6 +167,8 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
 void lower_symmetric_values(SymOps& y, mlem_value_type vt, cudaStream_t s);
 // Forward (transposed = false: Correl or Raw epilogue) or back projection
 // (true: Update or Raw) through the compact operands; natural order in and out.
+// Refills the image orbit array from f (natural order).
+void sym_gather_image(const SymOps& y, const float* f, cudaStream_t s);
 // unroll: entries per lane in flight (2, 4 or 8).
 void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, L2Window win,
                 cudaStream_t s);

@@ -307,13 +307,9 @@ void prepare_kernel(mlem_matrix* m, const mlem_run_opts& o) {
     }
 }
 
-void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, const mlem_run_opts& o,
-             L2Window win, cudaStream_t s) {
+// The csr-vector configuration a projection of A (or Aᵀ) uses under opts o.
+static ProjCfg resolve_cfg(const mlem_matrix* m, bool transposed, const mlem_run_opts& o) {
     const DevCsr& op = transposed ? m->AT : m->A;
-    if (o.spmv == MLEM_SPMV_MERGE) {
-        launch_merge_spmv(op, merge_plan(m, transposed, transposed ? o.secsize_bp : o.secsize_fp), x, e, win, s);
-        return;
-    }
     ProjCfg c;
     if (o.kernel == MLEM_KERNEL_AUTO) {
         MLEM_REQUIRE(m->tuned[transposed], MLEM_EINVAL, "internal: projection used before autotuning");
@@ -349,7 +345,24 @@ void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, 
         c.ordered = o.row_order && op.order && c.lanes >= 16;
         c.pipelined = o.pipeline && c.lanes >= 16;
     }
-    launch_cfg(m, op, x, e, c, win, s);
+    return c;
+}
+
+void project(mlem_matrix* m, bool transposed, const float* x, const EpiArgs& e, const mlem_run_opts& o,
+             L2Window win, cudaStream_t s) {
+    const DevCsr& op = transposed ? m->AT : m->A;
+    if (o.spmv == MLEM_SPMV_MERGE) {
+        launch_merge_spmv(op, merge_plan(m, transposed, transposed ? o.secsize_bp : o.secsize_fp), x, e, win, s);
+        return;
+    }
+    launch_cfg(m, op, x, e, resolve_cfg(m, transposed, o), win, s);
+}
+
+// Both projections of an MLEM iteration run the symmetry-compressed kernels:
+// they then hand each other their outputs in orbit order.
+static bool sym_pair(const mlem_matrix* m, const mlem_run_opts& o) {
+    return m->sym.fp_rowptr && o.spmv == MLEM_SPMV_CSR_VECTOR && o.bp_mode == MLEM_BP_TRANS &&
+           resolve_cfg(m, false, o).kind == MLEM_KERNEL_SYM && resolve_cfg(m, true, o).kind == MLEM_KERNEL_SYM;
 }
 
 // One MLEM iteration on stream s using the matrix workspace.
@@ -378,7 +391,8 @@ StageTimer::~StageTimer() {
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
 }
 
-void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, double* ll_slot, StageTimer* timer) {
+void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, double* ll_slot, StageTimer* timer,
+                       bool sym_fused) {
     Workspace& w = m->ws;
     const DevCsr& A = m->A;
     const bool want_ll = ll_slot != nullptr;
@@ -402,6 +416,10 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
         fe.g = w.g;
         fe.out = w.ratio;
         fe.fwproj = want_ll ? w.fwproj : nullptr;
+        if (sym_fused) {
+            fe.orbit_out = m->sym.orb_r;
+            fe.orbit_ready = true;
+        }
         if (timer) timer->record(s);
         project(m, false, w.f, fe, o, wf, s);
         if (timer) {
@@ -413,6 +431,10 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
             be.kind = Epi::Update;
             be.f = w.f;
             be.norm = m->norm;
+            if (sym_fused) {
+                be.orbit_out = m->sym.orb_x;
+                be.orbit_ready = true;
+            }
             project(m, true, w.ratio, be, o, wr, s);
         } else {
             launch_scatter(A, w.ratio, w.bp, pick_lanes(A.nnz, A.nrows), wr, s);
@@ -452,10 +474,15 @@ static void enable_l2_persisting(int dev) {
 // Runs `iters` iterations on the workspace (g and f already in place).
 static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
                      double* ll_dev, StageTimer* timer = nullptr) {
+    // symmetry-compressed pair: the image orbit array is gathered once, then
+    // every back projection refreshes it and every forward projection the
+    // ratio's
+    const bool fused = iters > 0 && sym_pair(m, o);
+    if (fused) sym_gather_image(m->sym, m->ws.f, s);
     if (o.loglik_every > 0 || !o.use_graph || timer) {
         for (uint32_t it = 0; it < iters; ++it) {
             double* slot = (o.loglik_every > 0 && it % o.loglik_every == 0) ? ll_dev + it : nullptr;
-            enqueue_iteration(m, o, s, slot, timer);
+            enqueue_iteration(m, o, s, slot, timer, fused);
         }
         return;
     }
@@ -476,7 +503,7 @@ static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cud
         const uint64_t l0 = g_launches.load();
         MLEM_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
         try {
-            for (uint32_t q = 0; q < chunk; ++q) enqueue_iteration(m, o, cs, nullptr);
+            for (uint32_t q = 0; q < chunk; ++q) enqueue_iteration(m, o, cs, nullptr, nullptr, fused);
         } catch (...) {
             cudaStreamEndCapture(cs, &graph);
             if (graph) cudaGraphDestroy(graph);

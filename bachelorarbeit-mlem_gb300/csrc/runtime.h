@@ -147,8 +147,10 @@ struct StageTimer {
     void means(double& fp_ms, double& bp_ms) const;
     ~StageTimer();
 };
+// sym_fused: both projections symmetry-compressed, the image orbit array
+// current on entry (they exchange their outputs in orbit order)
 void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, double* ll_slot,
-                       StageTimer* timer = nullptr);
+                       StageTimer* timer = nullptr, bool sym_fused = false);
 void enqueue_batch_iteration(mlem_matrix* m, BatchState& b, cudaStream_t s);
 float reference_initial_value(const mlem_matrix* m, const int32_t* g);
 void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o);

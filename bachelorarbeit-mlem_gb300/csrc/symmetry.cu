@@ -230,7 +230,8 @@ __global__ void __launch_bounds__(256, orbit_min_blocks(U))
 k_sym_orbit(const uint64_t* __restrict__ rowptr4, const uint32_t* __restrict__ key, const V* __restrict__ val,
             uint32_t nrows, const float4* __restrict__ orb, const uint32_t* __restrict__ oimg,
             const uint32_t* __restrict__ omask, const int32_t* __restrict__ g, float* __restrict__ out,
-            float* __restrict__ fwproj, float* __restrict__ f, const float* __restrict__ norm) {
+            float* __restrict__ fwproj, float* __restrict__ f, const float* __restrict__ norm,
+            float* __restrict__ orbit_out) {
     const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
     if (row >= nrows) return;  // warp-uniform
@@ -257,18 +258,30 @@ k_sym_orbit(const uint64_t* __restrict__ rowptr4, const uint32_t* __restrict__ k
     const float b0 = __shfl_sync(0xffffffffu, acc[0], src), b1 = __shfl_sync(0xffffffffu, acc[1], src);
     const float b2 = __shfl_sync(0xffffffffu, acc[2], src), b3 = __shfl_sync(0xffffffffu, acc[3], src);
     const float mine = q == 0 ? b0 : (q == 1 ? b1 : (q == 2 ? b2 : b3));
-    if (lane < 16 && ((omask[row] >> lane) & 1u)) {
-        const uint32_t r = oimg[16 * (uint64_t)row + lane];
+    const uint32_t r = lane < 16 ? oimg[16 * (uint64_t)row + lane] : 0u;
+    const bool writer = lane < 16 && ((omask[row] >> lane) & 1u);
+    float res = mine;
+    if (writer) {
         if (EPI == (int)Epi::Correl) {
-            out[r] = (mine != 0.0f) ? __fdiv_rn((float)g[r], mine) : 0.0f;
+            res = (mine != 0.0f) ? __fdiv_rn((float)g[r], mine) : 0.0f;
+            out[r] = res;
             if (fwproj) fwproj[r] = mine;
         } else if (EPI == (int)Epi::Update) {
             const float tt = __fmul_rn(f[r], mine);
             const float nn = norm[r];
-            f[r] = (nn == 0.0f) ? tt : __fdiv_rn(tt, nn);
+            res = (nn == 0.0f) ? tt : __fdiv_rn(tt, nn);
+            f[r] = res;
         } else {
-            out[r] = mine;
+            out[r] = res;
         }
+    }
+    if (orbit_out) {
+        // every s gets the value written for its output row (by the first s
+        // with that row), so the orbit array equals a gather of the output
+        const unsigned long long id = lane < 16 ? (unsigned long long)r : (1ull << 32) | lane;
+        const uint32_t leader = __ffs(__match_any_sync(0xffffffffu, id)) - 1;
+        const float v = __shfl_sync(0xffffffffu, res, leader);
+        if (lane < 16) orbit_out[16 * (uint64_t)row + lane] = v;
     }
 }
 
@@ -416,12 +429,15 @@ void orbit_launch(const SymOps& y, bool transposed, const float* x, const EpiArg
     float* orb = transposed ? y.orb_r : y.orb_x;
     const uint32_t* table = transposed ? y.img : y.vimg;  // input orbits: LORs for BP, voxels for FP
     const uint64_t n_orb = 16ull * (transposed ? y.K : y.J);
-    k_orbit_gather<<<grid_of(n_orb), 256, 0, s>>>(orb, x, table, n_orb);
-    MLEM_LAUNCHED();
+    if (!e.orbit_ready) {
+        k_orbit_gather<<<grid_of(n_orb), 256, 0, s>>>(orb, x, table, n_orb);
+        MLEM_LAUNCHED();
+    }
     launch_ex(k_sym_orbit<V, EPI, U>, dim3(ceil_div_u((uint64_t)rows * 32, 256)), dim3(256), 0, s, win,
               transposed ? y.bp_rowptr : y.fp_rowptr, transposed ? y.bp_key : y.fp_key,
               static_cast<const V*>(transposed ? y.bp_val : y.fp_val), rows, reinterpret_cast<const float4*>(orb),
-              transposed ? y.vimg : y.img, transposed ? y.vmask : y.mask, e.g, e.out, e.fwproj, e.f, e.norm);
+              transposed ? y.vimg : y.img, transposed ? y.vmask : y.mask, e.g, e.out, e.fwproj, e.f, e.norm,
+              e.orbit_out);
 }
 
 template <typename V, int EPI>
@@ -712,6 +728,13 @@ void lower_symmetric_values(SymOps& y, mlem_value_type vt, cudaStream_t s) {
     lower(y.fp_val, y.fp_nnz);
     lower(y.bp_val, y.bp_nnz);
     y.vt = vt;
+}
+
+void sym_gather_image(const SymOps& y, const float* f, cudaStream_t s) {
+    MLEM_REQUIRE(y.fp_rowptr != nullptr, MLEM_EINVAL, "matrix has no symmetry operands");
+    const uint64_t n = 16ull * y.J;
+    k_orbit_gather<<<grid_of(n), 256, 0, s>>>(y.orb_x, f, y.vimg, n);
+    MLEM_LAUNCHED();
 }
 
 void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, L2Window win,
