@@ -34,6 +34,11 @@ struct EpiArgs {
     // take the input's orbit array as current instead of gathering it
     float* orbit_out = nullptr;
     bool orbit_ready = false;
+    // ... and, inside an MLEM loop of two such projections, keep everything in
+    // orbit order: g (Correl), the image and the sensitivity (Update) are read
+    // from their orbit arrays and no natural-order output is written (fwproj
+    // excepted)
+    bool orbit_only = false;
 };
 
 // Rows of `op` times x, one group of `lanes` (4/8/16/32) threads per row,
@@ -147,14 +152,16 @@ struct SymOps {
     uint32_t* fp_key = nullptr;      // [fp_nnz] canonical voxel << 4 | t
     void* fp_val = nullptr;          // [fp_nnz]
     uint32_t* img = nullptr;         // [16 K] LOR s(r_k)
-    uint32_t* mask = nullptr;        // [K] transformations giving distinct LORs
+    uint64_t* lead = nullptr;        // [K] 4 bits per s: first transformation with the same LOR
     uint64_t* bp_rowptr = nullptr;   // [4 J + 1]
     uint32_t* bp_key = nullptr;      // [bp_nnz] canonical LOR << 4 | t
     void* bp_val = nullptr;          // [bp_nnz]
     uint32_t* vimg = nullptr;        // [16 J] voxel s(v_j)
-    uint32_t* vmask = nullptr;       // [J] transformations giving distinct voxels
+    uint64_t* vlead = nullptr;       // [J] 4 bits per s: first transformation with the same voxel
     float* orb_x = nullptr;          // [16 J] image in orbit order (forward projection input)
     float* orb_r = nullptr;          // [16 K] ratio in orbit order (back projection input)
+    float* norm_orb = nullptr;       // [16 J] sensitivity image in orbit order
+    int32_t* g_orb = nullptr;        // [16 K] sinogram of the running reconstruction in orbit order
     mlem_value_type vt = MLEM_VAL_F32;
     void release();
     uint64_t bytes() const;
@@ -167,8 +174,13 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
 void lower_symmetric_values(SymOps& y, mlem_value_type vt, cudaStream_t s);
 // Forward (transposed = false: Correl or Raw epilogue) or back projection
 // (true: Update or Raw) through the compact operands; natural order in and out.
-// Refills the image orbit array from f (natural order).
+// Orbit arrays of the sensitivity image (once per matrix), of the image and
+// of the sinogram (at the start of an MLEM loop), and the image back in
+// natural order (at its end).
+void sym_set_norm(SymOps& y, const float* norm, cudaStream_t s);
 void sym_gather_image(const SymOps& y, const float* f, cudaStream_t s);
+void sym_gather_sinogram(const SymOps& y, const int32_t* g, cudaStream_t s);
+void sym_scatter_image(const SymOps& y, float* f, cudaStream_t s);
 // unroll: entries per lane in flight (2, 4 or 8).
 void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, L2Window win,
                 cudaStream_t s);

@@ -419,6 +419,7 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
         if (sym_fused) {
             fe.orbit_out = m->sym.orb_r;
             fe.orbit_ready = true;
+            fe.orbit_only = true;
         }
         if (timer) timer->record(s);
         project(m, false, w.f, fe, o, wf, s);
@@ -434,6 +435,7 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
             if (sym_fused) {
                 be.orbit_out = m->sym.orb_x;
                 be.orbit_ready = true;
+                be.orbit_only = true;
             }
             project(m, true, w.ratio, be, o, wr, s);
         } else {
@@ -471,14 +473,26 @@ static void enable_l2_persisting(int dev) {
     cudaGetLastError();
 }
 
+static void run_iterations(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
+                           double* ll_dev, StageTimer* timer, bool fused);
+
 // Runs `iters` iterations on the workspace (g and f already in place).
 static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
                      double* ll_dev, StageTimer* timer = nullptr) {
-    // symmetry-compressed pair: the image orbit array is gathered once, then
-    // every back projection refreshes it and every forward projection the
-    // ratio's
+    // symmetry-compressed pair: the image and the sinogram are gathered into
+    // orbit order once, the iterations stay in orbit order, and the image is
+    // scattered back into natural order at the end
     const bool fused = iters > 0 && sym_pair(m, o);
-    if (fused) sym_gather_image(m->sym, m->ws.f, s);
+    if (fused) {
+        sym_gather_image(m->sym, m->ws.f, s);
+        sym_gather_sinogram(m->sym, m->ws.g, s);
+    }
+    run_iterations(m, o, iters, s, ll_dev, timer, fused);
+    if (fused) sym_scatter_image(m->sym, m->ws.f, s);
+}
+
+static void run_iterations(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
+                           double* ll_dev, StageTimer* timer, bool fused) {
     if (o.loglik_every > 0 || !o.use_graph || timer) {
         for (uint32_t it = 0; it < iters; ++it) {
             double* slot = (o.loglik_every > 0 && it % o.loglik_every == 0) ? ll_dev + it : nullptr;
@@ -820,6 +834,8 @@ mlem_status mlem_matrix_generate(const mlem_geometry* geo, const mlem_matrix_opt
                 m->has_t = true;
                 postprocess_matrix(m, o);
                 lower_symmetric_values(m->sym, o.value_type, m->stream);
+                sym_set_norm(m->sym, m->norm, m->stream);
+                MLEM_CUDA(cudaStreamSynchronize(m->stream));
             } else {
                 siddon_generate_device(*geo, m->A, m->stream);
                 MLEM_REQUIRE(m->A.nrows >= 1, MLEM_EINVAL, "geometry produced no rows");

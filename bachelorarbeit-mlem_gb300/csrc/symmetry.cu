@@ -215,23 +215,28 @@ __device__ __forceinline__ void orbit_segment(const uint32_t* __restrict__ key, 
     for (int p = 0; p < 4; ++p) acc[p] += mg ? comp4(sa, (p + D1) & 3) : comp4(sa, (p + D0) & 3);
 }
 
-// Compact product with epilogue: out row oimg[16 row + s] for every s with
-// bit s of omask[row].  EPI Correl / Raw (forward projection: rows are
+// Compact product with epilogue: out row oimg[16 row + s] for every s that
+// is its own leader in olead[row] (4 bits per s: the first transformation
+// with the same output row).  EPI Correl / Raw (forward projection: rows are
 // canonical LORs) or Update / Raw (back projection: canonical voxels).
 // Segment q of a row holds the entries with q_t = q; lane l of an entry
 // loads chunk (key >> 2) ^ (l & 3) of the orbit row (key >> 4).  U entries
 // per lane in flight.
-// register budget per unroll: U = 2 or 4 -> 6 blocks of 256 threads per SM
-// (40 registers), 8 -> 4 (64)
-constexpr int orbit_min_blocks(int U) { return U <= 4 ? 6 : 4; }
+// Blocks of 2 warps (rows differ in length; a small block frees its slot
+// early).  Register budget per unroll: U = 2 or 4 -> 24 blocks per SM
+// (40 registers), 8 -> 16 (64).
+constexpr int kOrbitBlock = 64;
+constexpr int orbit_min_blocks(int U) { return (U <= 4 ? 6 : 4) * (256 / kOrbitBlock); }
 
 template <typename V, int EPI, int U>
-__global__ void __launch_bounds__(256, orbit_min_blocks(U))
+__global__ void __launch_bounds__(kOrbitBlock, orbit_min_blocks(U))
 k_sym_orbit(const uint64_t* __restrict__ rowptr4, const uint32_t* __restrict__ key, const V* __restrict__ val,
             uint32_t nrows, const float4* __restrict__ orb, const uint32_t* __restrict__ oimg,
-            const uint32_t* __restrict__ omask, const int32_t* __restrict__ g, float* __restrict__ out,
+            const uint64_t* __restrict__ olead,
+            const int32_t* __restrict__ g, float* __restrict__ out,
             float* __restrict__ fwproj, float* __restrict__ f, const float* __restrict__ norm,
-            float* __restrict__ orbit_out) {
+            float* orbit_out, bool orbit_only, const int32_t* __restrict__ g_orb,
+            const float* __restrict__ norm_orb) {
     const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
     if (row >= nrows) return;  // warp-uniform
@@ -258,8 +263,35 @@ k_sym_orbit(const uint64_t* __restrict__ rowptr4, const uint32_t* __restrict__ k
     const float b0 = __shfl_sync(0xffffffffu, acc[0], src), b1 = __shfl_sync(0xffffffffu, acc[1], src);
     const float b2 = __shfl_sync(0xffffffffu, acc[2], src), b3 = __shfl_sync(0xffffffffu, acc[3], src);
     const float mine = q == 0 ? b0 : (q == 1 ? b1 : (q == 2 ? b2 : b3));
-    const uint32_t r = lane < 16 ? oimg[16 * (uint64_t)row + lane] : 0u;
-    const bool writer = lane < 16 && ((omask[row] >> lane) & 1u);
+    const uint64_t o16 = 16 * (uint64_t)row + lane;
+    // lane s < 16: the first transformation with the same output row as s
+    // (itself for the rows it writes); lanes 16-31 point at themselves
+    const uint32_t leader = lane < 16 ? (uint32_t)(olead[row] >> (4 * lane)) & 15u : lane;
+    if (orbit_only) {
+        // MLEM loop of two compact projections: per-row operands and results
+        // in orbit order (64 contiguous bytes per row), natural order only for
+        // the optional forward projection
+        const uint32_t r = (lane < 16 && fwproj) ? oimg[o16] : 0u;
+        float res = mine;
+        if (lane < 16) {
+            if (EPI == (int)Epi::Correl) {
+                res = (mine != 0.0f) ? __fdiv_rn((float)g_orb[o16], mine) : 0.0f;
+            } else if (EPI == (int)Epi::Update) {
+                const float tt = __fmul_rn(orbit_out[o16], mine);
+                const float nn = norm_orb[o16];
+                res = (nn == 0.0f) ? tt : __fdiv_rn(tt, nn);
+            }
+        }
+        // duplicates take the value of the first s with the same output row
+        const float v = __shfl_sync(0xffffffffu, res, leader);
+        if (lane < 16) {
+            orbit_out[o16] = v;
+            if (EPI == (int)Epi::Correl && fwproj && leader == lane) fwproj[r] = mine;
+        }
+        return;
+    }
+    const uint32_t r = lane < 16 ? oimg[o16] : 0u;
+    const bool writer = lane < 16 && leader == lane;
     float res = mine;
     if (writer) {
         if (EPI == (int)Epi::Correl) {
@@ -278,10 +310,25 @@ k_sym_orbit(const uint64_t* __restrict__ rowptr4, const uint32_t* __restrict__ k
     if (orbit_out) {
         // every s gets the value written for its output row (by the first s
         // with that row), so the orbit array equals a gather of the output
-        const unsigned long long id = lane < 16 ? (unsigned long long)r : (1ull << 32) | lane;
-        const uint32_t leader = __ffs(__match_any_sync(0xffffffffu, id)) - 1;
         const float v = __shfl_sync(0xffffffffu, res, leader);
-        if (lane < 16) orbit_out[16 * (uint64_t)row + lane] = v;
+        if (lane < 16) orbit_out[o16] = v;
+    }
+}
+
+// orb[i] = src[table[i]] for int32 (the sinogram in orbit order).
+__global__ void k_orbit_gather_i32(int32_t* __restrict__ orb, const int32_t* __restrict__ src,
+                                   const uint32_t* __restrict__ table, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        orb[i] = __ldg(src + __ldg(table + i));
+}
+
+// dst[table[i]] = orb[i] for every i that is its own leader (orbit order
+// back to natural order; every natural element has exactly one leader).
+__global__ void k_orbit_scatter(float* __restrict__ dst, const float* __restrict__ orb,
+                                const uint32_t* __restrict__ table, const uint64_t* __restrict__ lead, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t sidx = (uint32_t)(i & 15u);
+        if (((lead[i >> 4] >> (4 * sidx)) & 15u) == sidx) dst[table[i]] = orb[i];
     }
 }
 
@@ -433,11 +480,14 @@ void orbit_launch(const SymOps& y, bool transposed, const float* x, const EpiArg
         k_orbit_gather<<<grid_of(n_orb), 256, 0, s>>>(orb, x, table, n_orb);
         MLEM_LAUNCHED();
     }
-    launch_ex(k_sym_orbit<V, EPI, U>, dim3(ceil_div_u((uint64_t)rows * 32, 256)), dim3(256), 0, s, win,
+    // the kernel gathers from the orbit array, not from x: an L2 window, if
+    // asked for, covers that
+    if (win.ptr) win = {orb, sizeof(float) * n_orb};
+    launch_ex(k_sym_orbit<V, EPI, U>, dim3(ceil_div_u((uint64_t)rows * 32, kOrbitBlock)), dim3(kOrbitBlock), 0, s, win,
               transposed ? y.bp_rowptr : y.fp_rowptr, transposed ? y.bp_key : y.fp_key,
               static_cast<const V*>(transposed ? y.bp_val : y.fp_val), rows, reinterpret_cast<const float4*>(orb),
-              transposed ? y.vimg : y.img, transposed ? y.vmask : y.mask, e.g, e.out, e.fwproj, e.f, e.norm,
-              e.orbit_out);
+              transposed ? y.vimg : y.img, transposed ? y.vlead : y.lead, e.g, e.out, e.fwproj, e.f, e.norm,
+              e.orbit_out, e.orbit_only, y.g_orb, y.norm_orb);
 }
 
 template <typename V, int EPI>
@@ -467,12 +517,14 @@ void SymOps::release() {
     cudaFree(fp_key);
     cudaFree(fp_val);
     cudaFree(img);
-    cudaFree(mask);
+    cudaFree(lead);
     cudaFree(bp_rowptr);
     cudaFree(bp_key);
     cudaFree(bp_val);
     cudaFree(vimg);
-    cudaFree(vmask);
+    cudaFree(vlead);
+    cudaFree(norm_orb);
+    cudaFree(g_orb);
     cudaFree(orb_x);
     cudaFree(orb_r);
     *this = SymOps();
@@ -481,7 +533,10 @@ void SymOps::release() {
 uint64_t SymOps::bytes() const {
     if (!fp_rowptr) return 0;
     const size_t vb = val_bytes(vt);
-    return sizeof(uint64_t) * (4 * ((uint64_t)K + J) + 2) + (4 + vb) * (fp_nnz + bp_nnz) + 4 * 33 * ((uint64_t)K + J);
+    // row pointers, entries, and per canonical row / voxel: 16 images, a
+    // leader word, 2 orbit arrays (image or ratio, plus sinogram or sensitivity)
+    return sizeof(uint64_t) * (4 * ((uint64_t)K + J) + 2) + (4 + vb) * (fp_nnz + bp_nnz) +
+           (16 * 4 + 8 + 2 * 16 * 4) * ((uint64_t)K + J);
 }
 
 void check_symmetric_geometry(const mlem_geometry& g) {
@@ -527,7 +582,8 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
     std::vector<uint8_t>().swap(canon_flag);
     const uint64_t K = canon.size();
     MLEM_REQUIRE(K < (1ull << 28), MLEM_EUNSUPPORTED, "symmetry: too many canonical rows");
-    std::vector<uint32_t> img(16 * K), mask(K, 0), can_row(nlor);
+    std::vector<uint32_t> img(16 * K), can_row(nlor);
+    std::vector<uint64_t> lead(K, 0);
     std::vector<uint8_t> sym_of(nlor);
 #pragma omp parallel for schedule(static)
     for (int64_t k = 0; k < (int64_t)K; ++k) {
@@ -536,10 +592,10 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
         for (int t = 0; t < 16; ++t) {
             const uint64_t im = M.lor(M.det(t, a), M.det(t, b));
             img[16 * k + t] = (uint32_t)im;
-            bool first = true;
-            for (int u = 0; u < t && first; ++u) first = img[16 * k + u] != im;
-            if (first) {
-                mask[k] |= 1u << t;
+            int first = 0;
+            while (img[16 * k + first] != im) ++first;
+            lead[k] |= (uint64_t)first << (4 * t);
+            if (first == t) {
                 can_row[im] = (uint32_t)k;
                 sym_of[im] = (uint8_t)t;
             }
@@ -548,7 +604,8 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
     // voxel orbits: canonical voxels (smallest index of each orbit), their 16
     // images, and for every voxel its canonical voxel and the first
     // transformation that produces it
-    std::vector<uint32_t> vrow, vimg, vmask, vorb(cols);
+    std::vector<uint32_t> vrow, vimg, vorb(cols);
+    std::vector<uint64_t> vlead;
     std::vector<uint8_t> vsym(cols);
     for (uint32_t c = 0; c < cols; ++c) {
         uint32_t seen[16];
@@ -556,19 +613,19 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
         for (int t = 0; t < 16; ++t) mn = std::min(mn, seen[t] = M.vox_index(t, c));
         if (mn != c) continue;
         const uint32_t j = (uint32_t)vrow.size();
-        uint32_t msk = 0;
+        uint64_t ld = 0;
         for (int t = 0; t < 16; ++t) {
-            bool first = true;
-            for (int u = 0; u < t && first; ++u) first = seen[u] != seen[t];
-            if (first) {
-                msk |= 1u << t;
+            int first = 0;
+            while (seen[first] != seen[t]) ++first;
+            ld |= (uint64_t)first << (4 * t);
+            if (first == t) {
                 vorb[seen[t]] = j;
                 vsym[seen[t]] = (uint8_t)t;
             }
             vimg.push_back(seen[t]);
         }
         vrow.push_back(c);
-        vmask.push_back(msk);
+        vlead.push_back(ld);
     }
     MLEM_REQUIRE(vrow.size() < (1ull << 28), MLEM_EUNSUPPORTED, "symmetry: too many canonical voxels");
 
@@ -676,7 +733,7 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
             cudaFree(d_vsym);
         }
         y.img = upload(img);
-        y.mask = upload(mask);
+        y.lead = upload(lead);
         // back-projection operand: rows of A^T for the canonical voxels, LORs as canonical row << 4 | t
         {
             uint32_t* d_vrow = upload(vrow);
@@ -690,7 +747,9 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
             cudaFree(d_vrow);
         }
         y.vimg = upload(vimg);
-        y.vmask = upload(vmask);
+        y.vlead = upload(vlead);
+        MLEM_CUDA(cudaMalloc(&y.norm_orb, sizeof(float) * 16 * std::max<uint64_t>(y.J, 1)));
+        MLEM_CUDA(cudaMalloc(&y.g_orb, sizeof(int32_t) * 16 * std::max<uint64_t>(y.K, 1)));
         MLEM_CUDA(cudaMalloc(&y.orb_x, sizeof(float) * 16 * std::max<uint64_t>(y.J, 1)));
         MLEM_CUDA(cudaMalloc(&y.orb_r, sizeof(float) * 16 * std::max<uint64_t>(y.K, 1)));
         y.vt = MLEM_VAL_F32;
@@ -728,6 +787,27 @@ void lower_symmetric_values(SymOps& y, mlem_value_type vt, cudaStream_t s) {
     lower(y.fp_val, y.fp_nnz);
     lower(y.bp_val, y.bp_nnz);
     y.vt = vt;
+}
+
+void sym_set_norm(SymOps& y, const float* norm, cudaStream_t s) {
+    if (!y.fp_rowptr) return;
+    const uint64_t n = 16ull * y.J;
+    k_orbit_gather<<<grid_of(n), 256, 0, s>>>(y.norm_orb, norm, y.vimg, n);
+    MLEM_LAUNCHED();
+}
+
+void sym_gather_sinogram(const SymOps& y, const int32_t* g, cudaStream_t s) {
+    MLEM_REQUIRE(y.fp_rowptr != nullptr, MLEM_EINVAL, "matrix has no symmetry operands");
+    const uint64_t n = 16ull * y.K;
+    k_orbit_gather_i32<<<grid_of(n), 256, 0, s>>>(y.g_orb, g, y.img, n);
+    MLEM_LAUNCHED();
+}
+
+void sym_scatter_image(const SymOps& y, float* f, cudaStream_t s) {
+    MLEM_REQUIRE(y.fp_rowptr != nullptr, MLEM_EINVAL, "matrix has no symmetry operands");
+    const uint64_t n = 16ull * y.J;
+    k_orbit_scatter<<<grid_of(n), 256, 0, s>>>(f, y.orb_x, y.vimg, y.vlead, n);
+    MLEM_LAUNCHED();
 }
 
 void sym_gather_image(const SymOps& y, const float* f, cudaStream_t s) {
