@@ -57,7 +57,9 @@ class MatrixOpts(C.Structure):
 class MatrixInfo(C.Structure):
     _fields_ = [("rows", C.c_uint32), ("cols", C.c_uint32), ("nnz", C.c_uint64),
                 ("value_type", C.c_int), ("has_transpose", C.c_uint32), ("device_bytes", C.c_uint64),
-                ("max_row_nnz", C.c_uint32), ("max_col_nnz", C.c_uint32)]
+                ("max_row_nnz", C.c_uint32), ("max_col_nnz", C.c_uint32),
+                ("sym_lor_rows", C.c_uint32), ("sym_voxel_rows", C.c_uint32),
+                ("sym_fp_nnz", C.c_uint64), ("sym_bp_nnz", C.c_uint64)]
 
 
 class RunOpts(C.Structure):
@@ -279,6 +281,8 @@ class Matrix:
         self.has_transpose = bool(info.has_transpose)
         self.device_bytes = info.device_bytes
         self.max_row_nnz, self.max_col_nnz = info.max_row_nnz, info.max_col_nnz
+        self.symmetry = {"lor_rows": info.sym_lor_rows, "voxel_rows": info.sym_voxel_rows,
+                         "fp_nnz": info.sym_fp_nnz, "bp_nnz": info.sym_bp_nnz} if info.sym_lor_rows else None
 
     # construction ---------------------------------------------------------
     @staticmethod

@@ -337,7 +337,7 @@ static ProjCfg resolve_cfg(const mlem_matrix* m, bool transposed, const mlem_run
         c.unroll = 2;
     } else if (o.kernel == MLEM_KERNEL_SYM) {
         c.kind = MLEM_KERNEL_SYM;
-        c.unroll = o.unroll >= 8 ? 8 : (o.unroll == 0 || o.unroll == 4 ? 4 : 2);
+        c.unroll = (o.unroll == 0 || o.unroll >= 8) ? 8 : (o.unroll == 4 ? 4 : 2);
     } else {
         c.kind = MLEM_KERNEL_DIRECT;
         c.lanes = o.lanes ? (int)o.lanes : pick_lanes(op.nnz, op.nrows);
@@ -877,6 +877,10 @@ mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info) {
         info->device_bytes = m->bytes();
         info->max_row_nnz = m->A.max_row;
         info->max_col_nnz = m->has_t ? m->AT.max_row : 0;
+        info->sym_lor_rows = m->sym.K;
+        info->sym_voxel_rows = m->sym.J;
+        info->sym_fp_nnz = m->sym.fp_nnz;
+        info->sym_bp_nnz = m->sym.bp_nnz;
     });
 }
 

@@ -454,7 +454,8 @@ def run_symmetry(pkg, torch, name):
     for vt, label in ((pkg.VAL_F32, "fp32"), (pkg.VAL_F16, "fp16")):
         t0 = time.time()
         m = pkg.Matrix.generate(geo, value_type=vt, symmetry=True)
-        r = {"build_s": time.time() - t0, "device_bytes": m.device_bytes, "plain_fp32_device_bytes": plain_bytes}
+        r = {"build_s": time.time() - t0, "device_bytes": m.device_bytes, "plain_fp32_device_bytes": plain_bytes,
+             "nnz": m.nnz, "compact": m.symmetry}
         g_dev = torch.from_numpy(g).cuda()
         f0_dev = torch.from_numpy(f0).cuda()
         f_dev = torch.empty_like(f0_dev)

@@ -136,6 +136,10 @@ typedef struct {
     uint32_t has_transpose;
     uint64_t device_bytes;      /* bytes of device memory held by the handle */
     uint32_t max_row_nnz, max_col_nnz;
+    /* symmetry = 1 only (else 0): canonical LOR rows and canonical voxels (the
+     * rows of the two compact operands) and the entries of each operand */
+    uint32_t sym_lor_rows, sym_voxel_rows;
+    uint64_t sym_fp_nnz, sym_bp_nnz;
 } mlem_matrix_info;
 
 mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info);
@@ -168,7 +172,7 @@ typedef struct {
                                    PERSISTENT 16 or 32); 0 = chosen from the mean row length */
     uint32_t unroll;            /* same kernels: vectors of 4 elements in flight per lane
                                    (1, 2, 4; PERSISTENT 1 or 2); 0 = 2.  SYM: entries in flight
-                                   per lane, 2 (1, 2), 4 (0, 4) or 8 */
+                                   per lane, 2 (1, 2), 4 or 8 (0, 8) */
     uint32_t row_order;         /* DIRECT / PERSISTENT with 16 or 32 lanes: 1 = process the rows in
                                    the locality order of a generated matrix */
     uint32_t pipeline;          /* DIRECT / ORDERED with 16 or 32 lanes: 1 = load a row's next vectors
