@@ -37,7 +37,7 @@ typedef enum {
     MLEM_ENOMEM = 3,      /* device or host allocation failed, or admission refused */
     MLEM_ECUDA = 4,       /* a CUDA runtime call failed */
     MLEM_ETIMEOUT = 5,    /* a bounded wait expired (server) */
-    MLEM_EUNSUPPORTED = 6,/* size or mode outside what this build handles */
+    MLEM_EUNSUPPORTED = 6,/* size or mode outside what the library handles */
     MLEM_EBUSY = 7        /* server queue full / object in use */
 } mlem_status;
 
