@@ -106,6 +106,10 @@ void composition(const SymMaps& M, uint8_t comp[16][16], uint8_t inv[16]) {
             const int d = ((s >> 2) & 1) ? (4 - (t & 3)) & 3 : (t & 3);
             const int closed = ((s + d) & 3) + 4 * (((s >> 2) ^ (t >> 2)) & 1) + 8 * ((s >> 3) ^ (t >> 3));
             MLEM_REQUIRE(found == closed, MLEM_EINVAL, "internal: symmetry composition differs from its closed form");
+            // ... and the detectors (hence LORs) compose the same way as the voxels
+            for (uint32_t d = 0; d < M.D; d += std::max(1u, M.D / 61))
+                MLEM_REQUIRE(M.det(s, M.det(t, d)) == M.det(closed, d), MLEM_EINVAL,
+                             "internal: detector maps compose differently from voxel maps");
             comp[s][t] = (uint8_t)found;
         }
     for (int s = 0; s < 16; ++s)
