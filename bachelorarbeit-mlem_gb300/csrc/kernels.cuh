@@ -181,9 +181,10 @@ void sym_set_norm(SymOps& y, const float* norm, cudaStream_t s);
 void sym_gather_image(const SymOps& y, const float* f, cudaStream_t s);
 void sym_gather_sinogram(const SymOps& y, const int32_t* g, cudaStream_t s);
 void sym_scatter_image(const SymOps& y, float* f, cudaStream_t s);
-// unroll: entries per lane in flight (2, 4 or 8).
-void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, L2Window win,
-                cudaStream_t s);
+// unroll: entries per lane in flight (2, 4 or 8); grouped: the blocks that
+// start together on an SM take neighbouring rows.
+void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, bool grouped,
+                L2Window win, cudaStream_t s);
 
 // ------------------------------------------------------------- siddon.cu
 uint64_t siddon_rows(const mlem_geometry& geo);

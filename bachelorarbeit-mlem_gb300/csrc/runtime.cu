@@ -217,7 +217,7 @@ static void launch_cfg(mlem_matrix* m, const DevCsr& op, const float* x, const E
     } else if (c.kind == MLEM_KERNEL_D16) {
         launch_csr_d16(op, x, e, win, s);
     } else if (c.kind == MLEM_KERNEL_SYM) {
-        launch_sym(m->sym, &op == &m->AT, x, e, c.unroll, win, s);
+        launch_sym(m->sym, &op == &m->AT, x, e, c.unroll, c.ordered, win, s);
     } else if (c.kind == MLEM_KERNEL_ILV) {
         launch_csr_ilv(op, x, e, c.unroll, win, s);
     } else if (c.kind == MLEM_KERNEL_PERSISTENT) {
@@ -252,7 +252,8 @@ static void tune_projection(mlem_matrix* m, bool transposed) {
     if (op.idx_ilv)
         for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_ILV, 32, u, 0.f});
     if (m->sym.fp_rowptr)
-        for (int u : {2, 4, 8}) cand.push_back(ProjCfg{MLEM_KERNEL_SYM, 32, u, 0.f});
+        for (int u : {2, 4, 8})
+            for (bool grouped : {false, true}) cand.push_back(ProjCfg{MLEM_KERNEL_SYM, 32, u, 0.f, grouped, false});
     prepare_csrvec_pipe(op.vt);
     prepare_csr_tma(op.vt);
     ensure_workspace(m);
@@ -338,6 +339,7 @@ static ProjCfg resolve_cfg(const mlem_matrix* m, bool transposed, const mlem_run
     } else if (o.kernel == MLEM_KERNEL_SYM) {
         c.kind = MLEM_KERNEL_SYM;
         c.unroll = (o.unroll == 0 || o.unroll >= 8) ? 8 : (o.unroll == 4 ? 4 : 2);
+        c.ordered = o.row_order != 0;
     } else {
         c.kind = MLEM_KERNEL_DIRECT;
         c.lanes = o.lanes ? (int)o.lanes : pick_lanes(op.nnz, op.nrows);

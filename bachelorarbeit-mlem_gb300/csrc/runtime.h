@@ -107,7 +107,7 @@ struct ProjCfg {
     int lanes = 32;  // DIRECT: lanes per row
     int unroll = 2;  // DIRECT: 4-element vectors in flight per lane; SYM: entries in flight per lane
     float ms = 0.f;  // measured time of one launch
-    bool ordered = false;    // DIRECT / PERSISTENT: rows in the operand's locality order
+    bool ordered = false;    // DIRECT / PERSISTENT: rows in the operand's locality order; SYM: rows grouped by SM
     bool pipelined = false;  // DIRECT: next vectors loaded before the current gathers; SYM: next keys
 };
 }  // namespace mlem

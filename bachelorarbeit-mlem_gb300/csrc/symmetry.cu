@@ -240,8 +240,13 @@ k_sym_orbit(const uint64_t* __restrict__ rowptr4, const uint32_t* __restrict__ k
             const int32_t* __restrict__ g, float* __restrict__ out,
             float* __restrict__ fwproj, float* __restrict__ f, const float* __restrict__ norm,
             float* orbit_out, bool orbit_only, const int32_t* __restrict__ g_orb,
-            const float* __restrict__ norm_orb) {
-    const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+            const float* __restrict__ norm_orb, uint32_t groups, uint32_t per_group) {
+    // block b works on row block (b % groups) * per_group + b / groups; with
+    // groups = the SM count, the blocks that start together on one SM take
+    // neighbouring canonical rows, whose orbit rows overlap (L1 reuse);
+    // groups = 1 is the plain order
+    const uint32_t rb = (blockIdx.x % groups) * per_group + blockIdx.x / groups;
+    const uint32_t row = rb * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const uint32_t lane = threadIdx.x & 31u;
     if (row >= nrows) return;  // warp-uniform
     const uint32_t lb = lane & 3u, mg = lane & 1u, slot = lane >> 2;
@@ -475,7 +480,8 @@ void build_segmented(const uint64_t* rp, const uint32_t* idx, const float* val, 
 }
 
 template <typename V, int EPI, int U>
-void orbit_launch(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+void orbit_launch(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, bool grouped, L2Window win,
+                  cudaStream_t s) {
     const uint32_t rows = transposed ? y.J : y.K;
     float* orb = transposed ? y.orb_r : y.orb_x;
     const uint32_t* table = transposed ? y.img : y.vimg;  // input orbits: LORs for BP, voxels for FP
@@ -487,30 +493,32 @@ void orbit_launch(const SymOps& y, bool transposed, const float* x, const EpiArg
     // the kernel gathers from the orbit array, not from x: an L2 window, if
     // asked for, covers that
     if (win.ptr) win = {orb, sizeof(float) * n_orb};
-    launch_ex(k_sym_orbit<V, EPI, U>, dim3(ceil_div_u((uint64_t)rows * 32, kOrbitBlock)), dim3(kOrbitBlock), 0, s, win,
+    const uint32_t row_blocks = (uint32_t)ceil_div_u((uint64_t)rows * 32, kOrbitBlock);
+    const uint32_t groups = grouped ? 152u : 1u, per_group = (uint32_t)ceil_div_u(row_blocks, groups);
+    launch_ex(k_sym_orbit<V, EPI, U>, dim3(groups * per_group), dim3(kOrbitBlock), 0, s, win,
               transposed ? y.bp_rowptr : y.fp_rowptr, transposed ? y.bp_key : y.fp_key,
               static_cast<const V*>(transposed ? y.bp_val : y.fp_val), rows, reinterpret_cast<const float4*>(orb),
               transposed ? y.vimg : y.img, transposed ? y.vlead : y.lead, e.g, e.out, e.fwproj, e.f, e.norm,
-              e.orbit_out, e.orbit_only, y.g_orb, y.norm_orb);
+              e.orbit_out, e.orbit_only, y.g_orb, y.norm_orb, groups, per_group);
 }
 
 template <typename V, int EPI>
-void orbit_variant(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, L2Window win,
-                   cudaStream_t s) {
-    if (unroll >= 8) orbit_launch<V, EPI, 8>(y, transposed, x, e, win, s);
-    else if (unroll >= 4) orbit_launch<V, EPI, 4>(y, transposed, x, e, win, s);
-    else orbit_launch<V, EPI, 2>(y, transposed, x, e, win, s);
+void orbit_variant(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, bool grouped,
+                   L2Window win, cudaStream_t s) {
+    if (unroll >= 8) orbit_launch<V, EPI, 8>(y, transposed, x, e, grouped, win, s);
+    else if (unroll >= 4) orbit_launch<V, EPI, 4>(y, transposed, x, e, grouped, win, s);
+    else orbit_launch<V, EPI, 2>(y, transposed, x, e, grouped, win, s);
 }
 
 template <typename V>
-void sym_dispatch(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, L2Window win,
-                  cudaStream_t s) {
+void sym_dispatch(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, bool grouped,
+                  L2Window win, cudaStream_t s) {
     if (!transposed) {
-        if (e.kind == Epi::Correl) orbit_variant<V, (int)Epi::Correl>(y, false, x, e, unroll, win, s);
-        else orbit_variant<V, (int)Epi::Raw>(y, false, x, e, unroll, win, s);
+        if (e.kind == Epi::Correl) orbit_variant<V, (int)Epi::Correl>(y, false, x, e, unroll, grouped, win, s);
+        else orbit_variant<V, (int)Epi::Raw>(y, false, x, e, unroll, grouped, win, s);
     } else {
-        if (e.kind == Epi::Update) orbit_variant<V, (int)Epi::Update>(y, true, x, e, unroll, win, s);
-        else orbit_variant<V, (int)Epi::Raw>(y, true, x, e, unroll, win, s);
+        if (e.kind == Epi::Update) orbit_variant<V, (int)Epi::Update>(y, true, x, e, unroll, grouped, win, s);
+        else orbit_variant<V, (int)Epi::Raw>(y, true, x, e, unroll, grouped, win, s);
     }
 }
 
@@ -821,13 +829,13 @@ void sym_gather_image(const SymOps& y, const float* f, cudaStream_t s) {
     MLEM_LAUNCHED();
 }
 
-void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, L2Window win,
-                cudaStream_t s) {
+void launch_sym(const SymOps& y, bool transposed, const float* x, const EpiArgs& e, int unroll, bool grouped,
+                L2Window win, cudaStream_t s) {
     MLEM_REQUIRE(y.fp_rowptr != nullptr, MLEM_EINVAL, "matrix has no symmetry operands");
     switch (y.vt) {
-        case MLEM_VAL_F32: sym_dispatch<float>(y, transposed, x, e, unroll, win, s); break;
-        case MLEM_VAL_F16: sym_dispatch<__half>(y, transposed, x, e, unroll, win, s); break;
-        default: sym_dispatch<__nv_bfloat16>(y, transposed, x, e, unroll, win, s);
+        case MLEM_VAL_F32: sym_dispatch<float>(y, transposed, x, e, unroll, grouped, win, s); break;
+        case MLEM_VAL_F16: sym_dispatch<__half>(y, transposed, x, e, unroll, grouped, win, s); break;
+        default: sym_dispatch<__nv_bfloat16>(y, transposed, x, e, unroll, grouped, win, s);
     }
 }
 

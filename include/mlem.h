@@ -174,7 +174,8 @@ typedef struct {
                                    (1, 2, 4; PERSISTENT 1 or 2); 0 = 2.  SYM: entries in flight
                                    per lane, 2 (1, 2), 4 or 8 (0, 8) */
     uint32_t row_order;         /* DIRECT / PERSISTENT with 16 or 32 lanes: 1 = process the rows in
-                                   the locality order of a generated matrix */
+                                   the locality order of a generated matrix; SYM: 1 = the blocks that
+                                   start together on an SM take neighbouring canonical rows */
     uint32_t pipeline;          /* DIRECT / ORDERED with 16 or 32 lanes: 1 = load a row's next vectors
                                    before the gathers of the current ones (same results) */
     uint32_t kernel_timing;     /* mlem_run only: 1 = CUDA events around the forward and back
