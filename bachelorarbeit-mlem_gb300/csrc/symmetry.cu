@@ -437,6 +437,55 @@ __global__ void k_seg_fill(const uint64_t* __restrict__ rp, const uint32_t* __re
     }
 }
 
+// Each segment sorted by key (orbit row, then transformation), so the entries
+// one load instruction covers tend to share 128-byte orbit lines.  One warp
+// per segment, bitonic in shared memory; segments longer than kSortCap stay
+// in column order (the order does not change the sums beyond rounding).
+constexpr uint32_t kSortCap = 2048;
+
+__global__ void k_seg_sort(const uint64_t* __restrict__ orp, uint64_t nseg, uint32_t* __restrict__ key,
+                           float* __restrict__ val) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    uint32_t* sk = reinterpret_cast<uint32_t*>(sm) + (size_t)w * kSortCap * 2;
+    float* sv = reinterpret_cast<float*>(sk + kSortCap);
+    for (uint64_t g = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; g < nseg;
+         g += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+        const uint64_t s0 = orp[g], n = orp[g + 1] - s0;
+        if (n < 2 || n > kSortCap) continue;  // warp-uniform
+        uint32_t m = 32;
+        while (m < n) m <<= 1;
+        for (uint32_t i = lane; i < m; i += 32) {
+            sk[i] = i < n ? key[s0 + i] : 0xffffffffu;
+            sv[i] = i < n ? val[s0 + i] : 0.f;
+        }
+        __syncwarp();
+        for (uint32_t k = 2; k <= m; k <<= 1)
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                for (uint32_t i = lane; i < m; i += 32) {
+                    const uint32_t p = i ^ j;
+                    if (p > i) {
+                        const bool up = (i & k) == 0;
+                        if ((sk[i] > sk[p]) == up) {
+                            const uint32_t tk = sk[i];
+                            sk[i] = sk[p];
+                            sk[p] = tk;
+                            const float tv = sv[i];
+                            sv[i] = sv[p];
+                            sv[p] = tv;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        for (uint32_t i = lane; i < n; i += 32) {
+            key[s0 + i] = sk[i];
+            val[s0 + i] = sv[i];
+        }
+        __syncwarp();
+    }
+}
+
 // Builds one compact operand (segmented row pointers [4 nrows + 1], keys, FP32 values).
 void build_segmented(const uint64_t* rp, const uint32_t* idx, const float* val, const uint32_t* rowsel, uint32_t nrows,
                      const uint32_t* orb_of, const uint8_t* sym, uint64_t*& orp, uint32_t*& okey, void*& oval,
@@ -470,6 +519,11 @@ void build_segmented(const uint64_t* rp, const uint32_t* idx, const float* val, 
         MLEM_CUDA(cudaMalloc(&oval, sizeof(float) * (onnz + 16)));
         k_seg_fill<<<grid_of((uint64_t)nrows * 32), 256, 0, s>>>(rp, idx, val, rowsel, nrows, orb_of, sym, orp, okey,
                                                                    static_cast<float*>(oval));
+        MLEM_LAUNCHED();
+        constexpr int kSortWarps = 4;
+        const size_t smem = (size_t)kSortWarps * kSortCap * 8;
+        MLEM_CUDA(cudaFuncSetAttribute(k_seg_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_seg_sort<<<grid_of(nseg * 32 / 2), kSortWarps * 32, smem, s>>>(orp, nseg, okey, static_cast<float*>(oval));
         MLEM_LAUNCHED();
         MLEM_CUDA(cudaStreamSynchronize(s));
     } catch (...) {
