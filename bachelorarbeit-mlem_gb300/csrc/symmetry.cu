@@ -161,58 +161,57 @@ __device__ __forceinline__ float comp4(const float4& v, int i) {
     return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
+// One step of a segment: UU entries per lane (entries base + slot + 8u),
+// predicated when PRED (the last step of a segment).
+template <typename V, int UU, bool PRED>
+__device__ __forceinline__ void orbit_step(const uint32_t* __restrict__ kp, const V* __restrict__ vp,
+                                           const float4* __restrict__ orb, uint32_t base, uint32_t n,
+                                           uint32_t slot, uint32_t lb, float4& sa) {
+    uint32_t kk[UU];
+    float v[UU];
+    float4 o[UU];
+#pragma unroll
+    for (int u = 0; u < UU; ++u) {
+        const uint32_t i = base + slot + 8 * u;
+        const bool ok = !PRED || i < n;
+        kk[u] = ok ? __ldcs(kp + i) : 0u;
+        v[u] = ok ? ld_val<V>(vp, i) : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < UU; ++u) {
+        const bool ok = !PRED || base + slot + 8 * u < n;
+        o[u] = ok ? __ldg(orb + ((kk[u] >> 2) ^ lb)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < UU; ++u) {
+        sa.x = fmaf(v[u], o[u].x, sa.x);
+        sa.y = fmaf(v[u], o[u].y, sa.y);
+        sa.z = fmaf(v[u], o[u].z, sa.z);
+        sa.w = fmaf(v[u], o[u].w, sa.w);
+    }
+}
+
 // Segment Q of a compact row (entries with q_t = Q): unrotated sums, then
 // acc[p] += sums[(p + d) & 3] with d = Q (m_s = 0) or -Q (m_s = 1).
+// Warp-uniform steps of 8·U entries, then one predicated step of 8·U'
+// entries, U' the smallest power of two that covers the remainder.
 template <typename V, int U, int Q>
 __device__ __forceinline__ void orbit_segment(const uint32_t* __restrict__ key, const V* __restrict__ val,
                                               const float4* __restrict__ orb, uint64_t s0, uint64_t s1,
                                               uint32_t slot, uint32_t lb, uint32_t mg, float (&acc)[4]) {
     float4 sa = make_float4(0.f, 0.f, 0.f, 0.f);
-    // row-local 32-bit offsets; full steps of U entries per lane, then one
-    // predicated step
+    // row-local 32-bit offsets
     const uint32_t* kp = key + s0;
     const V* vp = val + s0;
     const uint32_t n = (uint32_t)(s1 - s0);
-    uint32_t i = slot;
-    for (; i + 8 * (U - 1) < n; i += 8 * U) {
-        uint32_t kk[U];
-        float v[U];
-        float4 o[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            kk[u] = __ldcs(kp + i + 8 * u);
-            v[u] = ld_val<V>(vp, i + 8 * u);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) o[u] = __ldg(orb + ((kk[u] >> 2) ^ lb));
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            sa.x = fmaf(v[u], o[u].x, sa.x);
-            sa.y = fmaf(v[u], o[u].y, sa.y);
-            sa.z = fmaf(v[u], o[u].z, sa.z);
-            sa.w = fmaf(v[u], o[u].w, sa.w);
-        }
-    }
-    if (i < n) {
-        uint32_t kk[U];
-        float v[U];
-        float4 o[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const bool ok = i + 8 * u < n;
-            kk[u] = ok ? __ldcs(kp + i + 8 * u) : 0u;
-            v[u] = ok ? ld_val<V>(vp, i + 8 * u) : 0.f;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-            o[u] = (i + 8 * u < n) ? __ldg(orb + ((kk[u] >> 2) ^ lb)) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            sa.x = fmaf(v[u], o[u].x, sa.x);
-            sa.y = fmaf(v[u], o[u].y, sa.y);
-            sa.z = fmaf(v[u], o[u].z, sa.z);
-            sa.w = fmaf(v[u], o[u].w, sa.w);
-        }
+    uint32_t base = 0;
+    for (; base + 8 * U <= n; base += 8 * U) orbit_step<V, U, false>(kp, vp, orb, base, n, slot, lb, sa);
+    const uint32_t rem = n - base;  // < 8 U, the same in every lane
+    if (rem > 0) {
+        if (U >= 8 && rem > 32) orbit_step<V, (U >= 8 ? 8 : 1), true>(kp, vp, orb, base, n, slot, lb, sa);
+        else if (U >= 4 && rem > 16) orbit_step<V, (U >= 4 ? 4 : 1), true>(kp, vp, orb, base, n, slot, lb, sa);
+        else if (U >= 2 && rem > 8) orbit_step<V, (U >= 2 ? 2 : 1), true>(kp, vp, orb, base, n, slot, lb, sa);
+        else orbit_step<V, 1, true>(kp, vp, orb, base, n, slot, lb, sa);
     }
     constexpr int D0 = Q, D1 = (4 - Q) & 3;
 #pragma unroll
