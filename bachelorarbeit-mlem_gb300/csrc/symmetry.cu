@@ -227,9 +227,9 @@ __device__ __forceinline__ void orbit_segment(const uint32_t* __restrict__ key, 
 // per lane in flight.
 // Blocks of 2 warps (rows differ in length; a small block frees its slot
 // early).  Register budget per unroll: U = 2 or 4 -> 24 blocks per SM
-// (40 registers), 8 -> 16 (64).
+// (40 registers), 8 -> 20 (48).
 constexpr int kOrbitBlock = 64;
-constexpr int orbit_min_blocks(int U) { return (U <= 4 ? 6 : 4) * (256 / kOrbitBlock); }
+constexpr int orbit_min_blocks(int U) { return U <= 4 ? 24 : 20; }
 
 template <typename V, int EPI, int U>
 __global__ void __launch_bounds__(kOrbitBlock, orbit_min_blocks(U))
