@@ -200,7 +200,29 @@ def cpu_baseline(pkg, name, stride, iters=1):
     t0 = time.perf_counter()
     O.mlem_omp((rp, col, val), AT, g, norm, f0, iters, threads)
     dt = (time.perf_counter() - t0) / iters
-    return dict(nnz=len(col), rows=len(rp) - 1, seconds=dt, cores=threads, stride=stride)
+    t0 = time.perf_counter()
+    O.mlem_omp((rp, col, val), AT, g, norm, f0, 1, 1)
+    dt1 = time.perf_counter() - t0
+    return dict(nnz=len(col), rows=len(rp) - 1, seconds=dt, seconds_one_thread=dt1, cores=threads, stride=stride)
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the platform)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
 
 
 def run_reference(args):
@@ -228,6 +250,8 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 values, f64 accumulation",
         "data": "synthetic", "config": {"workload": name, "iterations_per_step": 1, "form": "fp32 plain"},
         "cpu_baseline": {"value": value, "unit": "iter/s", "cores": s["cores"], "kind": "port",
+                         "cpu_model": cpu_model(),
+                         "one_thread_value": 1.0 / (s["seconds_one_thread"] * full_nnz / s["nnz"]),
                          "sample": f"every {stride}th LOR row ({s['rows']} rows, {s['nnz']} nnz), 1 iteration, "
                                    f"time scaled by full/sample nnz"},
         "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -713,6 +737,8 @@ def main():
         full_nnz = line["config"]["nnz"]
         sec_full = cb["seconds"] * full_nnz / cb["nnz"]
         line["cpu_baseline"] = {"value": 1.0 / sec_full, "unit": "iter/s", "cores": cb["cores"], "kind": "port",
+                                "cpu_model": cpu_model(),
+                                "one_thread_value": 1.0 / (cb["seconds_one_thread"] * full_nnz / cb["nnz"]),
                                 "sample": f"every {cb['stride']}th LOR row of the same matrix ({cb['rows']} rows, "
                                           f"{cb['nnz']} nnz), 1 OpenMP MLEM iteration (FP32 values, FP64 "
                                           f"accumulation), time scaled by {full_nnz}/{cb['nnz']} nnz"}

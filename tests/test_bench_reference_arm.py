@@ -14,6 +14,7 @@ def test_reference_arm_prints_its_line():
     line = json.loads([x for x in r.stdout.splitlines() if x.startswith("{")][-1])
     assert line["impl"] == "reference" and line["unit"] == "iter/s" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["cpu_baseline"]["one_thread_value"] > 0 and line["cpu_baseline"]["cpu_model"]
     assert line["e2e"] == {"value": line["value"], "unit": "iter/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert line["config"]["workload"] == "ring2d"
