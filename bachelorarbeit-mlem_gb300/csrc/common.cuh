@@ -116,11 +116,13 @@ struct DevCsr {
     void* val = nullptr;         // f32/f16/bf16 [padded(nnz)]
     mlem_value_type vt = MLEM_VAL_F32;
     uint32_t max_row = 0;        // longest row
-    // optional delta-compressed indices (spmv_d16.cu)
-    uint64_t* rowmeta = nullptr; // [nrows] first column | first escape index << 32
-    uint16_t* d16 = nullptr;     // [padded(nnz)]
-    uint32_t* esc = nullptr;     // [nesc]
-    uint64_t nesc = 0;
+    // optional delta-coded copy (spmv_d16.cu): rows of 8-entry vectors
+    uint64_t* dvptr = nullptr;   // [nrows+1] first vector of each row
+    uint32_t* dbase = nullptr;   // [nrows] first column of each row
+    uint16_t* d16 = nullptr;     // [8 dvec] column deltas (dummies and padding included)
+    void* dval = nullptr;        // [8 dvec] values at the same positions
+    uint64_t dvec = 0;           // vectors
+    int d16_lanes = 0;           // lanes per row the D16 layout is built for (4 or 8)
     // optional processing order of the rows (locality of the gathers); the
     // k-th row group handles row order[k].  Results are written per row.
     uint32_t* order = nullptr;   // [nrows]

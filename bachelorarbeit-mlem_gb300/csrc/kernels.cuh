@@ -54,7 +54,9 @@ void launch_csr_ilv(const DevCsr& op, const float* x, const EpiArgs& epi, int un
 // Delta-compressed (16-bit) column indices: build from the u32 indices, and
 // the projection that reads them.
 void build_d16(DevCsr& op, cudaStream_t s);
-void launch_csr_d16(const DevCsr& op, const float* x, const EpiArgs& epi, L2Window win, cudaStream_t s);
+// unroll: 1 or 2 vectors of 8 entries in flight per lane (the lanes per row
+// are those the layout was built for).
+void launch_csr_d16(const DevCsr& op, const float* x, const EpiArgs& epi, int unroll, L2Window win, cudaStream_t s);
 // Persistent, software-pipelined csr-vector variant (16 or 32 lanes per row,
 // 1 or 2 vectors per lane and step, optional locality order); bit-identical
 // to launch_csrvec with the same lanes.  prepare_* settles the grid sizes

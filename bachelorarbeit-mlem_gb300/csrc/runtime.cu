@@ -84,9 +84,10 @@ static void free_csr(DevCsr& c) {
     cudaFree(c.rowptr);
     cudaFree(c.idx);
     cudaFree(c.val);
-    cudaFree(c.rowmeta);
+    cudaFree(c.dvptr);
+    cudaFree(c.dbase);
     cudaFree(c.d16);
-    cudaFree(c.esc);
+    cudaFree(c.dval);
     cudaFree(c.idx_ilv);
     cudaFree(c.val_ilv);
     cudaFree(c.order);
@@ -97,7 +98,7 @@ static uint64_t csr_bytes(const DevCsr& c) {
     if (!c.rowptr) return 0;
     uint64_t b = sizeof(uint64_t) * ((uint64_t)c.nrows + 1) + sizeof(uint32_t) * padded(c.nnz) +
                  val_bytes(c.vt) * padded(c.nnz);
-    if (c.d16) b += sizeof(uint64_t) * c.nrows + sizeof(uint16_t) * padded(c.nnz) + sizeof(uint32_t) * c.nesc;
+    if (c.d16) b += 12ull * c.nrows + 8 + (sizeof(uint16_t) + val_bytes(c.vt)) * 8 * c.dvec;
     if (c.idx_ilv) b += (sizeof(uint32_t) + val_bytes(c.vt)) * c.ilv_len;
     if (c.order) b += sizeof(uint32_t) * c.nrows;
     return b;
@@ -215,7 +216,7 @@ static void launch_cfg(mlem_matrix* m, const DevCsr& op, const float* x, const E
         ensure_workspace(m);
         launch_csr_tma(op, x, e, m->ws.err, win, s);
     } else if (c.kind == MLEM_KERNEL_D16) {
-        launch_csr_d16(op, x, e, win, s);
+        launch_csr_d16(op, x, e, c.unroll, win, s);
     } else if (c.kind == MLEM_KERNEL_SYM) {
         launch_sym(m->sym, &op == &m->AT, x, e, c.unroll, c.ordered, win, s);
     } else if (c.kind == MLEM_KERNEL_ILV) {
@@ -248,7 +249,8 @@ static void tune_projection(mlem_matrix* m, bool transposed) {
         }
     if (base >= 16) cand.push_back(ProjCfg{MLEM_KERNEL_PERSISTENT, base, 1, 0.f, false, false});
     cand.push_back(ProjCfg{MLEM_KERNEL_TMA, 32, 2, 0.f});
-    if (op.d16) cand.push_back(ProjCfg{MLEM_KERNEL_D16, 32, 1, 0.f});
+    if (op.d16)
+        for (int u : {1, 2}) cand.push_back(ProjCfg{MLEM_KERNEL_D16, op.d16_lanes, u, 0.f});
     if (op.idx_ilv)
         for (int u : {1, 2, 4}) cand.push_back(ProjCfg{MLEM_KERNEL_ILV, 32, u, 0.f});
     if (m->sym.fp_rowptr)
@@ -325,6 +327,8 @@ static ProjCfg resolve_cfg(const mlem_matrix* m, bool transposed, const mlem_run
     } else if (o.kernel == MLEM_KERNEL_D16) {
         MLEM_REQUIRE(op.d16 != nullptr, MLEM_EINVAL, "kernel D16 needs a matrix created with compress_indices = 1");
         c.kind = MLEM_KERNEL_D16;
+        c.lanes = op.d16_lanes;
+        c.unroll = o.unroll == 1 ? 1 : 2;
     } else if (o.kernel == MLEM_KERNEL_ORDERED) {
         MLEM_REQUIRE(op.order != nullptr, MLEM_EINVAL, "kernel ORDERED needs a generated matrix (row orders)");
         c.kind = MLEM_KERNEL_DIRECT;

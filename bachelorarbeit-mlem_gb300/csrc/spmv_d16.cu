@@ -1,30 +1,32 @@
-// spmv_d16.cu — projections over delta-compressed column indices (D16).
+// spmv_d16.cu — projections over 16-bit delta-coded column indices (D16).
 //
-// Layout of an operand in D16 form (kept beside the u32 indices):
-//   rowmeta[r] = first column of row r | (index of the row's first escape << 32)
-//   d16[e]     = column(e) - column(e-1) for e inside a row (0 for the row's
-//                first element), or 0xFFFF ("escape") when that difference is
-//                negative or does not fit in 16 bits
-//   esc[k]     = absolute column of the k-th escaped element (element order)
-// With FP16 values a nonzero costs 4 bytes instead of 8 (u32 + f32).
-//
-// Kernel: one warp per row; a round covers 32 vectors of 8 consecutive
-// elements (lane l owns vector l of the round).  The columns are the prefix
-// sum of the deltas with resets at escapes: each lane summarises its vector
-// (escape count; column after its last escape, or its delta sum), two warp
-// scans (escape counts, then columns with the reset operator) give every
-// lane the column before its vector, then the lane decodes its 8 columns,
-// gathers x and accumulates in element order.  Deterministic.
+// A row is cut into steps of 8·L entries, L = op.d16_lanes (4 or 8) lanes per
+// row: position p of a row belongs to lane p % L as element p / L of that
+// lane's sequence, so one gather instruction covers L consecutive entries of
+// the row (few cache lines: its columns are ascending and close).  Each entry
+// stores the difference between its column and the column L positions earlier
+// (the previous element of the same lane; the row's first column for the first
+// L positions): every lane decodes its own columns with one add per entry, no
+// scans and no shuffles.  Layout of an operand in D16 form (beside the u32 CSR):
+//   dvptr[r]  first 8-entry vector of row r (u64[nrows + 1]); vector
+//             dvptr[r] + k·L + l holds lane l's elements 8k..8k+7
+//   dbase[r]  first column of row r
+//   d16[8 v + j], dval[8 v + j]  the delta and the value (the operand's type)
+// A difference of 65,536 or more is bridged by dummy entries (value 0,
+// column = the earlier column + 65,535); rows are padded to whole steps with
+// delta 0 and value 0.  Dummies and padding add 4% (L = 4) to 9% (L = 8) on
+// the generated matrices in the locality layout: with FP16 values ~4.2 bytes
+// per nonzero instead of 8 (u32 + f32).  The lane sums are reduced by a fixed
+// xor tree: deterministic.
 #include "kernels.cuh"
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 namespace mlem {
 
 namespace {
-
-constexpr uint16_t kEsc = 0xFFFF;
 
 template <typename V>
 struct Val8;
@@ -67,101 +69,68 @@ struct Val8<__nv_bfloat16> {
     }
 };
 
-template <typename V, int EPI>
+template <typename V, int EPI, int LPR, int U>
 __global__ void __launch_bounds__(256)
-k_csr_d16(const uint64_t* __restrict__ rowptr, const uint64_t* __restrict__ rowmeta,
-          const uint16_t* __restrict__ d16, const V* __restrict__ val, const uint32_t* __restrict__ esc,
-          const float* __restrict__ x, uint32_t nrows, const int32_t* __restrict__ g, float* __restrict__ out,
-          float* __restrict__ fwproj, float* __restrict__ f, const float* __restrict__ norm) {
-    const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (row >= nrows) return;  // warp-uniform
-    const uint64_t s = rowptr[row], t = rowptr[row + 1];
-    const uint64_t meta = rowmeta[row];
-    uint32_t carry_col = (uint32_t)meta;          // column before the next round
-    uint64_t esc_next = meta >> 32;               // esc[] index of the next escape
-    const uint64_t v1 = (t + 7) >> 3;
+k_csr_d16(const uint64_t* __restrict__ dvptr, const uint32_t* __restrict__ dbase, const uint16_t* __restrict__ d16,
+          const V* __restrict__ dval, const float* __restrict__ x, uint32_t nrows, const int32_t* __restrict__ g,
+          float* __restrict__ out, float* __restrict__ fwproj, float* __restrict__ f, const float* __restrict__ norm) {
+    const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) / LPR;
+    const uint32_t gl = threadIdx.x % LPR;
+    const bool live = row < nrows;
+    const uint64_t v0 = live ? dvptr[row] : 0, v1 = live ? dvptr[row + 1] : 0;
+    const uint32_t nsteps = (uint32_t)((v1 - v0) / LPR);
+    const uint4* dv = reinterpret_cast<const uint4*>(d16);
+    if (live && gl == 0 && v1 > v0) {
+        // the row's vectors into L2 ahead of the loads (whole 16-byte vectors)
+        const uint64_t lo = reinterpret_cast<uint64_t>(dv + v0), nb = 16 * (v1 - v0);
+        const uint64_t lv = reinterpret_cast<uint64_t>(dval) + 8 * sizeof(V) * v0, nv = 8 * sizeof(V) * (v1 - v0);
+        for (uint64_t q = 0; q < nb; q += 65536)
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo + q),
+                         "r"((uint32_t)(nb - q < 65536 ? nb - q : 65536)) : "memory");
+        for (uint64_t q = 0; q < nv; q += 65536)
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lv + q),
+                         "r"((uint32_t)(nv - q < 65536 ? nv - q : 65536)) : "memory");
+    }
+    uint32_t prev = live ? dbase[row] : 0u;  // column of this lane's previous element
     float acc = 0.f;
-    for (uint64_t vb = s >> 3; vb < v1; vb += 32) {
-        const uint64_t v = vb + lane;
-        const bool have = v < v1;
-        uint32_t dw[4] = {0, 0, 0, 0};
-        float a[8];
-        if (have) {
-            const uint4 u = __ldcs(reinterpret_cast<const uint4*>(d16) + v);
-            dw[0] = u.x; dw[1] = u.y; dw[2] = u.z; dw[3] = u.w;
-            Val8<V>::load(val, v, a);
-        }
-        uint32_t d[8];
-        bool ok[8];
-        uint32_t nesc = 0, sum = 0;
-        bool reset = false;
+    for (uint32_t k = 0; k < nsteps; k += U) {
+        uint4 dw[U];
+        float a[U][8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            d[j] = (dw[j >> 1] >> (16 * (j & 1))) & 0xFFFFu;
-            const uint64_t e = (v << 3) + j;
-            ok[j] = have && e >= s && e < t;
-            if (ok[j]) {
-                if (d[j] == kEsc) {
-                    ++nesc;
-                    reset = true;
-                    sum = 0;
-                } else {
-                    sum += d[j];
-                }
+        for (int u = 0; u < U; ++u) {
+            if (k + u < nsteps) {
+                const uint64_t v = v0 + (uint64_t)(k + u) * LPR + gl;
+                dw[u] = __ldcs(dv + v);
+                Val8<V>::load(dval, v, a[u]);
+            } else {
+                dw[u] = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) a[u][j] = 0.f;
             }
         }
-        // escape ordinals: exclusive scan of the per-lane escape counts
-        uint32_t incl_n = nesc;
+        uint32_t col[U][8];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl_n, o);
-            if (lane >= o) incl_n += y;
-        }
-        const uint64_t my_esc = esc_next + (incl_n - nesc);
-        const uint32_t round_esc = __shfl_sync(0xffffffffu, incl_n, 31);
-        // column after this lane's vector: last escape value + deltas after it
-        uint32_t cv = sum;
-        if (reset) cv = esc[my_esc + nesc - 1] + sum;
-        // inclusive scan with resets: (r1, c1) then (r2, c2) -> r2 ? c2 : c1 + c2
-        bool sr = reset;
-        uint32_t sc = cv;
+        for (int u = 0; u < U; ++u) {
+            const uint32_t w[4] = {dw[u].x, dw[u].y, dw[u].z, dw[u].w};
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t yc = __shfl_up_sync(0xffffffffu, sc, o);
-            const bool yr = __shfl_up_sync(0xffffffffu, sr ? 1u : 0u, o) != 0;
-            if (lane >= o && !sr) {
-                sc = yc + sc;
-                sr = yr;
+            for (int j = 0; j < 8; ++j) {
+                prev += (w[j >> 1] >> (16 * (j & 1))) & 0xFFFFu;
+                col[u][j] = prev;
             }
         }
-        // column before this lane's vector
-        uint32_t pc = __shfl_up_sync(0xffffffffu, sc, 1);
-        const bool pr = __shfl_up_sync(0xffffffffu, sr ? 1u : 0u, 1) != 0;
-        uint32_t col = (lane == 0) ? carry_col : (pr ? pc : carry_col + pc);
-        // next round's carry from lane 31
-        const uint32_t c31 = __shfl_sync(0xffffffffu, sc, 31);
-        const bool r31 = __shfl_sync(0xffffffffu, sr ? 1u : 0u, 31) != 0;
-        // decode, gather, accumulate
-        uint32_t cols[8];
-        uint64_t k = my_esc;
+        float gx[U][8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            if (ok[j]) col = (d[j] == kEsc) ? esc[k++] : col + d[j];
-            cols[j] = col;
-        }
-        float gx[8];
+        for (int u = 0; u < U; ++u)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) gx[j] = ok[j] ? __ldg(x + cols[j]) : 0.f;
+            for (int j = 0; j < 8; ++j) gx[u][j] = (k + u < nsteps) ? __ldg(x + col[u][j]) : 0.f;
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if (ok[j]) acc = fmaf(a[j], gx[j], acc);
-        carry_col = r31 ? c31 : carry_col + c31;
-        esc_next += round_esc;
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc = fmaf(a[u][j], gx[u][j], acc);
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) {
+    for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, LPR);
+    if (live && gl == 0) {
         if (EPI == (int)Epi::Correl) {
             out[row] = (acc != 0.0f) ? __fdiv_rn((float)g[row], acc) : 0.0f;
             if (fwproj) fwproj[row] = acc;
@@ -176,68 +145,81 @@ k_csr_d16(const uint64_t* __restrict__ rowptr, const uint64_t* __restrict__ rowm
 }
 
 // ---------------------------------------------------------------- conversion
-__device__ __forceinline__ bool is_escape(const uint32_t* __restrict__ col, uint64_t e, uint64_t s) {
-    if (e == s) return false;
-    const uint32_t a = col[e - 1], b = col[e];
-    return b < a || b - a >= kEsc;
-}
-
-__global__ void k_d16_count(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ col, uint32_t rows,
-                            uint32_t* __restrict__ cnt) {
-    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Sets *unsorted when some row lists a column below its predecessor.
+__global__ void k_d16_check(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ col, uint32_t rows,
+                            int* __restrict__ unsorted) {
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t r = wid; r < rows; r += nw) {
+    for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += nw) {
         const uint64_t s = rowptr[r], t = rowptr[r + 1];
-        uint32_t n = 0;
-        for (uint64_t e = s + lane; e < t; e += 32) n += is_escape(col, e, s) ? 1u : 0u;
+        bool bad = false;
+        for (uint64_t e = s + 1 + lane; e < t; e += 32) bad |= col[e] < col[e - 1];
+        if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(unsorted, 1);
+    }
+}
+
+// Walks row r's positions: a dummy wherever the next column is 65,536 or more
+// past the column L positions earlier.  emit(p, delta, e) for every position
+// (e = entry index, or ~0 for a dummy); returns the positions used.
+template <int L, class Emit>
+__device__ __forceinline__ uint64_t d16_walk(const uint32_t* __restrict__ col, uint64_t s, uint64_t t, Emit&& emit) {
+    if (s == t) return 0;
+    uint32_t ring[L];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
-        if (lane == 0) cnt[r] = n;
-    }
-}
-
-__global__ void k_d16_fill(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ col, uint32_t rows,
-                           const uint64_t* __restrict__ escptr, uint64_t* __restrict__ rowmeta,
-                           uint16_t* __restrict__ d16, uint32_t* __restrict__ esc) {
-    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t r = wid; r < rows; r += nw) {
-        const uint64_t s = rowptr[r], t = rowptr[r + 1];
-        uint64_t k = escptr[r];
-        if (lane == 0) rowmeta[r] = (uint64_t)(s < t ? col[s] : 0u) | (k << 32);
-        for (uint64_t b = s; b < t; b += 32) {
-            const uint64_t e = b + lane;
-            const bool in = e < t;
-            const bool x = in && is_escape(col, e, s);
-            const unsigned bal = __ballot_sync(0xffffffffu, x);
-            if (in) {
-                if (x) {
-                    d16[e] = kEsc;
-                    esc[k + __popc(bal & ((1u << lane) - 1u))] = col[e];
-                } else {
-                    d16[e] = (uint16_t)(e == s ? 0u : col[e] - col[e - 1]);
-                }
-            }
-            k += __popc(bal);
+    for (int i = 0; i < L; ++i) ring[i] = col[s];
+    uint64_t p = 0;
+    for (uint64_t e = s; e < t;) {
+        uint32_t earlier = ring[0];
+#pragma unroll
+        for (int i = 1; i < L; ++i)
+            if ((p % L) == (uint64_t)i) earlier = ring[i];
+        const uint32_t c = col[e];
+        uint32_t now, d;
+        uint64_t ent;
+        if (c - earlier >= 65536u) {
+            now = earlier + 65535u;
+            d = 65535u;
+            ent = ~0ull;
+        } else {
+            now = c;
+            d = c - earlier;
+            ent = e;
+            ++e;
         }
+        emit(p, d, ent);
+#pragma unroll
+        for (int i = 0; i < L; ++i)
+            if ((p % L) == (uint64_t)i) ring[i] = now;
+        ++p;
+    }
+    return p;
+}
+
+// Vectors per row (positions rounded up to whole steps of 8·L).  One thread per row.
+template <int L>
+__global__ void k_d16_count(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ col, uint32_t rows,
+                            uint32_t* __restrict__ nvec) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        const uint64_t n = d16_walk<L>(col, rowptr[r], rowptr[r + 1], [](uint64_t, uint32_t, uint64_t) {});
+        nvec[r] = (uint32_t)((n + 8 * L - 1) / (8 * L) * L);
     }
 }
 
-template <typename V, int EPI>
-void d16_launch(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
-    launch_ex(k_csr_d16<V, EPI>, dim3(ceil_div_u((uint64_t)op.nrows * 32, 256)), dim3(256), 0, s, win, op.rowptr,
-              op.rowmeta, op.d16, static_cast<const V*>(op.val), op.esc, x, op.nrows, e.g, e.out, e.fwproj, e.f,
-              e.norm);
-}
-
-template <typename V>
-void d16_dispatch(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
-    switch (e.kind) {
-        case Epi::Correl: d16_launch<V, (int)Epi::Correl>(op, x, e, win, s); break;
-        case Epi::Update: d16_launch<V, (int)Epi::Update>(op, x, e, win, s); break;
-        default: d16_launch<V, (int)Epi::Raw>(op, x, e, win, s);
+// Deltas and values at their positions (the arrays are zeroed beforehand,
+// which is the padding).  One thread per row.
+template <typename V, int L>
+__global__ void k_d16_fill(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ col,
+                           const V* __restrict__ val, uint32_t rows, const uint64_t* __restrict__ dvptr,
+                           uint32_t* __restrict__ dbase, uint16_t* __restrict__ d16, V* __restrict__ dval) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        const uint64_t s = rowptr[r], t = rowptr[r + 1], v0 = dvptr[r];
+        dbase[r] = s < t ? col[s] : 0u;
+        d16_walk<L>(col, s, t, [&](uint64_t p, uint32_t d, uint64_t e) {
+            // position p: step p / (8L), lane p % L, element (p / L) % 8
+            const uint64_t v = v0 + (p / (8 * L)) * L + p % L, q = 8 * v + (p / L) % 8;
+            d16[q] = (uint16_t)d;
+            if (e != ~0ull) dval[q] = val[e];
+        });
     }
 }
 
@@ -245,45 +227,159 @@ unsigned grid_rows(uint32_t rows) {
     return std::max(1u, std::min<unsigned>(ceil_div_u((uint64_t)rows * 32, 256), 152u * 32u));
 }
 
-}  // namespace
+unsigned grid_threads(uint32_t rows) {
+    return std::max(1u, std::min<unsigned>(ceil_div_u(rows, 128), 152u * 32u));
+}
 
-void build_d16(DevCsr& op, cudaStream_t s) {
-    MLEM_REQUIRE(op.nnz < (1ull << 32), MLEM_EUNSUPPORTED, "D16 indices: nnz must be < 2^32");
-    uint32_t* cnt = nullptr;
-    uint64_t* escptr = nullptr;
-    const uint64_t R = std::max<uint32_t>(op.nrows, 1);
-    MLEM_CUDA(cudaMallocAsync(&cnt, sizeof(uint32_t) * R, s));
-    MLEM_CUDA(cudaMallocAsync(&escptr, sizeof(uint64_t) * (R + 1), s));
-    if (op.nrows) {
-        k_d16_count<<<grid_rows(op.nrows), 256, 0, s>>>(op.rowptr, op.idx, op.nrows, cnt);
-        MLEM_LAUNCHED();
-    }
-    scan_counts_u64(cnt, escptr, op.nrows, s);
-    uint64_t nesc = 0;
-    MLEM_CUDA(cudaMemcpyAsync(&nesc, escptr + op.nrows, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+template <typename V>
+void d16_fill(DevCsr& op, const uint32_t* idx, const void* val, cudaStream_t s) {
+    if (op.d16_lanes == 4)
+        k_d16_fill<V, 4><<<grid_threads(op.nrows), 128, 0, s>>>(op.rowptr, idx, static_cast<const V*>(val), op.nrows,
+                                                                op.dvptr, op.dbase, op.d16, static_cast<V*>(op.dval));
+    else
+        k_d16_fill<V, 8><<<grid_threads(op.nrows), 128, 0, s>>>(op.rowptr, idx, static_cast<const V*>(val), op.nrows,
+                                                                op.dvptr, op.dbase, op.d16, static_cast<V*>(op.dval));
+    MLEM_LAUNCHED();
+}
+
+// A copy of the operand's entries with every row sorted by column (stable),
+// made on the host: only for rows given out of order (generated and
+// transposed operands are sorted already).
+void sorted_copy(const DevCsr& op, uint32_t*& idx, void*& val, cudaStream_t s) {
+    const size_t vb = val_bytes(op.vt);
+    std::vector<uint64_t> rp(op.nrows + 1);
+    std::vector<uint32_t> c(op.nnz);
+    std::vector<unsigned char> v(op.nnz * vb);
+    MLEM_CUDA(cudaMemcpyAsync(rp.data(), op.rowptr, sizeof(uint64_t) * rp.size(), cudaMemcpyDeviceToHost, s));
+    MLEM_CUDA(cudaMemcpyAsync(c.data(), op.idx, sizeof(uint32_t) * op.nnz, cudaMemcpyDeviceToHost, s));
+    MLEM_CUDA(cudaMemcpyAsync(v.data(), op.val, vb * op.nnz, cudaMemcpyDeviceToHost, s));
     MLEM_CUDA(cudaStreamSynchronize(s));
-    op.nesc = nesc;
-    MLEM_CUDA(cudaMalloc(&op.rowmeta, sizeof(uint64_t) * R));
-    MLEM_CUDA(cudaMalloc(&op.d16, sizeof(uint16_t) * padded(op.nnz)));
-    MLEM_CUDA(cudaMalloc(&op.esc, sizeof(uint32_t) * std::max<uint64_t>(nesc, 1)));
-    MLEM_CUDA(cudaMemsetAsync(op.d16, 0, sizeof(uint16_t) * padded(op.nnz), s));
-    if (op.nrows) {
-        k_d16_fill<<<grid_rows(op.nrows), 256, 0, s>>>(op.rowptr, op.idx, op.nrows, escptr, op.rowmeta, op.d16,
-                                                       op.esc);
-        MLEM_LAUNCHED();
+    std::vector<uint32_t> c2(op.nnz);
+    std::vector<unsigned char> v2(op.nnz * vb);
+#pragma omp parallel
+    {
+        std::vector<uint64_t> perm;
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t r = 0; r < (int64_t)op.nrows; ++r) {
+            const uint64_t a = rp[r], b = rp[r + 1];
+            perm.resize(b - a);
+            for (uint64_t e = a; e < b; ++e) perm[e - a] = e;
+            std::stable_sort(perm.begin(), perm.end(), [&](uint64_t x, uint64_t y) { return c[x] < c[y]; });
+            for (uint64_t k = 0; k < b - a; ++k) {
+                c2[a + k] = c[perm[k]];
+                std::memcpy(&v2[(a + k) * vb], &v[perm[k] * vb], vb);
+            }
+        }
     }
-    MLEM_CUDA(cudaFreeAsync(cnt, s));
-    MLEM_CUDA(cudaFreeAsync(escptr, s));
+    MLEM_CUDA(cudaMalloc(&idx, sizeof(uint32_t) * std::max<uint64_t>(op.nnz, 1)));
+    MLEM_CUDA(cudaMalloc(&val, vb * std::max<uint64_t>(op.nnz, 1)));
+    MLEM_CUDA(cudaMemcpyAsync(idx, c2.data(), sizeof(uint32_t) * op.nnz, cudaMemcpyHostToDevice, s));
+    MLEM_CUDA(cudaMemcpyAsync(val, v2.data(), vb * op.nnz, cudaMemcpyHostToDevice, s));
     MLEM_CUDA(cudaStreamSynchronize(s));
 }
 
-void launch_csr_d16(const DevCsr& op, const float* x, const EpiArgs& epi, L2Window win, cudaStream_t s) {
+template <typename V, int EPI, int LPR, int U>
+void d16_launch(const DevCsr& op, const float* x, const EpiArgs& e, L2Window win, cudaStream_t s) {
+    launch_ex(k_csr_d16<V, EPI, LPR, U>, dim3(ceil_div_u((uint64_t)op.nrows * LPR, 256)), dim3(256), 0, s, win,
+              op.dvptr, op.dbase, op.d16, static_cast<const V*>(op.dval), x, op.nrows, e.g, e.out, e.fwproj, e.f,
+              e.norm);
+}
+
+template <typename V, int EPI>
+void d16_shape(const DevCsr& op, const float* x, const EpiArgs& e, int unroll, L2Window win, cudaStream_t s) {
+    if (op.d16_lanes == 4) {
+        if (unroll >= 2) d16_launch<V, EPI, 4, 2>(op, x, e, win, s);
+        else d16_launch<V, EPI, 4, 1>(op, x, e, win, s);
+    } else {
+        if (unroll >= 2) d16_launch<V, EPI, 8, 2>(op, x, e, win, s);
+        else d16_launch<V, EPI, 8, 1>(op, x, e, win, s);
+    }
+}
+
+template <typename V>
+void d16_dispatch(const DevCsr& op, const float* x, const EpiArgs& e, int unroll, L2Window win, cudaStream_t s) {
+    switch (e.kind) {
+        case Epi::Correl: d16_shape<V, (int)Epi::Correl>(op, x, e, unroll, win, s); break;
+        case Epi::Update: d16_shape<V, (int)Epi::Update>(op, x, e, unroll, win, s); break;
+        default: d16_shape<V, (int)Epi::Raw>(op, x, e, unroll, win, s);
+    }
+}
+
+}  // namespace
+
+void build_d16(DevCsr& op, cudaStream_t s) {
+    const uint64_t R = std::max<uint32_t>(op.nrows, 1);
+    // 4 lanes per row for short rows, 8 for long ones (the padding to whole
+    // steps of 8 L entries costs less than 10% either way)
+    op.d16_lanes = op.nrows && op.nnz / op.nrows >= 256 ? 8 : 4;
+    // deltas need every row in ascending column order
+    const uint32_t* idx = op.idx;
+    const void* val = op.val;
+    uint32_t* sidx = nullptr;
+    void* sval = nullptr;
+    int* flag = nullptr;
+    int unsorted = 0;
+    MLEM_CUDA(cudaMallocAsync(&flag, sizeof(int), s));
+    MLEM_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+    if (op.nrows) {
+        k_d16_check<<<grid_rows(op.nrows), 256, 0, s>>>(op.rowptr, op.idx, op.nrows, flag);
+        MLEM_LAUNCHED();
+    }
+    MLEM_CUDA(cudaMemcpyAsync(&unsorted, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MLEM_CUDA(cudaFreeAsync(flag, s));
+    MLEM_CUDA(cudaStreamSynchronize(s));
+    if (unsorted) {
+        sorted_copy(op, sidx, sval, s);
+        idx = sidx;
+        val = sval;
+    }
+    uint32_t* nvec = nullptr;
+    try {
+        MLEM_CUDA(cudaMallocAsync(&nvec, sizeof(uint32_t) * R, s));
+        MLEM_CUDA(cudaMalloc(&op.dvptr, sizeof(uint64_t) * (R + 1)));
+        if (op.nrows) {
+            if (op.d16_lanes == 4) k_d16_count<4><<<grid_threads(op.nrows), 128, 0, s>>>(op.rowptr, idx, op.nrows, nvec);
+            else k_d16_count<8><<<grid_threads(op.nrows), 128, 0, s>>>(op.rowptr, idx, op.nrows, nvec);
+            MLEM_LAUNCHED();
+        }
+        scan_counts_u64(nvec, op.dvptr, op.nrows, s);
+        uint64_t nv = 0;
+        MLEM_CUDA(cudaMemcpyAsync(&nv, op.dvptr + op.nrows, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        MLEM_CUDA(cudaStreamSynchronize(s));
+        op.dvec = nv;
+        const uint64_t slots = 8 * std::max<uint64_t>(nv, 1);
+        MLEM_CUDA(cudaMalloc(&op.dbase, sizeof(uint32_t) * R));
+        MLEM_CUDA(cudaMalloc(&op.d16, sizeof(uint16_t) * slots));
+        MLEM_CUDA(cudaMalloc(&op.dval, val_bytes(op.vt) * slots));
+        MLEM_CUDA(cudaMemsetAsync(op.d16, 0, sizeof(uint16_t) * slots, s));
+        MLEM_CUDA(cudaMemsetAsync(op.dval, 0, val_bytes(op.vt) * slots, s));
+        if (op.nrows) {
+            switch (op.vt) {
+                case MLEM_VAL_F32: d16_fill<float>(op, idx, val, s); break;
+                case MLEM_VAL_F16: d16_fill<__half>(op, idx, val, s); break;
+                default: d16_fill<__nv_bfloat16>(op, idx, val, s);
+            }
+        }
+        MLEM_CUDA(cudaStreamSynchronize(s));
+    } catch (...) {
+        cudaStreamSynchronize(s);
+        cudaFree(nvec);
+        cudaFree(sidx);
+        cudaFree(sval);
+        throw;
+    }
+    cudaFree(nvec);
+    cudaFree(sidx);
+    cudaFree(sval);
+}
+
+void launch_csr_d16(const DevCsr& op, const float* x, const EpiArgs& epi, int unroll, L2Window win, cudaStream_t s) {
     if (op.nrows == 0) return;
     MLEM_REQUIRE(op.d16 != nullptr, MLEM_EINVAL, "operand has no D16 indices");
     switch (op.vt) {
-        case MLEM_VAL_F32: d16_dispatch<float>(op, x, epi, win, s); break;
-        case MLEM_VAL_F16: d16_dispatch<__half>(op, x, epi, win, s); break;
-        default: d16_dispatch<__nv_bfloat16>(op, x, epi, win, s);
+        case MLEM_VAL_F32: d16_dispatch<float>(op, x, epi, unroll, win, s); break;
+        case MLEM_VAL_F16: d16_dispatch<__half>(op, x, epi, unroll, win, s); break;
+        default: d16_dispatch<__nv_bfloat16>(op, x, epi, unroll, win, s);
     }
 }
 
