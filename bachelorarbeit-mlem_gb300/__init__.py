@@ -59,7 +59,9 @@ class MatrixInfo(C.Structure):
                 ("value_type", C.c_int), ("has_transpose", C.c_uint32), ("device_bytes", C.c_uint64),
                 ("max_row_nnz", C.c_uint32), ("max_col_nnz", C.c_uint32),
                 ("sym_lor_rows", C.c_uint32), ("sym_voxel_rows", C.c_uint32),
-                ("sym_fp_nnz", C.c_uint64), ("sym_bp_nnz", C.c_uint64)]
+                ("sym_fp_nnz", C.c_uint64), ("sym_bp_nnz", C.c_uint64),
+                ("d16_slots", C.c_uint64), ("d16_slots_t", C.c_uint64),
+                ("d16_lanes", C.c_uint32), ("d16_lanes_t", C.c_uint32)]
 
 
 class RunOpts(C.Structure):
@@ -283,6 +285,8 @@ class Matrix:
         self.max_row_nnz, self.max_col_nnz = info.max_row_nnz, info.max_col_nnz
         self.symmetry = {"lor_rows": info.sym_lor_rows, "voxel_rows": info.sym_voxel_rows,
                          "fp_nnz": info.sym_fp_nnz, "bp_nnz": info.sym_bp_nnz} if info.sym_lor_rows else None
+        self.d16 = {"slots": info.d16_slots, "slots_t": info.d16_slots_t, "lanes": info.d16_lanes,
+                    "lanes_t": info.d16_lanes_t} if info.d16_slots else None
 
     # construction ---------------------------------------------------------
     @staticmethod

@@ -887,6 +887,10 @@ mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info) {
         info->sym_voxel_rows = m->sym.J;
         info->sym_fp_nnz = m->sym.fp_nnz;
         info->sym_bp_nnz = m->sym.bp_nnz;
+        info->d16_slots = 8 * m->A.dvec;
+        info->d16_slots_t = m->has_t ? 8 * m->AT.dvec : 0;
+        info->d16_lanes = (uint32_t)m->A.d16_lanes;
+        info->d16_lanes_t = m->has_t ? (uint32_t)m->AT.d16_lanes : 0;
     });
 }
 

@@ -73,10 +73,23 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def algorithmic_bytes(rows, cols, nnz, sv):
-    """Per-launch algorithmic bytes of the two kernels of an iteration."""
+# kernel of each autotuner choice
+KERNEL_NAMES = {"direct": "k_csrvec", "persistent": "k_csrvec_pipe", "tma": "k_csr_tma", "d16": "k_csr_d16",
+                "ilv": "k_csr_ilv", "sym": "k_sym_orbit"}
+
+
+def algorithmic_bytes(rows, cols, nnz, sv, m=None):
+    """Per-launch algorithmic bytes of the two kernels of an iteration.  With m
+    given and an operand tuned to its D16 copy, that operand is counted as its
+    stored entries (2 index bytes + sv each, dummies and padding included) and
+    its vector pointers and base columns."""
     fp = nnz * (sv + 4) + 8 * (rows + 1) + 4 * cols + 4 * rows + 4 * rows   # A, rowptr, x once, g, ratio
     bp = nnz * (sv + 4) + 8 * (cols + 1) + 4 * rows + 12 * cols             # Aᵀ, colptr, ratio once, norm, f r/w
+    if m is not None and m.d16:
+        if m.tuning(False)["kernel"] == "d16":
+            fp = m.d16["slots"] * (sv + 2) + 12 * rows + 8 + 4 * cols + 4 * rows + 4 * rows
+        if m.tuning(True)["kernel"] == "d16":
+            bp = m.d16["slots_t"] * (sv + 2) + 12 * cols + 8 + 4 * rows + 12 * cols
     return fp, bp
 
 
@@ -372,8 +385,15 @@ def run_forms(pkg, torch, args):
     f0_dev = torch.from_numpy(f0).cuda()
     f_dev = torch.empty_like(f0_dev)
     kt16 = time_kernels(pkg, m16, torch, g, f0)
+    fb, bb = algorithmic_bytes(m16.rows, m16.cols, m16.nnz, 2, m16)
+    pk, pkind = peaks()
     res["fp16_kernels"] = {"fp_ms": kt16["fp"], "bp_ms": kt16["bp"], "fp": m16.tuning(False), "bp": m16.tuning(True),
-                           "device_bytes": m16.device_bytes}
+                           "device_bytes": m16.device_bytes, "d16": m16.d16,
+                           "roofline": {"fp_bytes": fb, "bp_bytes": bb, "peak": pk, "peak_kind": pkind,
+                                        "fp_gbs": fb / (kt16["fp"] * 1e-3) / 1e9,
+                                        "bp_gbs": bb / (kt16["bp"] * 1e-3) / 1e9,
+                                        "fp_frac": fb / (kt16["fp"] * 1e-3) / 1e9 / pk,
+                                        "bp_frac": bb / (kt16["bp"] * 1e-3) / 1e9 / pk}}
     # each variant with its default lanes / vectors in flight (the tuned choice is above)
     variants = {}
     for label, kern in (("direct", pkg.KERNEL_DIRECT), ("ilv", pkg.KERNEL_ILV), ("d16", pkg.KERNEL_D16)):
@@ -592,6 +612,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--spmv", default="csr-vector", choices=["csr-vector", "merge"],
                     help="SpMV of the timed reconstruction (the reference's argv[8])")
+    ap.add_argument("--values", default="f32", choices=["f32", "f16", "bf16"],
+                    help="value type of the timed matrix (f32: the plain path; FP32 accumulation always)")
+    ap.add_argument("--compress", action="store_true",
+                    help="also build the 16-bit delta-coded index copy (D16) of the timed matrix for the autotuner")
     ap.add_argument("--layout", default="locality", choices=["natural", "locality"],
                     help="device layout of the generated matrices (rows in LOR tubes, columns in voxel bricks)")
     ap.add_argument("--bp", default="trans", choices=["trans", "scatter", "fused"],
@@ -612,7 +636,10 @@ def main():
     pkg = load_pkg()
     name = args.workload
     iters = WORKLOADS[name]["iters"]
-    m, geo, g, t_gen = make_problem(pkg, name, torch, interleave=not args.no_interleave)
+    vt = {"f32": pkg.VAL_F32, "f16": pkg.VAL_F16, "bf16": pkg.VAL_BF16}[args.values]
+    sv = 4 if args.values == "f32" else 2
+    m, geo, g, t_gen = make_problem(pkg, name, torch, value_type=vt, compress=args.compress,
+                                    interleave=not args.no_interleave)
     s = torch.cuda.current_stream()
     g_dev = torch.from_numpy(g).cuda()
     f0 = np.full(m.cols, m.initial_value(g), np.float32)
@@ -621,7 +648,7 @@ def main():
 
     SPMV = 0 if args.spmv == "merge" else 1
     BP = {"trans": 0, "scatter": 1, "fused": 2}[args.bp]
-    default_form = SPMV == 1 and BP == 0
+    default_form = SPMV == 1 and BP == 0 and args.values == "f32" and not args.compress
 
     def step():
         f_dev.copy_(f0_dev)
@@ -681,7 +708,7 @@ def main():
     kt_direct = time_kernels(pkg, m, torch, g, f0, kernel=0)
     kt_tma = time_kernels(pkg, m, torch, g, f0, kernel=1)
     kt_pers = time_kernels(pkg, m, torch, g, f0, kernel=2)
-    fp_b, bp_b = algorithmic_bytes(m.rows, m.cols, m.nnz, 4)
+    fp_b, bp_b = algorithmic_bytes(m.rows, m.cols, m.nnz, sv, m)
     dom = "fp" if kt["fp"] >= kt["bp"] else "bp"
     dom_bytes = fp_b if dom == "fp" else bp_b
     peak, peak_kind = peaks()
@@ -696,18 +723,23 @@ def main():
     line = {
         "metric": "MLEM iterations/s", "value": value, "unit": "iter/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.values == "f32" else f"{args.values} values, f32 accumulation",
         "data": "synthetic (seeded multi-ray Siddon matrix, ellipsoid phantom, Poisson sinogram)",
         "config": {"workload": name, "rows": m.rows, "cols": m.cols, "nnz": m.nnz, "iterations_per_step": iters,
-                   "form": f"fp32 plain: {args.spmv} SpMV, {args.bp} BP, {args.layout} layout",
+                   "form": (f"fp32 plain: {args.spmv} SpMV, {args.bp} BP, {args.layout} layout"
+                            if args.values == "f32" and not args.compress else
+                            f"{args.values} values{', D16 indices' if args.compress else ''}: {args.spmv} SpMV, "
+                            f"{args.bp} BP, {args.layout} layout"),
                    "l2": "inputs larger than L2 "
                    f"({(m.device_bytes) / 1e9:.1f} GB resident matrix)", "replicas": world,
                    "matrix_generation_s": round(t_gen, 2)},
         "e2e": {"value": e2e_value, "unit": "iter/s", "h2d_bytes_per_step": int(4 * m.rows + 4 * m.cols),
                 "d2h_bytes_per_step": int(4 * m.cols)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "k_csrvec (FP, fused correlation)" if dom == "fp"
-                     else "k_csrvec (BP over Aᵀ, fused update)", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES.get(m.tuning(dom == "bp")["kernel"], "k_csrvec") + " "
+                     + ("(FP, fused correlation)" if dom == "fp" else "(BP over Aᵀ, fused update)"),
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes": dom_bytes, "kernel_ms": kt[dom],
                      "iteration": {"bytes": iter_bytes, "ms": ms / args.steps / iters,

@@ -140,6 +140,11 @@ typedef struct {
      * rows of the two compact operands) and the entries of each operand */
     uint32_t sym_lor_rows, sym_voxel_rows;
     uint64_t sym_fp_nnz, sym_bp_nnz;
+    /* compress_indices = 1 only (else 0): stored entries of the D16 copies of
+     * A and of Aᵀ (nonzeros + dummies + padding; 2 bytes of index and one
+     * value each) and the lanes per row their layout is built for */
+    uint64_t d16_slots, d16_slots_t;
+    uint32_t d16_lanes, d16_lanes_t;
 } mlem_matrix_info;
 
 mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info);

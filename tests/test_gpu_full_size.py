@@ -1,6 +1,6 @@
 """Full-size accuracy: the 3-D mid matrix (208 M nonzeros) and the 12 GB-class
 matrix (1.43 B nonzeros), 100 MLEM iterations, FP32 values and FP16 values
-(FP32 accumulation), against the FP64 oracle (back projection over Aᵀ, OpenMP)
+with 16-bit delta-coded indices (FP32 accumulation), against the FP64 oracle (back projection over Aᵀ, OpenMP)
 on the FP32 matrix.  Bars: image relative L2 1e-5 (FP32) and 1e-3 (FP16);
 log-likelihood relative error 1e-6 (FP32) and 1e-4 (FP16).  The measured
 errors are printed (run with -s to see them)."""
@@ -36,8 +36,11 @@ def test_full_size_fp32_and_fp16_against_fp64_oracle(pkg, O, cuda, name):
     m.close()
     ref, llref = O.mlem_f64_t(A, AT, g, norm, f0, iters, loglik=True)
     del A, AT
-    m16 = pkg.Matrix.generate(geo, value_type=pkg.VAL_F16)
+    # FP16 values with 16-bit delta-coded indices (the compact precision form;
+    # the autotuner picks among the csr-vector, interleaved and D16 kernels)
+    m16 = pkg.Matrix.generate(geo, value_type=pkg.VAL_F16, compress=True)
     img16, ll16 = m16.run(g, iters, f0=f0, loglik=True)
+    print(f"\n{name}: FP16 kernels {m16.tuning(False)['kernel']} / {m16.tuning(True)['kernel']}")
     m16.close()
     e32, e16 = O.rel_l2(img32, ref), O.rel_l2(img16, ref)
     l32 = float(np.max(np.abs(ll32 - llref) / np.abs(llref)))
