@@ -78,17 +78,19 @@ KERNEL_NAMES = {"direct": "k_csrvec", "persistent": "k_csrvec_pipe", "tma": "k_c
                 "ilv": "k_csr_ilv", "sym": "k_sym_orbit"}
 
 
-def algorithmic_bytes(rows, cols, nnz, sv, m=None):
+def algorithmic_bytes(rows, cols, nnz, sv, m=None, kinds=None):
     """Per-launch algorithmic bytes of the two kernels of an iteration.  With m
-    given and an operand tuned to its D16 copy, that operand is counted as its
-    stored entries (2 index bytes + sv each, dummies and padding included) and
-    its vector pointers and base columns."""
+    given and an operand run on its D16 copy (kinds = the FP and BP kernel
+    names, else the autotuner's choices), that operand is counted as its stored
+    entries (2 index bytes + sv each, dummies and padding included) and its
+    vector pointers and base columns."""
     fp = nnz * (sv + 4) + 8 * (rows + 1) + 4 * cols + 4 * rows + 4 * rows   # A, rowptr, x once, g, ratio
     bp = nnz * (sv + 4) + 8 * (cols + 1) + 4 * rows + 12 * cols             # Aᵀ, colptr, ratio once, norm, f r/w
     if m is not None and m.d16:
-        if m.tuning(False)["kernel"] == "d16":
+        kinds = kinds or (m.tuning(False)["kernel"], m.tuning(True)["kernel"])
+        if kinds[0] == "d16":
             fp = m.d16["slots"] * (sv + 2) + 12 * rows + 8 + 4 * cols + 4 * rows + 4 * rows
-        if m.tuning(True)["kernel"] == "d16":
+        if kinds[1] == "d16":
             bp = m.d16["slots_t"] * (sv + 2) + 12 * cols + 8 + 4 * rows + 12 * cols
     return fp, bp
 
@@ -614,6 +616,9 @@ def main():
                     help="SpMV of the timed reconstruction (the reference's argv[8])")
     ap.add_argument("--values", default="f32", choices=["f32", "f16", "bf16"],
                     help="value type of the timed matrix (f32: the plain path; FP32 accumulation always)")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "direct", "d16", "ilv", "tma", "persistent"],
+                    help="csr-vector kernel of the timed path (auto: the autotuner's choice per operand; a fixed "
+                         "choice keeps profiled runs on the same kernel as plain ones)")
     ap.add_argument("--compress", action="store_true",
                     help="also build the 16-bit delta-coded index copy (D16) of the timed matrix for the autotuner")
     ap.add_argument("--layout", default="locality", choices=["natural", "locality"],
@@ -648,11 +653,14 @@ def main():
 
     SPMV = 0 if args.spmv == "merge" else 1
     BP = {"trans": 0, "scatter": 1, "fused": 2}[args.bp]
-    default_form = SPMV == 1 and BP == 0 and args.values == "f32" and not args.compress
+    KERN = {"auto": pkg.KERNEL_AUTO, "direct": pkg.KERNEL_DIRECT, "d16": pkg.KERNEL_D16, "ilv": pkg.KERNEL_ILV,
+            "tma": pkg.KERNEL_TMA, "persistent": pkg.KERNEL_PERSISTENT}[args.kernel]
+    default_form = SPMV == 1 and BP == 0 and args.values == "f32" and not args.compress and args.kernel == "auto"
 
     def step():
         f_dev.copy_(f0_dev)
-        m.run_device(g_dev.data_ptr(), f_dev.data_ptr(), iters, stream=s.cuda_stream, spmv=SPMV, bp_mode=BP)
+        m.run_device(g_dev.data_ptr(), f_dev.data_ptr(), iters, stream=s.cuda_stream, spmv=SPMV, bp_mode=BP,
+                     kernel=KERN)
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -682,7 +690,7 @@ def main():
     out_pin = torch.empty(m.cols, dtype=torch.float32).pin_memory()
     import ctypes as C
     lib = pkg.load_library()
-    ro = pkg.Matrix.run_opts(spmv=SPMV, bp_mode=BP)
+    ro = pkg.Matrix.run_opts(spmv=SPMV, bp_mode=BP, kernel=KERN)
 
     def e2e_step():
         st = lib.mlem_run(m.handle, C.c_void_p(g_pin.data_ptr()), C.c_void_p(f0_pin.data_ptr()), iters,
@@ -704,11 +712,12 @@ def main():
     e2e_value = world * args.steps * iters / float(te.item())
 
     # roofline of the dominant kernel
-    kt = time_kernels(pkg, m, torch, g, f0, spmv=SPMV, bp_mode=BP)
+    kt = time_kernels(pkg, m, torch, g, f0, spmv=SPMV, bp_mode=BP, kernel=KERN)
     kt_direct = time_kernels(pkg, m, torch, g, f0, kernel=0)
     kt_tma = time_kernels(pkg, m, torch, g, f0, kernel=1)
     kt_pers = time_kernels(pkg, m, torch, g, f0, kernel=2)
-    fp_b, bp_b = algorithmic_bytes(m.rows, m.cols, m.nnz, sv, m)
+    kinds = None if args.kernel == "auto" else (args.kernel, args.kernel)
+    fp_b, bp_b = algorithmic_bytes(m.rows, m.cols, m.nnz, sv, m, kinds)
     dom = "fp" if kt["fp"] >= kt["bp"] else "bp"
     dom_bytes = fp_b if dom == "fp" else bp_b
     peak, peak_kind = peaks()
@@ -737,7 +746,8 @@ def main():
         "e2e": {"value": e2e_value, "unit": "iter/s", "h2d_bytes_per_step": int(4 * m.rows + 4 * m.cols),
                 "d2h_bytes_per_step": int(4 * m.cols)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES.get(m.tuning(dom == "bp")["kernel"], "k_csrvec") + " "
+        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES.get(kinds[dom == "bp"] if kinds else
+                                                               m.tuning(dom == "bp")["kernel"], "k_csrvec") + " "
                      + ("(FP, fused correlation)" if dom == "fp" else "(BP over Aᵀ, fused update)"),
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
