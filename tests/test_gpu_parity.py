@@ -270,7 +270,8 @@ def test_device_generator_matches_host(pkg, name, stride):
 # ------------------------------------------------------- compressed indices
 @pytest.mark.parametrize("vt", [0, 1, 2])
 def test_d16_projection_matches_oracle(pkg, O, golden, cuda, vt):
-    # escapes: unsorted rows (rand_dup has repeated columns), large gaps (rand_long, one_row)
+    # rows out of order (rand_dup, with repeated columns) are sorted in the D16 copy; gaps of
+    # 65,536 or more columns (rand_long, one_row) are bridged by dummy entries
     for name in ("rand_small", "rand_long", "rand_dup", "one_row", "empty_rows", "tall", "cyl3d_tiny"):
         rp, c, v, cols = golden_csr(golden, name)
         m = pkg.Matrix.from_csr(rp, c, v, cols, value_type=vt, compress=True)
