@@ -414,6 +414,23 @@ def run_forms(pkg, torch, args):
         b.synchronize()
         res[label] = {"images_iterations_per_s": iters / (a.elapsed_time(b) * 1e-3)}
     m16.close()
+    # FP32 values with the same 16-bit delta-coded indices (lossless: the FP32 matrix)
+    m32d, _, g32, _ = make_problem(pkg, name, torch, value_type=pkg.VAL_F32, compress=True, interleave=False)
+    g32_dev = torch.from_numpy(g32).cuda()
+    f32_0 = torch.from_numpy(np.full(m32d.cols, m32d.initial_value(g32), np.float32)).cuda()
+    f32_dev = torch.empty_like(f32_0)
+    f32_dev.copy_(f32_0)
+    m32d.run_device(g32_dev.data_ptr(), f32_dev.data_ptr(), 5, stream=s.cuda_stream)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f32_dev.copy_(f32_0)
+    a.record(s)
+    m32d.run_device(g32_dev.data_ptr(), f32_dev.data_ptr(), iters, stream=s.cuda_stream)
+    b.record(s)
+    b.synchronize()
+    res["fp32_d16"] = {"iterations_per_s": iters / (a.elapsed_time(b) * 1e-3),
+                       "fp": m32d.tuning(False)["kernel"], "bp": m32d.tuning(True)["kernel"],
+                       "form": "FP32 values, 16-bit delta-coded indices (same matrix as the FP32 plain path)"}
+    m32d.close()
     # plain FP32 on the smaller matrices (the baselines of the batched and served forms)
     for small in ("cyl3d_mid", "ring2d"):
         msm, _, gs, _ = make_problem(pkg, small, torch, interleave=False)
