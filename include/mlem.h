@@ -80,8 +80,12 @@ typedef struct {
     const float* norm;          /* optional host sensitivity image f32[cols];
                                    NULL = computed on the GPU as Aᵀ1 in FP64 */
     int device;                 /* CUDA device ordinal (reference: GPU 0) */
-    uint32_t compress_indices;  /* 1: also keep 16-bit delta-coded column indices (2 B per
-                                   nonzero instead of 4) for the csr-vector projections */
+    uint32_t compress_indices;  /* 1: also keep a copy with 16-bit delta-coded column indices
+                                   (each entry: the difference to the column 4 or 8 entries
+                                   earlier in its row, plus its value; ~2.2 B of index per
+                                   nonzero instead of 4, dummies and padding included) for the
+                                   csr-vector projections (kernel D16, an autotuner candidate);
+                                   with FP16 values the fastest form for a stored matrix */
     uint32_t interleave;        /* 1: also keep a lane-interleaved copy (16-byte loads whose
                                    gathers cover consecutive columns) for the projections */
     uint32_t layout;            /* mlem_layout: device order of rows and columns */
@@ -201,7 +205,7 @@ typedef enum {
     MLEM_KERNEL_TMA = 1,
     MLEM_KERNEL_PERSISTENT = 2,
     MLEM_KERNEL_AUTO = 3, /* autotuned per matrix operand (lanes per row, vectors in flight, variant) */
-    MLEM_KERNEL_D16 = 4,  /* delta-compressed indices (matrix created with compress_indices = 1) */
+    MLEM_KERNEL_D16 = 4,  /* delta-coded indices (matrix created with compress_indices = 1) */
     MLEM_KERNEL_ILV = 5,  /* lane-interleaved copy (matrix created with interleave = 1) */
     MLEM_KERNEL_ORDERED = 6, /* DIRECT with rows in locality order (generated matrices:
                                LORs in 4x4 detector tubes, voxels in 4x2x2 bricks) */
