@@ -181,7 +181,8 @@ typedef struct {
                                    PERSISTENT 16 or 32); 0 = chosen from the mean row length */
     uint32_t unroll;            /* same kernels: vectors of 4 elements in flight per lane
                                    (1, 2, 4; PERSISTENT 1 or 2); 0 = 2.  SYM: entries in flight
-                                   per lane, 2 (1, 2), 4 or 8 (0, 8) */
+                                   per lane, 2 (1, 2), 4 or 8 (0, 8).  D16: vectors of 8
+                                   entries in flight per lane, 1 or 2 (0, 2) */
     uint32_t row_order;         /* DIRECT / PERSISTENT with 16 or 32 lanes: 1 = process the rows in
                                    the locality order of a generated matrix; SYM: 1 = the blocks that
                                    start together on an SM take neighbouring canonical rows */
