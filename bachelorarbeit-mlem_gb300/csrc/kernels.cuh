@@ -139,6 +139,10 @@ void launch_invert_perm(const uint32_t* map, uint32_t n, uint32_t* inv, cudaStre
 // unchanged), sorted; *keep_t (optional) receives the transpose of out.  f32.
 void remap_csr(const DevCsr& in, const uint32_t* row_src, const uint32_t* col_map, DevCsr& out, DevCsr* keep_t,
                cudaStream_t s);
+// Row order of a matrix without a detector numbering: rows sorted (stably) by
+// the coarse voxel cells of their lowest and highest column, empty rows last.
+// Returns the natural row of every internal row.
+std::vector<uint32_t> derived_lor_order(const DevCsr& A, uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t s);
 
 // ------------------------------------------------------------- symmetry.cu
 // Symmetry-compressed projection operands of a generated cylindrical scanner

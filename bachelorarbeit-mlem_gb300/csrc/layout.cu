@@ -11,6 +11,13 @@
 // the ratios of nearby LORs), which lowers the L1 line lookups per nonzero of
 // both projections.
 //
+// Rows of a matrix the library did not generate (no detector numbering to
+// build tubes from) are ordered from the matrix itself: by the coarse voxel
+// cells (about 1/12 of the grid across, 1/10 along z) of their lowest and of
+// their highest column, so LORs that enter and leave the grid at nearly the
+// same places — nearly parallel neighbours, like a detector tube — sit next to
+// each other.
+//
 // Construction: rows are copied in the new order with the column map
 // applied, then two stable transposes (transpose.cu) sort the columns of
 // every row; the intermediate transpose is exactly the transpose of A' and is
@@ -70,7 +77,56 @@ __global__ void k_invert(const uint32_t* __restrict__ map, uint32_t n, uint32_t*
 
 unsigned grid_of(uint64_t n) { return std::max(1u, std::min<unsigned>(ceil_div_u(n, 256), 152u * 16u)); }
 
+// Lowest and highest column of every row (one warp per row; ~0u / 0 when empty).
+__global__ void k_row_minmax(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx, uint32_t rows,
+                             uint2* __restrict__ mm) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += nw) {
+        uint32_t lo = 0xffffffffu, hi = 0u;
+        for (uint64_t e = rowptr[r] + lane; e < rowptr[r + 1]; e += 32) {
+            const uint32_t c = idx[e];
+            lo = min(lo, c);
+            hi = max(hi, c);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if (lane == 0) mm[r] = make_uint2(lo, hi);
+    }
+}
+
 }  // namespace
+
+std::vector<uint32_t> derived_lor_order(const DevCsr& A, uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t s) {
+    std::vector<uint2> mm(A.nrows);
+    uint2* d_mm = nullptr;
+    MLEM_CUDA(cudaMalloc(&d_mm, sizeof(uint2) * std::max<uint32_t>(A.nrows, 1)));
+    if (A.nrows) {
+        const unsigned grid = std::max(1u, std::min<unsigned>(ceil_div_u((uint64_t)A.nrows * 32, 256), 152u * 32u));
+        k_row_minmax<<<grid, 256, 0, s>>>(A.rowptr, A.idx, A.nrows, d_mm);
+        MLEM_LAUNCHED();
+        MLEM_CUDA(cudaMemcpyAsync(mm.data(), d_mm, sizeof(uint2) * A.nrows, cudaMemcpyDeviceToHost, s));
+    }
+    MLEM_CUDA(cudaStreamSynchronize(s));
+    cudaFree(d_mm);
+    const uint32_t qxy = std::max(4u, (std::max(nx, ny) + 6) / 12), qz = std::max(2u, (nz + 5) / 10);
+    const uint64_t cx = (nx + qxy - 1) / qxy, cy = (ny + qxy - 1) / qxy, cz = (nz + qz - 1) / qz;
+    const uint64_t ncell = cx * cy * cz;
+    auto cell = [&](uint32_t c) -> uint64_t {
+        const uint32_t x = c % nx, y = (c / nx) % ny, z = c / (nx * ny);
+        return (uint64_t)(z / qz) * cx * cy + (uint64_t)(y / qxy) * cx + x / qxy;
+    };
+    std::vector<uint64_t> key(A.nrows);
+    for (uint32_t r = 0; r < A.nrows; ++r)
+        key[r] = mm[r].x > mm[r].y ? ~0ull : cell(mm[r].x) * ncell + cell(mm[r].y);  // empty rows last
+    std::vector<uint32_t> ord(A.nrows);
+    for (uint32_t r = 0; r < A.nrows; ++r) ord[r] = r;
+    std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
+    return ord;
+}
 
 void launch_gather_i32(int32_t* out, const int32_t* in, const uint32_t* map, uint64_t n, cudaStream_t s) {
     if (n == 0) return;

@@ -662,14 +662,16 @@ static void apply_layout(mlem_matrix* m, const std::vector<uint32_t>& lor, const
     m->vox_of_host = vox;
 }
 
-// The layout the options ask for, given the voxel grid (and, for generated
-// matrices, the LOR order).
+// The layout the options ask for, given the voxel grid and, for generated
+// matrices, the detector-tube LOR order (empty: the order derived from the
+// matrix's own columns).
 static void maybe_apply_layout(mlem_matrix* m, const mlem_matrix_opts& o, uint32_t nx, uint32_t ny, uint32_t nz,
                                const std::vector<uint32_t>& lor) {
     if (o.layout == MLEM_LAYOUT_NATURAL) return;
     MLEM_REQUIRE(nx && ny && nz && (uint64_t)nx * ny * nz == m->A.ncols, MLEM_EINVAL,
                  "locality layout needs the voxel grid: nx*ny*nz must equal the number of columns");
-    apply_layout(m, lor, voxel_brick_order(nx, ny, nz, 4, 4, 2), o.build_transpose != 0);
+    apply_layout(m, lor.empty() ? derived_lor_order(m->A, nx, ny, nz, m->stream) : lor,
+                 voxel_brick_order(nx, ny, nz, 4, 4, 2), o.build_transpose != 0);
 }
 
 static mlem_matrix* new_matrix(const mlem_matrix_opts& o) {

@@ -106,7 +106,8 @@ typedef struct {
 
 /* Device layout of a matrix.  LOCALITY stores A' = P_L A P_Vᵀ: columns
  * (voxels) in 4x4x2 bricks, rows (LORs) in 4x4 detector tubes for generated
- * matrices (natural row order otherwise), each row's columns ascending.  The
+ * matrices (other matrices: rows sorted by the coarse voxel cells of their
+ * lowest and highest column), each row's columns ascending.  The
  * gathers of both projections then hit fewer cache lines.  Every entry point
  * still takes and returns natural order (sinograms, images, projections,
  * mlem_matrix_get_csr / _transpose / _norm); results agree with the natural

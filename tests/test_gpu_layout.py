@@ -110,6 +110,55 @@ def test_locality_layout_from_csr_and_csr4(pkg, O, tmp_path):
         pkg.Matrix.from_csr(*A, p["cols"], layout=7, grid=grid)
 
 
+def test_derived_row_order(pkg, O, cuda):
+    """A matrix with no detector numbering (rows shuffled, empty rows added)
+    gets its row order from its own columns; every entry point stays natural."""
+    p = problem(pkg, O, "cyl3d_tiny")
+    geo = p["geo"]
+    rng = np.random.default_rng(11)
+    lens = np.diff(p["rp"])
+    rows = [(p["col"][p["rp"][i]:p["rp"][i + 1]], p["val"][p["rp"][i]:p["rp"][i + 1]]) for i in range(len(lens))]
+    empty = (np.zeros(0, np.uint32), np.zeros(0, np.float32))
+    rows = [rows[i] for i in rng.permutation(len(rows))] + [empty] * 5
+    perm = rng.permutation(len(rows))
+    rows = [rows[i] for i in perm]
+    rp = np.concatenate([[0], np.cumsum([len(c) for c, _ in rows])]).astype(np.uint64)
+    col = np.concatenate([c for c, _ in rows]).astype(np.uint32)
+    val = np.concatenate([v for _, v in rows]).astype(np.float32)
+    A = (rp, col, val)
+    cols = p["cols"]
+    g = rng.poisson(20.0, len(rows)).astype(np.int32)
+    m = pkg.Matrix.from_csr(*A, cols, layout=pkg.LAYOUT_LOCALITY, grid=(geo.nx, geo.ny, geo.nz))
+    got = m.csr()
+    assert np.array_equal(got[0], rp) and np.array_equal(got[1], col)
+    assert np.array_equal(got[2].view(np.uint32), val.view(np.uint32))
+    for a, b in zip(m.transpose(), O.transpose(rp, col, val, cols)):
+        assert np.array_equal(a, b)
+    norm = O.colsum(*A, cols)
+    np.testing.assert_allclose(m.norm(), norm, rtol=1e-6, atol=0)
+    f0 = np.full(cols, m.initial_value(g), np.float32)
+    ref64 = O.mlem_f64(A, g, norm.astype(np.float64), f0, 10)
+    for spmv, bp in MODES:
+        assert O.rel_l2(m.run(g, 10, f0=f0, spmv=spmv, bp_mode=bp), ref64) < TOL_F32, (spmv, bp)
+    x = rng.uniform(0.1, 1.0, cols).astype(np.float32)
+    dx, dg = dev(cuda, x), dev(cuda, g)
+    ratio = cuda.zeros(len(rows), dtype=cuda.float32, device="cuda")
+    fwp = cuda.zeros(len(rows), dtype=cuda.float32, device="cuda")
+    m.forward_project(dx.data_ptr(), dg.data_ptr(), ratio.data_ptr(), fwp.data_ptr())
+    cuda.cuda.synchronize()
+    np.testing.assert_allclose(fwp.cpu().numpy(), O.spmv_csrvec(*A, x), rtol=2e-5, atol=1e-6)
+    r = rng.uniform(0.0, 2.0, len(rows)).astype(np.float32)
+    bp = cuda.zeros(cols, dtype=cuda.float32, device="cuda")
+    m.back_project(dev(cuda, r).data_ptr(), bp.data_ptr())
+    cuda.cuda.synchronize()
+    np.testing.assert_allclose(bp.cpu().numpy(), O.scatter(*A, r, cols), rtol=2e-5, atol=1e-6)
+    G = np.stack([g, rng.poisson(5.0, len(rows)).astype(np.int32)])
+    out = m.batch_run(G, np.array([10, 4], np.uint32), tile=8)
+    for k, it in enumerate((10, 4)):
+        assert O.rel_l2(out[k], m.run(G[k], it)) < TOL_F32
+    m.close()
+
+
 def test_locality_layout_server(pkg, O):
     p = problem(pkg, O, "ring2d")
     loc = pkg.Matrix.generate(p["geo"], layout=pkg.LAYOUT_LOCALITY)
