@@ -106,7 +106,8 @@ class BatchOpts(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("slots_per_matrix", C.c_uint32), ("hbm_budget_bytes", C.c_uint64),
-                ("hbm_reserve_bytes", C.c_uint64), ("queue_capacity", C.c_uint32)]
+                ("hbm_reserve_bytes", C.c_uint64), ("queue_capacity", C.c_uint32),
+                ("stream_priority", C.c_uint32)]
 
 
 class ServerStats(C.Structure):
@@ -576,9 +577,9 @@ class Server:
     """Continuous-batching reconstruction server over resident matrices."""
 
     def __init__(self, slots_per_matrix=0, hbm_budget_bytes=0, hbm_reserve_bytes=2 << 30,
-                 queue_capacity=4096):
+                 queue_capacity=4096, stream_priority=1):
         lib = load_library()
-        o = ServerOpts(slots_per_matrix, hbm_budget_bytes, hbm_reserve_bytes, queue_capacity)
+        o = ServerOpts(slots_per_matrix, hbm_budget_bytes, hbm_reserve_bytes, queue_capacity, stream_priority)
         h = C.c_void_p()
         _check(lib.mlem_server_create(C.byref(o), C.byref(h)))
         self._h = h

@@ -1,13 +1,19 @@
 // batch.cu — many sinograms against one resident matrix (batched SpMM).
 //
-// The matrix stream is shared by a tile of BT instances (8, 16 or 32): one
-// warp per row; the warp loads 32 (index, value) pairs with one coalesced
-// access each, broadcasts them with shuffles, and each lane multiplies them
-// against its instance's entry of the interleaved image f[col*BT + b] (one
-// 4*BT-byte coalesced gather per nonzero).  With BT < 32, 32/BT lane groups
-// take every (32/BT)-th nonzero and are combined by a fixed xor tree, so an
-// instance's arithmetic depends only on BT, never on which other slots are
-// occupied: an instance gives the same bits alone and in a full batch.
+// The matrix stream is shared by the instances of a tile (BT = 8, 16 or 32
+// slots, interleaved: slot b of voxel c is f[c*BT + b]).  A launch covers the
+// first W slots (the active width, 4..BT, the smallest power of two holding
+// every slot with iterations left): a row is handled by a segment of W lanes
+// of a warp (32/W rows per warp); each lane owns 4 instances of a nonzero and
+// reads their image entries with one 16-byte load, so W/4 lanes cover a
+// nonzero and a segment takes 4 nonzeros per gather instruction.  The
+// segment's lanes load the row 32 entries at a time (coalesced) and broadcast
+// them with shuffles.
+//
+// Every instance sums its row in 4 chains — nonzero k of the row goes to
+// chain k mod 4, each chain a sequential FMA chain in k order — combined as
+// (c0 + c1) + (c2 + c3).  That order depends on neither W nor BT nor the slot,
+// so an instance gives the same bits alone and in a full batch, in any tile.
 //
 // Per-slot iteration counters live on the device (remaining[b]); an
 // iteration is FP, BP+update and a counter tick, replayable as one CUDA
@@ -20,67 +26,124 @@ namespace mlem {
 
 namespace {
 
-template <typename V, int BT>
-__device__ __forceinline__ void batch_row(const uint32_t* __restrict__ idx, const V* __restrict__ val,
-                                          const float* __restrict__ x, uint64_t s, uint64_t t,
-                                          int lane, float& acc) {
-    constexpr int G = 32 / BT;       // lane groups
-    const int grp = lane / BT, b = lane % BT;
-    for (uint64_t base = s; base < t; base += 32) {
-        const uint64_t e = base + lane;
-        uint32_t c = 0;
-        float v = 0.f;
-        if (e < t) {
-            c = __ldcs(idx + e);
-            v = Val4<V>::one(val, e);
+// Row sums of one warp's 32/W rows (segment seg of W lanes holds row `row`,
+// `ok` = the row exists).  On return the lanes sl < W/4 of each segment hold
+// instances 4*sl..4*sl+3 of their row.
+template <typename V, int W>
+__device__ __forceinline__ void batch_rows(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
+                                           const V* __restrict__ val, const float* __restrict__ x, uint32_t BT,
+                                           uint32_t row, bool ok, int lane, float4& acc) {
+    constexpr int LPN = W / 4;  // lanes per nonzero
+    constexpr int E = 32 / W;   // entries per lane per 32-entry chunk
+    const int sl = lane % W, chain = sl / LPN, q4 = (sl % LPN) * 4, seg0 = lane - sl;
+    uint64_t s = 0, t = 0;
+    if (ok) {
+        s = rowptr[row];
+        t = rowptr[row + 1];
+    }
+    // the warp runs as many chunks as its longest row needs (shuffles stay converged)
+    uint32_t chunks = (uint32_t)((t - s + 31) >> 5);
+#pragma unroll
+    for (int o = W; o < 32; o <<= 1) chunks = max(chunks, __shfl_xor_sync(0xffffffffu, chunks, o));
+    for (uint32_t ch = 0; ch < chunks; ++ch) {
+        const uint64_t base = s + 32ull * ch;
+        // entry base + sl + i*W sits in slot i of lane sl
+        uint32_t c[E];
+        float v[E];
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+            const uint64_t e = base + sl + (uint64_t)i * W;
+            c[i] = 0;
+            v[i] = 0.f;
+            if (e < t) {
+                c[i] = __ldcs(idx + e);
+                v[i] = Val4<V>::one(val, e);
+            }
         }
-        // every lane runs the same trip count so the shuffles stay converged
-        const int n = (t - base) > 32 ? 32 : (int)(t - base);
-        const int trips = (n + G - 1) / G;
-#pragma unroll 4
-        for (int q = 0; q < trips; ++q) {
-            const int k = q * G + grp;
-            const uint32_t ck = __shfl_sync(0xffffffffu, c, k);
-            const float vk = __shfl_sync(0xffffffffu, v, k);
-            if (k < n) acc = fmaf(vk, __ldg(x + (uint64_t)ck * BT + b), acc);
+        // entries of this row left in the chunk, less the chain offset
+        const int64_t left = (int64_t)t - (int64_t)base;
+        const int r = (int)(left < 0 ? 0 : left > 32 ? 32 : left) - chain;
+        // trip q: nonzero k = 4q + chain of the chunk, held by lane k % W in
+        // slot k / W = 4q / W; k % W = 4q % W + chain since chain < 4 <= W
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            if (W == 32 && 4 * q >= r + chain) break;  // one row per warp: uniform
+            const int src = seg0 + chain + (4 * q) % W;
+            const uint32_t ck = __shfl_sync(0xffffffffu, c[(4 * q) / W], src);
+            const float vk = __shfl_sync(0xffffffffu, v[(4 * q) / W], src);
+            if (4 * q < r) {
+                const float4 xv = __ldg(reinterpret_cast<const float4*>(x + (uint64_t)ck * BT + q4));
+                acc.x = fmaf(vk, xv.x, acc.x);
+                acc.y = fmaf(vk, xv.y, acc.y);
+                acc.z = fmaf(vk, xv.z, acc.z);
+                acc.w = fmaf(vk, xv.w, acc.w);
+            }
         }
     }
+    // (c0 + c1) + (c2 + c3): chains sit LPN lanes apart inside the segment
 #pragma unroll
-    for (int o = BT; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    for (int o = LPN; o < W; o <<= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+        acc.w += __shfl_xor_sync(0xffffffffu, acc.w, o);
+    }
 }
 
-template <typename V, int BT>
+__device__ __forceinline__ float correl1(int32_t g, float fp) { return (fp != 0.0f) ? __fdiv_rn((float)g, fp) : 0.0f; }
+
+__device__ __forceinline__ float update1(float f, float acc, float n) {
+    const float t = __fmul_rn(f, acc);
+    return (n == 0.0f) ? t : __fdiv_rn(t, n);
+}
+
+// ratio[row*BT + b] = g/(A f)_b for the first W slots.
+template <typename V, int W>
 __global__ void __launch_bounds__(256)
 k_batch_fp(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
-           const V* __restrict__ val, const float* __restrict__ f, uint32_t rows,
+           const V* __restrict__ val, const float* __restrict__ f, uint32_t rows, uint32_t BT,
            const int32_t* __restrict__ g, float* __restrict__ ratio) {
-    const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (row >= rows) return;
-    float acc = 0.f;
-    batch_row<V, BT>(idx, val, f, rowptr[row], rowptr[row + 1], lane, acc);
-    if (lane < BT) {
-        const uint64_t o = (uint64_t)row * BT + lane;
-        ratio[o] = (acc != 0.0f) ? __fdiv_rn((float)g[o], acc) : 0.0f;
+    const uint64_t first = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * (32 / W);
+    if (first >= rows) return;  // whole warp
+    const uint64_t row = first + lane / W;
+    const bool ok = row < rows;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    batch_rows<V, W>(rowptr, idx, val, f, BT, (uint32_t)row, ok, lane, acc);
+    const int sl = lane % W;
+    if (ok && sl < W / 4) {
+        const uint64_t o = row * BT + sl * 4;
+        const int4 gg = *reinterpret_cast<const int4*>(g + o);
+        *reinterpret_cast<float4*>(ratio + o) =
+            make_float4(correl1(gg.x, acc.x), correl1(gg.y, acc.y), correl1(gg.z, acc.z), correl1(gg.w, acc.w));
     }
 }
 
-template <typename V, int BT>
+// f[c*BT + b] = f·(Aᵀ ratio)_b / norm[c] for the slots b < W with iterations left.
+template <typename V, int W>
 __global__ void __launch_bounds__(256)
 k_batch_bp(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
-           const V* __restrict__ val, const float* __restrict__ ratio, uint32_t cols,
+           const V* __restrict__ val, const float* __restrict__ ratio, uint32_t cols, uint32_t BT,
            const float* __restrict__ norm, const uint32_t* __restrict__ remaining,
            float* __restrict__ f) {
-    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (c >= cols) return;
-    float acc = 0.f;
-    batch_row<V, BT>(idx, val, ratio, rowptr[c], rowptr[c + 1], lane, acc);
-    if (lane < BT && remaining[lane] > 0) {
-        const uint64_t o = (uint64_t)c * BT + lane;
-        const float t = __fmul_rn(f[o], acc);
+    const uint64_t first = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * (32 / W);
+    if (first >= cols) return;  // whole warp
+    const uint64_t c = first + lane / W;
+    const bool ok = c < cols;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    batch_rows<V, W>(rowptr, idx, val, ratio, BT, (uint32_t)c, ok, lane, acc);
+    const int sl = lane % W;
+    if (ok && sl < W / 4) {
+        const uint64_t o = c * BT + sl * 4;
+        const uint4 rem = *reinterpret_cast<const uint4*>(remaining + sl * 4);
         const float n = norm[c];
-        f[o] = (n == 0.0f) ? t : __fdiv_rn(t, n);
+        float4 fv = *reinterpret_cast<const float4*>(f + o);
+        if (rem.x) fv.x = update1(fv.x, acc.x, n);
+        if (rem.y) fv.y = update1(fv.y, acc.y, n);
+        if (rem.z) fv.z = update1(fv.z, acc.z, n);
+        if (rem.w) fv.w = update1(fv.w, acc.w, n);
+        *reinterpret_cast<float4*>(f + o) = fv;
     }
 }
 
@@ -135,16 +198,16 @@ __global__ void k_batch_tick(uint32_t* remaining, uint32_t BT) {
     if (threadIdx.x < BT && remaining[threadIdx.x] > 0) remaining[threadIdx.x] -= 1;
 }
 
-template <int BT, typename V>
-void fp_bt(const DevCsr& A, const BatchArgs& b, L2Window win, cudaStream_t s) {
-    launch_ex(k_batch_fp<V, BT>, dim3(ceil_div_u((uint64_t)A.nrows * 32, 256)), dim3(256), 0, s, win,
-              A.rowptr, A.idx, static_cast<const V*>(A.val), (const float*)b.f, A.nrows, b.g, b.ratio);
+template <int W, typename V>
+void fp_w(const DevCsr& A, const BatchArgs& b, L2Window win, cudaStream_t s) {
+    launch_ex(k_batch_fp<V, W>, dim3(ceil_div_u((uint64_t)A.nrows * W, 256)), dim3(256), 0, s, win, A.rowptr,
+              A.idx, static_cast<const V*>(A.val), (const float*)b.f, A.nrows, b.tile, b.g, b.ratio);
 }
 
-template <int BT, typename V>
-void bp_bt(const DevCsr& AT, const float* norm, const BatchArgs& b, L2Window win, cudaStream_t s) {
-    launch_ex(k_batch_bp<V, BT>, dim3(ceil_div_u((uint64_t)AT.nrows * 32, 256)), dim3(256), 0, s, win,
-              AT.rowptr, AT.idx, static_cast<const V*>(AT.val), (const float*)b.ratio, AT.nrows, norm,
+template <int W, typename V>
+void bp_w(const DevCsr& AT, const float* norm, const BatchArgs& b, L2Window win, cudaStream_t s) {
+    launch_ex(k_batch_bp<V, W>, dim3(ceil_div_u((uint64_t)AT.nrows * W, 256)), dim3(256), 0, s, win, AT.rowptr,
+              AT.idx, static_cast<const V*>(AT.val), (const float*)b.ratio, AT.nrows, b.tile, norm,
               (const uint32_t*)b.remaining, b.f);
 }
 
@@ -157,15 +220,21 @@ void sc_bt(const DevCsr& A, const BatchArgs& b, float* bp, cudaStream_t s) {
 
 template <typename V>
 void fp_v(const DevCsr& A, const BatchArgs& b, L2Window win, cudaStream_t s) {
-    if (b.tile == 32) fp_bt<32, V>(A, b, win, s);
-    else if (b.tile == 16) fp_bt<16, V>(A, b, win, s);
-    else fp_bt<8, V>(A, b, win, s);
+    switch (b.width()) {
+        case 4: fp_w<4, V>(A, b, win, s); break;
+        case 8: fp_w<8, V>(A, b, win, s); break;
+        case 16: fp_w<16, V>(A, b, win, s); break;
+        default: fp_w<32, V>(A, b, win, s);
+    }
 }
 template <typename V>
 void bp_v(const DevCsr& AT, const float* norm, const BatchArgs& b, L2Window win, cudaStream_t s) {
-    if (b.tile == 32) bp_bt<32, V>(AT, norm, b, win, s);
-    else if (b.tile == 16) bp_bt<16, V>(AT, norm, b, win, s);
-    else bp_bt<8, V>(AT, norm, b, win, s);
+    switch (b.width()) {
+        case 4: bp_w<4, V>(AT, norm, b, win, s); break;
+        case 8: bp_w<8, V>(AT, norm, b, win, s); break;
+        case 16: bp_w<16, V>(AT, norm, b, win, s); break;
+        default: bp_w<32, V>(AT, norm, b, win, s);
+    }
 }
 template <typename V>
 void sc_v(const DevCsr& A, const BatchArgs& b, float* bp, cudaStream_t s) {

@@ -4,6 +4,7 @@
 
 #include "common.cuh"
 
+#include <algorithm>
 #include <vector>
 
 namespace mlem {
@@ -211,14 +212,29 @@ std::vector<uint32_t> voxel_brick_order(uint32_t nx, uint32_t ny, uint32_t nz, u
 // are [rows][tile]; remaining[b] counts the iterations slot b still runs.
 struct BatchArgs {
     uint32_t tile = 16;          // instances per tile (8/16/32)
+    uint32_t active = 0;         // slots 0..active-1 may have iterations left (0 = the whole tile)
     const int32_t* g = nullptr;
     float* f = nullptr;
     float* ratio = nullptr;
     uint32_t* remaining = nullptr;
+    // slots the projections cover: the smallest power of two >= active, 4..tile
+    uint32_t width() const {
+        const uint32_t a = active ? std::min(active, tile) : tile;
+        uint32_t w = 4;
+        while (w < a) w <<= 1;
+        return w;
+    }
 };
-// ratio[r][b] = g[r][b] / (A f_b)[r] for all slots.
+// Slots the projections cover for `active` leading slots in a tile (4..tile).
+inline uint32_t batch_width(uint32_t tile, uint32_t active) {
+    BatchArgs a;
+    a.tile = tile;
+    a.active = active;
+    return a.width();
+}
+// ratio[r][b] = g[r][b] / (A f_b)[r] for the slots b < width().
 void launch_batch_fp(const DevCsr& A, const BatchArgs& b, L2Window win, cudaStream_t s);
-// f_b = f_b * (Aᵀ ratio_b) / norm for slots with remaining > 0.
+// f_b = f_b * (Aᵀ ratio_b) / norm for slots b < width() with remaining > 0.
 void launch_batch_bp_update(const DevCsr& AT, const float* norm, const BatchArgs& b,
                             L2Window win, cudaStream_t s);
 // remaining[b] -= 1 where positive.

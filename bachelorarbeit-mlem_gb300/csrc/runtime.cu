@@ -69,7 +69,8 @@ void BatchState::alloc(uint32_t rows, uint32_t cols, uint32_t t, bool scatter) {
 }
 
 void BatchState::release() {
-    if (graph) cudaGraphExecDestroy(graph);
+    for (cudaGraphExec_t ge : graph)
+        if (ge) cudaGraphExecDestroy(ge);
     cudaFree(g);
     cudaFree(f);
     cudaFree(ratio);

@@ -83,13 +83,16 @@ struct BatchState {
     uint32_t* remaining = nullptr;  // [tile]
     int32_t* stage_g = nullptr;  // [rows] contiguous staging
     float* stage_f = nullptr;    // [cols] contiguous staging
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph[4] = {};  // one iteration per projection width 4/8/16/32
+    uint64_t graph_nodes[4] = {};
     uint64_t bytes = 0;
     void alloc(uint32_t rows, uint32_t cols, uint32_t tile, bool scatter);
     void release();
-    BatchArgs args() const {
+    // active: slots 0..active-1 may have iterations left (0 = all)
+    BatchArgs args(uint32_t active = 0) const {
         BatchArgs a;
         a.tile = tile;
+        a.active = active;
         a.g = g;
         a.f = f;
         a.ratio = ratio;
@@ -151,7 +154,7 @@ struct StageTimer {
 // current on entry (they exchange their outputs in orbit order)
 void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, double* ll_slot,
                        StageTimer* timer = nullptr, bool sym_fused = false);
-void enqueue_batch_iteration(mlem_matrix* m, BatchState& b, cudaStream_t s);
+void enqueue_batch_iteration(mlem_matrix* m, BatchState& b, cudaStream_t s, uint32_t active);
 float reference_initial_value(const mlem_matrix* m, const int32_t* g);
 void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o);
 // Settles kernel attributes / occupancy of the selected variant (outside captures).

@@ -4,8 +4,11 @@
 // Batched form: instances are packed into tiles of BT slots (interleaved
 // image/ratio state, per-slot iteration counters on the device).  One
 // iteration of a tile = batched FP, batched BP + update, counter tick; it is
-// captured once as a CUDA graph and replayed until the longest slot of the
-// tile finishes.  BT is picked by timing 8/16/32 on the matrix (autotuner).
+// captured as a CUDA graph per projection width and replayed until the
+// longest slot of the tile finishes.  The projections cover only the leading
+// slots that still run (width 4/8/16/32), so a tile that is emptying, or a
+// server matrix with few requests in flight, costs less per iteration.  BT is
+// picked by timing 8/16/32 on the matrix (autotuner).
 //
 // Server: one worker thread owns per-matrix slot states; every matrix runs on
 // its own stream and advances independently: when one of its iterations
@@ -13,8 +16,9 @@
 // requests are admitted into free slots (a matrix's slot state is allocated
 // on first use if it fits the HBM budget) and its next iteration is launched.
 // Kernels of different matrices overlap on the GPU, and a small matrix is
-// not paced by a large one.  A request's arithmetic depends only on its
-// slot's tile size, so its result is the same alone and in a mix.
+// not paced by a large one.  A request's arithmetic depends on neither its
+// slot, the tile size nor the width, so its result is the same alone and in
+// a mix.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -28,8 +32,8 @@
 
 namespace mlem {
 
-void enqueue_batch_iteration(mlem_matrix* m, BatchState& b, cudaStream_t s) {
-    const BatchArgs a = b.args();
+void enqueue_batch_iteration(mlem_matrix* m, BatchState& b, cudaStream_t s, uint32_t active) {
+    const BatchArgs a = b.args(m->has_t ? active : 0);  // the scatter form covers the whole tile
     launch_batch_fp(m->A, a, {}, s);
     if (m->has_t) {
         launch_batch_bp_update(m->AT, m->norm, a, {}, s);
@@ -55,20 +59,24 @@ static uint64_t batch_state_bytes(uint32_t rows, uint32_t cols, uint32_t tile, b
     return 8ull * R * tile + 4ull * C * tile * (scatter ? 2 : 1) + 4 * R + 4 * C + 128;
 }
 
-// Replays one iteration of the tile as a CUDA graph (captured on first use).
-static void batch_step(mlem_matrix* m, BatchState& b, cudaStream_t s, bool use_graph, uint64_t& nodes) {
+// Replays one iteration of the tile as a CUDA graph (one per projection
+// width, captured on first use).  active: slots 0..active-1 may have
+// iterations left; the projections cover the smallest width holding them.
+static void batch_step(mlem_matrix* m, BatchState& b, cudaStream_t s, bool use_graph, uint32_t active) {
     if (!use_graph) {
-        enqueue_batch_iteration(m, b, s);
+        enqueue_batch_iteration(m, b, s, active);
         return;
     }
-    if (!b.graph) {
+    const uint32_t w = m->has_t ? batch_width(b.tile, active) : b.tile;  // the scatter form covers the tile
+    const int gi = w == 4 ? 0 : w == 8 ? 1 : w == 16 ? 2 : 3;
+    if (!b.graph[gi]) {
         cudaStream_t cs = nullptr;
         MLEM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         cudaGraph_t graph = nullptr;
         const uint64_t l0 = g_launches.load();
         MLEM_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
         try {
-            enqueue_batch_iteration(m, b, cs);
+            enqueue_batch_iteration(m, b, cs, w);
         } catch (...) {
             cudaStreamEndCapture(cs, &graph);
             if (graph) cudaGraphDestroy(graph);
@@ -76,15 +84,15 @@ static void batch_step(mlem_matrix* m, BatchState& b, cudaStream_t s, bool use_g
             throw;
         }
         MLEM_CUDA(cudaStreamEndCapture(cs, &graph));
-        nodes = g_launches.load() - l0;
-        g_launches.fetch_sub(nodes);
-        const cudaError_t e = cudaGraphInstantiate(&b.graph, graph, 0);
+        b.graph_nodes[gi] = g_launches.load() - l0;
+        g_launches.fetch_sub(b.graph_nodes[gi]);
+        const cudaError_t e = cudaGraphInstantiate(&b.graph[gi], graph, 0);
         cudaGraphDestroy(graph);
         cudaStreamDestroy(cs);
         MLEM_CUDA(e);
     }
-    MLEM_CUDA(cudaGraphLaunch(b.graph, s));
-    count_launch(nodes);
+    MLEM_CUDA(cudaGraphLaunch(b.graph[gi], s));
+    count_launch(b.graph_nodes[gi]);
 }
 
 // Picks the batch tile with the highest images*iterations per second.
@@ -111,9 +119,9 @@ static uint32_t autotune_tile(mlem_matrix* m, cudaStream_t s) {
         std::vector<int32_t> cnt((uint64_t)std::max(rows, 1u) * bt, 1);
         MLEM_CUDA(cudaMemcpyAsync(b.f, ones.data(), sizeof(float) * ones.size(), cudaMemcpyHostToDevice, s));
         MLEM_CUDA(cudaMemcpyAsync(b.g, cnt.data(), sizeof(int32_t) * cnt.size(), cudaMemcpyHostToDevice, s));
-        enqueue_batch_iteration(m, b, s);  // warm-up
+        enqueue_batch_iteration(m, b, s, bt);  // warm-up
         MLEM_CUDA(cudaEventRecord(e0, s));
-        for (int q = 0; q < 3; ++q) enqueue_batch_iteration(m, b, s);
+        for (int q = 0; q < 3; ++q) enqueue_batch_iteration(m, b, s, bt);
         MLEM_CUDA(cudaEventRecord(e1, s));
         MLEM_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
@@ -160,12 +168,13 @@ struct MatrixSlots {
     bool inflight = false;            // an iteration is running on `stream`
     std::vector<uint64_t> slot_req;   // 0 = free
     std::vector<uint32_t> slot_left;
-    uint64_t graph_nodes = 0;
     uint32_t tile = 0;
-    bool active() const {
-        for (uint64_t x : slot_req)
-            if (x) return true;
-        return false;
+    bool active() const { return active_slots() > 0; }
+    // one past the highest occupied slot
+    uint32_t active_slots() const {
+        for (uint32_t b = (uint32_t)slot_req.size(); b > 0; --b)
+            if (slot_req[b - 1]) return b;
+        return 0;
     }
 };
 
@@ -289,7 +298,7 @@ void mlem_server::run() {
             // 3. next iteration of every idle matrix with work
             for (auto& ms : mats) {
                 if (!ms.inflight && ms.active()) {
-                    batch_step(ms.m, ms.bs, ms.stream, true, ms.graph_nodes);
+                    batch_step(ms.m, ms.bs, ms.stream, true, ms.active_slots());
                     MLEM_CUDA(cudaEventRecord(ms.done, ms.stream));
                     ms.inflight = true;
                 }
@@ -335,7 +344,7 @@ mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, con
                              [&](uint32_t a, uint32_t b) { return iterations[a] > iterations[b]; });
         BatchState bs;
         bs.alloc(rows, cols, tile, !m->has_t);
-        uint64_t nodes = 0, h2d = 0, d2h = 0, iters_total = 0;
+        uint64_t h2d = 0, d2h = 0, iters_total = 0;
         cudaEvent_t e0, e1;
         MLEM_CUDA(cudaEventCreate(&e0));
         MLEM_CUDA(cudaEventCreate(&e1));
@@ -366,7 +375,14 @@ mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, con
                     iters_total += iterations[i];
                 }
                 MLEM_CUDA(cudaEventRecord(e0, s));
-                for (uint32_t it = 0; it < maxit; ++it) batch_step(m, bs, s, o.use_graph != 0, nodes);
+                // slots hold their instances by decreasing iteration count when
+                // ordered, so the slots still running are a prefix that shrinks
+                for (uint32_t it = 0; it < maxit; ++it) {
+                    uint32_t act = 0;
+                    for (uint32_t b = 0; b < n; ++b)
+                        if (iterations[order[base + b]] > it) act = b + 1;
+                    batch_step(m, bs, s, o.use_graph != 0, act);
+                }
                 MLEM_CUDA(cudaEventRecord(e1, s));
                 for (uint32_t b = 0; b < n; ++b) {
                     const uint32_t i = order[base + b];
@@ -409,6 +425,7 @@ void mlem_server_opts_default(mlem_server_opts* o) {
     o->hbm_budget_bytes = 0;
     o->hbm_reserve_bytes = 2ull << 30;
     o->queue_capacity = 4096;
+    o->stream_priority = 1;
 }
 
 mlem_status mlem_server_create(const mlem_server_opts* opts, mlem_server** out) {
@@ -422,6 +439,10 @@ mlem_status mlem_server_create(const mlem_server_opts* opts, mlem_server** out) 
               s->opts.slots_per_matrix == 32)) {
             delete s;
             fail(MLEM_EINVAL, "slots_per_matrix must be 0 (autotuned), 8, 16 or 32");
+        }
+        if (s->opts.stream_priority > 2) {
+            delete s;
+            fail(MLEM_EINVAL, "stream_priority must be 0, 1 or 2");
         }
         cudaGetDevice(&s->device);
         if (s->opts.hbm_budget_bytes) {
@@ -451,13 +472,19 @@ mlem_status mlem_server_add_matrix(mlem_server* s, mlem_matrix* m, uint32_t* mat
         ms.tile = s->opts.slots_per_matrix ? s->opts.slots_per_matrix : autotune_tile(m, m->stream);
         ms.slot_req.assign(ms.tile, 0);
         ms.slot_left.assign(ms.tile, 0);
-        // smaller matrices get higher stream priority, so their short
-        // iterations are scheduled ahead of the CTAs of large ones
+        // smaller matrices can get higher stream priority, so their short
+        // iterations are scheduled ahead of the CTAs of large ones.  The
+        // default raises only small matrices: a matrix with requests in flight
+        // runs its iterations back to back, so a mid-size matrix ranked above a
+        // large one takes most of the GPU while few of its slots are occupied,
+        // and the large matrix's requests pile up (3-matrix Poisson mix: p99
+        // 5.8 s with three levels, 2.5 s with small-first-then-equal)
         int least = 0, greatest = 0;
         MLEM_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
         int prio = least;
-        if (m->A.nnz < (16ull << 20)) prio = greatest;
-        else if (m->A.nnz < (512ull << 20)) prio = (least + greatest) / 2;
+        const uint32_t pol = s->opts.stream_priority;
+        if (pol != 2 && m->A.nnz < (16ull << 20)) prio = greatest;
+        else if (pol == 0 && m->A.nnz < (512ull << 20)) prio = (least + greatest) / 2;
         MLEM_CUDA(cudaStreamCreateWithPriority(&ms.stream, cudaStreamNonBlocking, prio));
         MLEM_CUDA(cudaEventCreateWithFlags(&ms.done, cudaEventDisableTiming));
         s->mats.push_back(std::move(ms));

@@ -603,7 +603,8 @@ def run_serving(pkg, torch, n_requests=300, rate=50.0, fp32_iter_s=None):
            "reconstructions_per_s": n_requests / wall, "wall_s": wall,
            "iterations_done": int(stats["iterations_done"]),
            "mix": "ring2d fp32 0.5 / cyl3d_mid fp32 0.35 / cyl3d_12gb fp16 0.15, counts log-U[1e5,1e9], "
-                  "iterations U{20..100}, autotuned slots per matrix, stream priority by matrix size"}
+                  "iterations U{20..100}, autotuned slots per matrix, projections over the occupied slots, "
+                  "small matrices (< 16 M nonzeros) on a high-priority stream"}
     for j, (name, _, _) in enumerate(specs):
         sel = which == j
         if sel.any():

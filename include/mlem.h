@@ -409,6 +409,10 @@ typedef struct {
     uint64_t hbm_budget_bytes;  /* admission limit for per-request state (0 = free HBM - reserve) */
     uint64_t hbm_reserve_bytes; /* HBM kept free when hbm_budget_bytes == 0 */
     uint32_t queue_capacity;    /* max queued requests before submit returns EBUSY */
+    uint32_t stream_priority;   /* per-matrix stream priority: 0 = by size (< 16 M nonzeros
+                                   highest, < 512 M middle, larger lowest), 1 (default) = small
+                                   matrices (< 16 M nonzeros) highest, all others equal,
+                                   2 = all equal */
 } mlem_server_opts;
 
 void mlem_server_opts_default(mlem_server_opts* o);

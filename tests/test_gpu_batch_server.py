@@ -58,6 +58,23 @@ def test_batch_without_transpose_and_fp16(pkg, O):
     m_half.close()
 
 
+def test_batch_bits_independent_of_tile_and_width(pkg, O):
+    """Each instance sums its rows in the same order in every tile (8/16/32)
+    and at every projection width, so the images agree bit for bit, also
+    while a tile empties (uneven iteration counts)."""
+    p = problem(pkg, O, "cyl3d_tiny")
+    m = pkg.Matrix.from_csr(p["rp"], p["col"], p["val"], p["cols"], value_type=pkg.VAL_F16)
+    G = sinograms(pkg, p, 11)
+    its = np.random.Generator(np.random.PCG64(9)).integers(1, 30, len(G)).astype(np.uint32)
+    outs = [m.batch_run(G, its, tile=t) for t in (8, 16, 32)]
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    unordered = m.batch_run(G, its, tile=16, order_by_iterations=False)
+    assert np.array_equal(unordered, outs[0])
+    for k in (0, 5, 10):
+        assert np.array_equal(m.batch_run(G[k:k + 1], its[k:k + 1], tile=32)[0], outs[0][k])
+    m.close()
+
+
 def test_batch_instance_independent_of_company(pkg, O):
     p = problem(pkg, O, "ring2d")
     m = pkg.Matrix.from_csr(p["rp"], p["col"], p["val"], p["cols"])
@@ -70,13 +87,16 @@ def test_batch_instance_independent_of_company(pkg, O):
     m.close()
 
 
-def test_server_same_alone_and_in_mix(pkg, O):
+@pytest.mark.parametrize("slots,priority", [(8, 0), (32, 2)])
+def test_server_same_alone_and_in_mix(pkg, O, slots, priority):
     pa = problem(pkg, O, "ring2d")
     pb = problem(pkg, O, "cyl3d_tiny")
     ma = pkg.Matrix.from_csr(pa["rp"], pa["col"], pa["val"], pa["cols"])
     mb = pkg.Matrix.from_csr(pb["rp"], pb["col"], pb["val"], pb["cols"], value_type=pkg.VAL_F16)
     Ga, Gb = sinograms(pkg, pa, 20, seed=1), sinograms(pkg, pb, 12, seed=2)
-    with pkg.Server(slots_per_matrix=8) as srv:
+    with pytest.raises(pkg.MlemError):
+        pkg.Server(stream_priority=3)
+    with pkg.Server(slots_per_matrix=slots, stream_priority=priority) as srv:
         ia, ib = srv.add_matrix(ma), srv.add_matrix(mb)
         alone_a, _ = srv.wait(srv.submit(ia, Ga[0], 15))
         alone_b, _ = srv.wait(srv.submit(ib, Gb[0], 9))
@@ -97,6 +117,8 @@ def test_server_same_alone_and_in_mix(pkg, O):
         assert st["active"] == 0 and st["queued"] == 0
     assert np.array_equal(res[("a", 0)], alone_a)
     assert np.array_equal(res[("b", 0)], alone_b)
+    # the batched arithmetic does not depend on the tile: the same bits as batch_run
+    assert np.array_equal(alone_a, ma.batch_run(Ga[:1], np.array([15], np.uint32), tile=16)[0])
     single = ma.run(Ga[0], 15)
     assert O.rel_l2(alone_a, single) < 1e-5
     ma.close()
