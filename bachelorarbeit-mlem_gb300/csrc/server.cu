@@ -4,11 +4,12 @@
 // Batched form: instances are packed into tiles of BT slots (interleaved
 // image/ratio state, per-slot iteration counters on the device).  One
 // iteration of a tile = batched FP, batched BP + update, counter tick; it is
-// captured as a CUDA graph per projection width and replayed until the
-// longest slot of the tile finishes.  The projections cover only the leading
-// slots that still run (width 4/8/16/32), so a tile that is emptying, or a
-// server matrix with few requests in flight, costs less per iteration.  BT is
-// picked by timing 8/16/32 on the matrix (autotuner).
+// captured as a CUDA graph per projection width and replayed; a slot whose
+// instance is done takes the next instance between two iterations.  The
+// projections cover only the leading slots that still run (width
+// 4/8/16/32), so a pool that is emptying, or a server matrix with few
+// requests in flight, costs less per iteration.  BT is picked by timing
+// 8/16/32 on the matrix (autotuner).
 //
 // Server: one worker thread owns per-matrix slot states; every matrix runs on
 // its own stream and advances independently: when one of its iterations
@@ -345,64 +346,139 @@ mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, con
         BatchState bs;
         bs.alloc(rows, cols, tile, !m->has_t);
         uint64_t h2d = 0, d2h = 0, iters_total = 0;
-        cudaEvent_t e0, e1;
-        MLEM_CUDA(cudaEventCreate(&e0));
-        MLEM_CUDA(cudaEventCreate(&e1));
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
         double dev_seconds = 0.0;
         const uint64_t l0 = g_launches.load();
-        try {
-            for (uint32_t base = 0; base < count; base += tile) {
-                const uint32_t n = std::min(tile, count - base);
-                MLEM_CUDA(cudaMemsetAsync(bs.remaining, 0, sizeof(uint32_t) * 32, s));
-                uint32_t maxit = 0;
-                for (uint32_t b = 0; b < n; ++b) {
-                    const uint32_t i = order[base + b];
-                    const int32_t* gi = g + (uint64_t)i * rows;
-                    MLEM_CUDA(cudaMemcpyAsync(bs.stage_g, gi, sizeof(int32_t) * rows, cudaMemcpyHostToDevice, s));
-                    h2d += sizeof(int32_t) * (uint64_t)rows;
-                    const float* f0d = nullptr;
-                    float init = 0.f;
-                    if (f0) {
-                        MLEM_CUDA(cudaMemcpyAsync(bs.stage_f, f0 + (uint64_t)i * cols, sizeof(float) * cols,
-                                                  cudaMemcpyHostToDevice, s));
-                        h2d += sizeof(float) * (uint64_t)cols;
-                        f0d = bs.stage_f;
-                    } else {
-                        init = reference_initial_value(m, gi);
-                    }
-                    batch_put_slot(m, bs, b, bs.stage_g, init, f0d, iterations[i], s);
-                    maxit = std::max(maxit, iterations[i]);
-                    iters_total += iterations[i];
-                }
-                MLEM_CUDA(cudaEventRecord(e0, s));
-                // slots hold their instances by decreasing iteration count when
-                // ordered, so the slots still running are a prefix that shrinks
-                for (uint32_t it = 0; it < maxit; ++it) {
-                    uint32_t act = 0;
-                    for (uint32_t b = 0; b < n; ++b)
-                        if (iterations[order[base + b]] > it) act = b + 1;
-                    batch_step(m, bs, s, o.use_graph != 0, act);
-                }
-                MLEM_CUDA(cudaEventRecord(e1, s));
-                for (uint32_t b = 0; b < n; ++b) {
-                    const uint32_t i = order[base + b];
-                    batch_get_slot(m, bs, b, bs.stage_f, s);
-                    MLEM_CUDA(cudaMemcpyAsync(f_out + (uint64_t)i * cols, bs.stage_f, sizeof(float) * cols,
-                                              cudaMemcpyDeviceToHost, s));
-                    d2h += sizeof(float) * (uint64_t)cols;
-                }
-                MLEM_CUDA(cudaStreamSynchronize(s));
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                dev_seconds += ms * 1e-3;
+        // The tile's slots form a pool: the instances enter in `order`
+        // (longest first when ordered), and a slot whose instance has run its
+        // iterations hands the image back and takes the next instance before
+        // the following iteration, so the pool stays full until the last
+        // instances.  The host knows when every slot finishes (the counts are
+        // fixed), so the refills are simply enqueued between iterations.
+        std::vector<int64_t> slot_inst(tile, -1);
+        std::vector<uint64_t> slot_end(tile, 0);
+        uint32_t next = 0;
+        uint64_t step = 0;
+        // Sinograms in and images out pass through a small ring of pinned host
+        // buffers, so a refill never waits for the GPU to drain (a pageable
+        // copy would): buffer j is reused once its previous copy has completed.
+        constexpr uint32_t kRing = 4;
+        int32_t* pin_g = nullptr;
+        float* pin_f = nullptr;
+        cudaEvent_t ev_g[kRing] = {}, ev_f[kRing] = {};
+        float* pending_f[kRing] = {};
+        uint32_t ring_g = 0, ring_f = 0;
+        const bool pinned =
+            cudaHostAlloc((void**)&pin_g, sizeof(int32_t) * std::max<uint64_t>(rows, 1) * kRing, cudaHostAllocDefault) ==
+                cudaSuccess &&
+            cudaHostAlloc((void**)&pin_f, sizeof(float) * std::max<uint64_t>(cols, 1) * kRing, cudaHostAllocDefault) ==
+                cudaSuccess;
+        if (!pinned) cudaGetLastError();  // fall back to pageable copies
+        auto drain_f = [&](uint32_t j) {  // completes the image copy held by ring buffer j
+            if (!pending_f[j]) return;
+            MLEM_CUDA(cudaEventSynchronize(ev_f[j]));
+            std::memcpy(pending_f[j], pin_f + (uint64_t)j * cols, sizeof(float) * cols);
+            pending_f[j] = nullptr;
+        };
+        auto admit = [&](uint32_t b) {
+            const uint32_t i = order[next++];
+            const int32_t* gi = g + (uint64_t)i * rows;
+            if (pinned) {
+                const uint32_t j = ring_g++ % kRing;
+                if (ev_g[j]) MLEM_CUDA(cudaEventSynchronize(ev_g[j]));
+                else MLEM_CUDA(cudaEventCreateWithFlags(&ev_g[j], cudaEventDisableTiming));
+                int32_t* hb = pin_g + (uint64_t)j * rows;
+                std::memcpy(hb, gi, sizeof(int32_t) * rows);
+                MLEM_CUDA(cudaMemcpyAsync(bs.stage_g, hb, sizeof(int32_t) * rows, cudaMemcpyHostToDevice, s));
+                MLEM_CUDA(cudaEventRecord(ev_g[j], s));
+            } else {
+                MLEM_CUDA(cudaMemcpyAsync(bs.stage_g, gi, sizeof(int32_t) * rows, cudaMemcpyHostToDevice, s));
             }
+            h2d += sizeof(int32_t) * (uint64_t)rows;
+            const float* f0d = nullptr;
+            float init = 0.f;
+            if (f0) {
+                MLEM_CUDA(cudaMemcpyAsync(bs.stage_f, f0 + (uint64_t)i * cols, sizeof(float) * cols,
+                                          cudaMemcpyHostToDevice, s));
+                h2d += sizeof(float) * (uint64_t)cols;
+                f0d = bs.stage_f;
+            } else {
+                init = reference_initial_value(m, gi);
+            }
+            batch_put_slot(m, bs, b, bs.stage_g, init, f0d, iterations[i], s);
+            iters_total += iterations[i];
+            slot_inst[b] = i;
+            slot_end[b] = step + iterations[i];
+        };
+        auto hand_back = [&](uint32_t b) {
+            const uint32_t i = (uint32_t)slot_inst[b];
+            batch_get_slot(m, bs, b, bs.stage_f, s);
+            if (pinned) {
+                const uint32_t j = ring_f++ % kRing;
+                if (ev_f[j]) drain_f(j);
+                else MLEM_CUDA(cudaEventCreateWithFlags(&ev_f[j], cudaEventDisableTiming));
+                MLEM_CUDA(cudaMemcpyAsync(pin_f + (uint64_t)j * cols, bs.stage_f, sizeof(float) * cols,
+                                          cudaMemcpyDeviceToHost, s));
+                MLEM_CUDA(cudaEventRecord(ev_f[j], s));
+                pending_f[j] = f_out + (uint64_t)i * cols;
+            } else {
+                MLEM_CUDA(cudaMemcpyAsync(f_out + (uint64_t)i * cols, bs.stage_f, sizeof(float) * cols,
+                                          cudaMemcpyDeviceToHost, s));
+            }
+            d2h += sizeof(float) * (uint64_t)cols;
+            slot_inst[b] = -1;
+        };
+        auto release_ring = [&] {
+            for (uint32_t j = 0; j < kRing; ++j) {
+                if (ev_g[j]) cudaEventDestroy(ev_g[j]);
+                if (ev_f[j]) cudaEventDestroy(ev_f[j]);
+            }
+            if (pin_g) cudaFreeHost(pin_g);
+            if (pin_f) cudaFreeHost(pin_f);
+        };
+        try {
+            MLEM_CUDA(cudaEventCreate(&e0));
+            MLEM_CUDA(cudaEventCreate(&e1));
+            MLEM_CUDA(cudaMemsetAsync(bs.remaining, 0, sizeof(uint32_t) * 32, s));
+            // zero-iteration instances are their initial image
+            for (uint32_t b = 0; b < tile && next < count; ++b) {
+                admit(b);
+                while (slot_end[b] == step) {
+                    hand_back(b);
+                    if (next == count) break;
+                    admit(b);
+                }
+            }
+            MLEM_CUDA(cudaEventRecord(e0, s));
+            while (true) {
+                uint32_t act = 0;
+                for (uint32_t b = 0; b < tile; ++b)
+                    if (slot_inst[b] >= 0) act = b + 1;
+                if (act == 0) break;
+                batch_step(m, bs, s, o.use_graph != 0, act);
+                ++step;
+                for (uint32_t b = 0; b < act; ++b) {
+                    while (slot_inst[b] >= 0 && slot_end[b] == step) {
+                        hand_back(b);
+                        if (next < count) admit(b);
+                    }
+                }
+            }
+            MLEM_CUDA(cudaEventRecord(e1, s));
+            MLEM_CUDA(cudaStreamSynchronize(s));
+            for (uint32_t j = 0; j < kRing; ++j) drain_f(j);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            dev_seconds = ms * 1e-3;
         } catch (...) {
             cudaStreamSynchronize(s);
+            release_ring();
             bs.release();
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
             throw;
         }
+        release_ring();
         bs.release();
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);

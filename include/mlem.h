@@ -385,14 +385,17 @@ mlem_status mlem_matrix_get_csr(const mlem_matrix* m, uint64_t* rowptr, uint32_t
 /* ------------------------------------------------------------- batched */
 /* Reconstructs `count` sinograms against one resident matrix as a batched
  * SpMM (forward and back projection shared by up to 32 instances per tile),
- * replayed as CUDA graphs.  g: i32[count][rows]; iterations: u32[count]
- * (uneven counts allowed); f0: NULL (reference initial value per instance) or
- * f32[count][cols]; f_out: f32[count][cols].  Results of an instance do not
- * depend on which other instances share its batch. */
+ * replayed as CUDA graphs.  The tile's slots are a pool: an instance that has
+ * run its iterations hands its image back and the next instance takes its slot
+ * before the following iteration.  g: i32[count][rows]; iterations: u32[count]
+ * (uneven counts allowed, 0 returns the initial image); f0: NULL (reference
+ * initial value per instance) or f32[count][cols]; f_out: f32[count][cols].
+ * An instance's image is bit-identical whichever tile, slot and company it
+ * runs in. */
 typedef struct {
     uint32_t tile;              /* instances per batch tile: 0 = autotune, else 8/16/32 */
     uint32_t use_graph;
-    uint32_t order_by_iterations; /* 1: group instances of similar length */
+    uint32_t order_by_iterations; /* 1: instances enter the pool longest first */
 } mlem_batch_opts;
 
 void mlem_batch_opts_default(mlem_batch_opts* o);

@@ -66,8 +66,10 @@ def test_batch_bits_independent_of_tile_and_width(pkg, O):
     m = pkg.Matrix.from_csr(p["rp"], p["col"], p["val"], p["cols"], value_type=pkg.VAL_F16)
     G = sinograms(pkg, p, 11)
     its = np.random.Generator(np.random.PCG64(9)).integers(1, 30, len(G)).astype(np.uint32)
+    its[2] = 0  # a zero-iteration instance returns its initial image
     outs = [m.batch_run(G, its, tile=t) for t in (8, 16, 32)]
     assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    assert np.array_equal(outs[0][2], np.full(m.cols, m.initial_value(G[2]), np.float32))
     unordered = m.batch_run(G, its, tile=16, order_by_iterations=False)
     assert np.array_equal(unordered, outs[0])
     for k in (0, 5, 10):
