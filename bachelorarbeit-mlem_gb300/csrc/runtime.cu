@@ -455,12 +455,11 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
 }
 
 float reference_initial_value(const mlem_matrix* m, const int32_t* g) {
-    // main.cu:83-97: FP32 running sum of norm in column order, integer sum of g
-    float sum_norm = 0.0f;
-    for (float v : m->norm_host) sum_norm += v;
+    // main.cu:83-97: FP32 running sum of norm in column order (kept with the
+    // matrix), integer sum of g
     int64_t sum_g = 0;
     for (uint32_t i = 0; i < m->A.nrows; ++i) sum_g += g[i];
-    return (float)sum_g / sum_norm;
+    return (float)sum_g / m->norm_sum;
 }
 
 static void enable_l2_persisting(int dev) {
@@ -617,6 +616,8 @@ static void postprocess_matrix(mlem_matrix* m, const mlem_matrix_opts& o) {
         }
     }
     MLEM_CUDA(cudaStreamSynchronize(s));
+    m->norm_sum = 0.0f;
+    for (float v : m->norm_host) m->norm_sum += v;
 }
 
 // Puts A (natural order, f32) into the locality layout.  lor: natural row of

@@ -122,6 +122,7 @@ struct mlem_matrix {
     bool has_t = false;
     float* norm = nullptr;
     std::vector<float> norm_host;     // host copy in natural column order (initial value)
+    float norm_sum = 0.0f;            // FP32 running sum of norm_host in column order
     // Locality layout: natural row / column of each internal row / column
     // (NULL = natural order).
     mlem::SymOps sym;                 // symmetry-compressed operands (symmetry = 1)

@@ -465,7 +465,15 @@ def run_forms(pkg, torch, args):
             res["modes_cyl3d_mid"] = modes
             res["csr4_ingest_cyl3d_mid"] = time_csr4_ingest(pkg, msm)
         msm.close()
-    # batched: the mid-size matrix with FP16 values, 64 sinograms, uneven iterations
+    res["batched_fp16_64"] = run_batched(pkg, torch, res["fp32_plain_cyl3d_mid"]["images_iterations_per_s"])
+    return res
+
+
+def run_batched(pkg, torch, fp32_mid_rate=None):
+    """Batched form: the 3-D mid matrix with FP16 values, 64 sinograms of seeded
+    phantoms, counts log-U[1e5, 1e9], iterations U{10..200}, one batch_run."""
+    from mlem_gb300 import synth
+    s = torch.cuda.current_stream()
     mb = pkg.Matrix.generate(pkg.preset("cyl3d_mid"), value_type=pkg.VAL_F16, layout=LAYOUT)
     rng = np.random.Generator(np.random.PCG64(7))
     totals = np.exp(rng.uniform(np.log(1e5), np.log(1e9), 64))
@@ -481,13 +489,13 @@ def run_forms(pkg, torch, args):
         G[k] = synth.poisson_sinogram(fp.cpu().numpy().astype(np.float64), totals[k], seed=2000 + k)
     _, st = mb.batch_run(G[:8], np.full(8, 2, np.uint32), stats=True)  # autotune + warm-up
     _, st = mb.batch_run(G, its, stats=True)
-    res["batched_fp16_64"] = {"images_iterations_per_s": float(its.sum()) / st["seconds_iterations"],
-                              "wall_images_iterations_per_s": float(its.sum()) / st["seconds_total"],
-                              "workload": "cyl3d_mid fp16, 64 sinograms, iterations U{10..200}",
-                              "vs_fp32_plain_same_matrix": float(its.sum()) / st["seconds_iterations"]
-                              / res["fp32_plain_cyl3d_mid"]["images_iterations_per_s"]}
+    out = {"images_iterations_per_s": float(its.sum()) / st["seconds_iterations"],
+           "wall_images_iterations_per_s": float(its.sum()) / st["seconds_total"],
+           "workload": "cyl3d_mid fp16, 64 sinograms, iterations U{10..200}"}
+    if fp32_mid_rate:
+        out["vs_fp32_plain_same_matrix"] = out["images_iterations_per_s"] / fp32_mid_rate
     mb.close()
-    return res
+    return out
 
 
 def run_symmetry(pkg, torch, name):
@@ -625,7 +633,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cyl3d_12gb", choices=sorted(WORKLOADS))
-    ap.add_argument("--forms", default="all", choices=["all", "none", "modes", "symmetry"],
+    ap.add_argument("--forms", default="all", choices=["all", "none", "modes", "symmetry", "batched"],
                     help="all: FP16, batched, serving, symmetry and the modes on the smaller matrices; modes: only "
                          "the reference's switch combinations, the fused pass and a batched run on --workload; "
                          "symmetry: only the symmetry-compressed operands on --workload")
@@ -783,6 +791,8 @@ def main():
         line["forms"] = run_modes(pkg, torch, name)
     if args.forms == "symmetry":
         line["forms"] = {"symmetry": run_symmetry(pkg, torch, name)}
+    if args.forms == "batched":
+        line["forms"] = {"batched_fp16_64": run_batched(pkg, torch)}
     if args.forms == "all":
         line["forms"] = run_forms(pkg, torch, args)
         line["forms"]["fp32_plain"] = {"images_iterations_per_s": value / world}
