@@ -17,7 +17,7 @@
 //
 // Per-slot iteration counters live on the device (remaining[b]); an
 // iteration is FP, BP+update and a counter tick, replayable as one CUDA
-// graph until the longest slot finishes.
+// graph per width; a slot whose counter reached 0 is no longer updated.
 #include "kernels.cuh"
 
 #include <algorithm>
