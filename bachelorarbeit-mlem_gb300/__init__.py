@@ -449,7 +449,11 @@ class Matrix:
 
     def batch_run(self, g, iterations, f0=None, tile=0, use_graph=True, order_by_iterations=True,
                   stats=False):
-        """Reconstructs g[count][rows] with per-instance iteration counts."""
+        """Reconstructs g[count][rows] with per-instance iteration counts (mlem_batch_run).
+
+        The tile's slots (8/16/32; 0 = autotuned) form a pool that the instances
+        enter longest first (order_by_iterations); an image is bit-identical in
+        every tile and slot, and to the same sinogram run alone."""
         g = _arr(g, np.int32)
         count = g.shape[0]
         its = _arr(iterations, np.uint32)
@@ -574,7 +578,10 @@ def write_image(path, f) -> None:
 
 # -------------------------------------------------------------------- server
 class Server:
-    """Continuous-batching reconstruction server over resident matrices."""
+    """Continuous-batching reconstruction server over resident matrices (mlem_server_*).
+
+    stream_priority: 0 = three levels by matrix size, 1 (default) = small
+    matrices (< 16 M nonzeros) first and the others equal, 2 = all equal."""
 
     def __init__(self, slots_per_matrix=0, hbm_budget_bytes=0, hbm_reserve_bytes=2 << 30,
                  queue_capacity=4096, stream_priority=1):
