@@ -21,9 +21,11 @@
 #include "kernels.cuh"
 
 #include <algorithm>
+#include <cstdint>
 #include <map>
 #include <mutex>
 #include <string>
+#include <utility>
 
 namespace mlem {
 
@@ -453,22 +455,57 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = 4u << 20;  // 4 MiB per device
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of the array, looked up once per device with that device
-// current (in host code the symbol itself is only a host-side stand-in).
+// Identity of the current context: a number that the driver never reuses
+// within the process (cuCtxGetId).  cudaDeviceReset destroys the primary
+// context, and the module holding the array is loaded again into the next one,
+// possibly at another address; keying the lookup on this identity keeps a
+// stale address from being used.  The two driver calls are fetched through the
+// runtime, so the library does not link libcuda.  Returns 0 where they are not
+// available (the address is then looked up on every call).
+unsigned long long current_context_id() {
+    using GetCurrent = int (*)(void**);
+    using GetId = int (*)(void*, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(p);
+    });
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || ctx == nullptr || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Device address of the array for the current device, looked up with that
+// device current on the first call in each context (in host code the symbol
+// itself is only a host-side stand-in, not a device address).
 unsigned char* noalloc_scratch_address() {
     static std::mutex mu;
-    static std::map<int, unsigned char*> addr;
+    static std::map<std::pair<int, unsigned long long>, unsigned char*> addr;
     int dev = -1;
     MLEM_CUDA(cudaGetDevice(&dev));
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> lk(mu);
-    auto it = addr.find(dev);
-    if (it != addr.end()) return it->second;
+    const auto key = std::make_pair(dev, ctx);
+    if (ctx != 0) {
+        auto it = addr.find(key);
+        if (it != addr.end()) return it->second;
+    }
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     MLEM_REQUIRE(e == cudaSuccess && p != nullptr, MLEM_ECUDA,
                  std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-    addr[dev] = static_cast<unsigned char*>(p);
-    return addr[dev];
+    if (ctx != 0) addr[key] = static_cast<unsigned char*>(p);
+    return static_cast<unsigned char*>(p);
 }
 
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -485,6 +522,7 @@ extern "C" mlem_status mlem_forward_project_merge_noalloc(const uint64_t* rowptr
         MLEM_REQUIRE(rowptr_dev && x_dev && g_dev && ratio_dev && (nnz == 0 || (col_dev && val_dev)), MLEM_EINVAL,
                      "NULL argument");
         MLEM_REQUIRE(rows >= 1 && cols >= 1, MLEM_EINVAL, "matrix must have rows and columns");
+        MLEM_REQUIRE(nnz <= UINT64_MAX - rows, MLEM_EINVAL, "allocation-free merge path: rows + nnz overflows");
         MLEM_REQUIRE(secsize >= 1 && secsize <= 125, MLEM_EINVAL,
                      "allocation-free merge path: secsize must be in 1..125");
         // tile of T threads * secsize items, sized so the tile's shared memory

@@ -14,12 +14,13 @@ e2e    : the same through mlem_run (the C ABI a user calls) from pinned host
          buffers: sinogram + initial image in, image out, every step.
 roofline: the dominant kernel's algorithmic bytes / its CUDA-event duration
          against the measured HBM copy bandwidth.
-cpu_baseline: the oracle's OpenMP MLEM (FP32 values, FP64 accumulation) on a
-         row sample of the same matrix, scaled to the full matrix by nnz.
+cpu_baseline: the oracle's OpenMP MLEM (FP32 values, FP64 accumulation) on the
+         full matrix, built on the host by the oracle's own generator.
 
 --impl reference times the CPU implementation of the path (the reference has
 no CPU path of its own; the oracle port, pinned bit-exact to the reference's
-compiled code, stands in) and prints its line.  The line also carries
+compiled code, stands in) on the full matrix, with inputs built by the
+oracle alone (the product library is not loaded), and prints its line.  The line also carries
 "reference_cuda": the reference's own kernel.cu, compiled unmodified for
 sm_103a into oracle/_ref/mlemref_kernels.cubin, launched with the grids and
 step order of its single-GPU MLEM loop on the same workload (all four
@@ -46,9 +47,9 @@ PKG_DIR = ROOT / "bachelorarbeit-mlem_gb300"
 PROFILES = ROOT / "profiles"
 
 WORKLOADS = {
-    "cyl3d_12gb": dict(iters=100, shapes=20, total=1e8, cpu_stride=64),
-    "cyl3d_mid": dict(iters=100, shapes=20, total=1e8, cpu_stride=8),
-    "ring2d": dict(iters=20, shapes=5, total=1e6, cpu_stride=1),
+    "cyl3d_12gb": dict(iters=100, shapes=20, total=1e8),
+    "cyl3d_mid": dict(iters=100, shapes=20, total=1e8),
+    "ring2d": dict(iters=20, shapes=5, total=1e6),
 }
 
 
@@ -199,26 +200,82 @@ def time_kernels(pkg, m, torch, g, f0, iters=20, **opts):
     return {"fp": st["fp_ms"], "bp": st["bp_ms"]}
 
 
-def cpu_baseline(pkg, name, stride, iters=1):
-    """Oracle OpenMP MLEM on every stride-th LOR of the workload, scaled by nnz."""
+def import_pkg():
+    """The package's Python modules (scanner presets, phantoms, sinograms)
+    without building or loading its CUDA library."""
+    if "mlem_gb300" in sys.modules:
+        return sys.modules["mlem_gb300"]
+    spec = importlib.util.spec_from_file_location("mlem_gb300", PKG_DIR / "__init__.py",
+                                                  submodule_search_locations=[str(PKG_DIR)])
+    m = importlib.util.module_from_spec(spec)
+    sys.modules["mlem_gb300"] = m
+    spec.loader.exec_module(m)
+    return m
+
+
+def cpu_problem(pkg, name):
+    """The workload built on the host CPU by the oracle alone (the product
+    library is neither built nor loaded): the full matrix A from the oracle's
+    generator (bit-identical to the library's), Aᵀ by the oracle's stable
+    transpose, FP64 column sums, the seeded phantom's Poisson sinogram and the
+    reference initial image."""
     from oracle import oracle as O
     from mlem_gb300 import synth
-    geo = pkg.preset(name, row_stride=stride)
-    rp, col, val, cols = pkg.siddon_host(geo)
+    cfg = WORKLOADS[name]
+    geo = pkg.preset(name)
+    t0 = time.perf_counter()
+    rp, col, val, cols = O.siddon(geo)
     AT = O.transpose(rp, col, val, cols)
-    norm = O.colsum(rp, col, val, cols)
-    xt = synth.phantom(pkg.preset(name), WORKLOADS[name]["shapes"], seed=1)
-    g = synth.poisson_sinogram(synth.project_host(rp, col, val, xt), WORKLOADS[name]["total"] / stride, seed=2)
+    norm = O.colsum_t(AT, cols)
+    xt = synth.phantom(geo, cfg["shapes"], seed=1)
+    g = synth.poisson_sinogram(O.project_f64(rp, col, val, xt), cfg["total"], seed=2)
     f0 = np.full(cols, O.initial_value(g, norm), np.float32)
-    threads = O.lib().oracle_max_threads()
-    O.mlem_omp((rp, col, val), AT, g, norm, f0, 1, threads)  # warm-up
+    return dict(A=(rp, col, val), AT=AT, rows=len(rp) - 1, cols=cols, nnz=len(col), g=g, norm=norm, f0=f0,
+                prep_s=time.perf_counter() - t0)
+
+
+def cpu_iterations(P, iters, nthreads):
+    """Seconds per MLEM iteration of the oracle's OpenMP CSR MLEM (transposed
+    form, FP32 values and image, FP64 accumulation) on the full matrix."""
+    from oracle import oracle as O
     t0 = time.perf_counter()
-    O.mlem_omp((rp, col, val), AT, g, norm, f0, iters, threads)
-    dt = (time.perf_counter() - t0) / iters
-    t0 = time.perf_counter()
-    O.mlem_omp((rp, col, val), AT, g, norm, f0, 1, 1)
-    dt1 = time.perf_counter() - t0
-    return dict(nnz=len(col), rows=len(rp) - 1, seconds=dt, seconds_one_thread=dt1, cores=threads, stride=stride)
+    O.mlem_omp(P["A"], P["AT"], P["g"], P["norm"], P["f0"], iters, nthreads)
+    return (time.perf_counter() - t0) / iters
+
+
+def cpu_baseline(P, iters=3):
+    """The CPU baseline on the full matrix: all host threads (one warm-up
+    iteration, then `iters` timed) and one thread (one iteration)."""
+    from oracle import oracle as O
+    threads = O.max_threads()
+    cpu_iterations(P, 1, threads)
+    sec = cpu_iterations(P, iters, threads)
+    sec1 = cpu_iterations(P, 1, 1)
+    assert O.max_threads() == threads  # the one-thread run leaves the default alone
+    return {"value": 1.0 / sec, "unit": "iter/s", "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+            "one_thread_value": 1.0 / sec1,
+            "sample": f"full matrix ({P['rows']} rows, {P['nnz']} nnz): {iters} OpenMP MLEM iterations on "
+                      f"{threads} threads after 1 warm-up, and 1 iteration on 1 thread (FP32 values and image, "
+                      f"FP64 accumulation, transposed form)",
+            "input_prep_s": round(P["prep_s"], 1)}
+
+
+def repo_libraries():
+    """The shared libraries of this repository mapped into the process."""
+    try:
+        maps = Path("/proc/self/maps").read_text().splitlines()
+    except OSError:
+        return None
+    root = str(ROOT) + os.sep
+    return sorted({ln.split()[-1][len(root):] for ln in maps
+                   if ln.split() and ln.split()[-1].startswith(root) and ".so" in ln.split()[-1]})
+
+
+def workload_config(name, rows, cols, nnz, replicas, values="f32"):
+    """The `config` both arms print for a workload."""
+    return {"workload": name, "rows": rows, "cols": cols, "nnz": nnz, "values": values,
+            "l2": f"inputs larger than L2 ({8 * nnz / 1e9:.1f} GB matrix + {8 * nnz / 1e9:.1f} GB transpose)",
+            "replicas": replicas}
 
 
 def cpu_model() -> str:
@@ -241,70 +298,65 @@ def cpu_model() -> str:
 
 
 def run_reference(args):
-    """CPU implementation of the path on the host cores (oracle port)."""
+    """The CPU implementation of the path on the host cores (the oracle port:
+    the reference's MLEM loop exists only as CUDA kernels).  Inputs come from
+    the oracle's generator; the product library is not loaded.  Each step is
+    one MLEM iteration over the full matrix on all host threads."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    pkg = load_pkg()
+    from oracle import oracle as O
+    pkg = import_pkg()
     name = args.workload
-    full_rows = pkg.siddon_rows(pkg.preset(name))
-    stride = WORKLOADS[name]["cpu_stride"]
-    for _ in range(args.warmup):
-        pass
-    samples = []
-    for _ in range(args.steps):
-        samples.append(cpu_baseline(pkg, name, stride))
-    # full-matrix nnz estimated from the sample's nnz per row
-    s = samples[-1]
-    full_nnz = s["nnz"] * full_rows / s["rows"]
-    sec = statistics.median(x["seconds"] for x in samples) * full_nnz / s["nnz"]
-    value = 1.0 / sec
+    P = cpu_problem(pkg, name)
+    threads = O.max_threads()
+    for _ in range(max(1, args.warmup)):
+        cpu_iterations(P, 1, threads)
+    per_step = [cpu_iterations(P, 1, threads) for _ in range(args.steps)]
+    total = sum(per_step)
+    value = args.steps / total
+    sec1 = cpu_iterations(P, 1, 1)
     line = {
         "impl": "reference", "metric": "MLEM iterations/s", "value": value, "unit": "iter/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": total / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 values, f64 accumulation",
-        "data": "synthetic", "config": {"workload": name, "iterations_per_step": 1, "form": "fp32 plain"},
-        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": s["cores"], "kind": "port",
-                         "cpu_model": cpu_model(),
-                         "one_thread_value": 1.0 / (s["seconds_one_thread"] * full_nnz / s["nnz"]),
-                         "sample": f"every {stride}th LOR row ({s['rows']} rows, {s['nnz']} nnz), 1 iteration, "
-                                   f"time scaled by full/sample nnz"},
+        "data": "synthetic (seeded multi-ray Siddon matrix, ellipsoid phantom, Poisson sinogram)",
+        "config": workload_config(name, P["rows"], P["cols"], P["nnz"], args.gpus),
+        "iterations_per_step": 1,
+        "form": "CPU CSR MLEM, transposed form, natural layout",
+        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": threads, "kind": "port",
+                         "cpu_model": cpu_model(), "one_thread_value": 1.0 / sec1,
+                         "sample": f"full matrix ({P['rows']} rows, {P['nnz']} nnz), one MLEM iteration per step "
+                                   f"on {threads} threads; one_thread_value: one iteration on 1 thread",
+                         "step_ms": [round(x * 1e3, 2) for x in per_step], "input_prep_s": round(P["prep_s"], 1)},
         "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's MLEM loop exists only as CUDA kernels + NCCL; its CPU-side restatement "
                 "(oracle/mlem_oracle.c, pinned bit-exact to the reference's compiled kernels) is timed",
     }
     if not args.no_ref_cuda:
-        line["reference_cuda"] = reference_cuda(pkg, name, args)
+        line["reference_cuda"] = reference_cuda(P, name, args)
+    line["repo_libraries_mapped"] = repo_libraries()
     print(json.dumps(line), flush=True)
 
 
-def reference_cuda(pkg, name, args):
-    """The reference's kernel.cu on this GPU, launched as its main.cu loop does."""
+def reference_cuda(P, name, args):
+    """The reference's kernel.cu on this GPU, launched as its main.cu loop
+    does, on the inputs of the CPU arm."""
     try:
         import torch
         from oracle import ref_cuda
-        from oracle import oracle as O
-        from mlem_gb300 import synth
     except Exception as e:  # pragma: no cover
         return {"unavailable": f"import failed: {e}"}
     if not torch.cuda.is_available():
         return {"unavailable": "no CUDA device"}
     if not ref_cuda.available():
         return {"unavailable": "oracle/_ref/mlemref_kernels.cubin not built (needs the reference sources)"}
-    t0 = time.perf_counter()
-    geo = pkg.preset(name)
-    rp, col, val, cols = pkg.siddon_host(geo)
-    AT = O.transpose(rp, col, val, cols)
-    xt = synth.phantom(geo, WORKLOADS[name]["shapes"], seed=1)
-    g = synth.poisson_sinogram(synth.project_host(rp, col, val, xt), WORKLOADS[name]["total"], seed=2)
-    norm = O.colsum(rp, col, val, cols).astype(np.float32)
-    f0 = np.full(cols, O.initial_value(g, norm), np.float32)
-    prep = time.perf_counter() - t0
+    g, norm, f0, cols = P["g"], P["norm"], P["f0"], P["cols"]
     out = {"kind": "reference kernel.cu compiled unmodified for sm_103a; main.cu:302-449 loop replayed at 1 GPU "
                    "(blocksize 1024, secsize 5/5, host synchronisations and memsets included)",
-           "workload": name, "input_prep_s": round(prep, 1), "modes": {}}
+           "workload": name, "modes": {}}
     iters = max(3, min(args.steps, 10))
-    with ref_cuda.ReferenceCudaMLEM((rp, col, val), cols, AT) as R:
+    with ref_cuda.ReferenceCudaMLEM(P["A"], cols, P["AT"]) as R:
         for label, spmv, trans in (("csr_vector_trans", 1, 0), ("merge_trans", 0, 0),
                                    ("csr_vector_scatter", 1, 1), ("merge_scatter", 0, 1)):
             if spmv == 1 and not R.csr_vector_ok(trans):
@@ -626,6 +678,37 @@ def run_serving(pkg, torch, n_requests=300, rate=50.0, fp32_iter_s=None):
     return out
 
 
+def forms_summary(forms, fp32_rate):
+    """The headline figure of each form and its ratio to the FP32 plain path."""
+    out = {"fp32_plain_iter_s": round(fp32_rate, 2)}
+
+    def put(key, val, ratio_to=None, nd=2):
+        if val is None:
+            return
+        out[key] = round(val, nd)
+        if ratio_to:
+            out[key.replace("_s", "") + "_vs_fp32_plain"] = round(val / ratio_to, 3)
+
+    put("fp16_d16_images_iter_s", forms.get("fp16_trans", {}).get("images_iterations_per_s"), fp32_rate)
+    mid = forms.get("fp32_plain_cyl3d_mid", {}).get("images_iterations_per_s")
+    put("mid_fp32_plain_iter_s", mid)
+    b = forms.get("batched_fp16_64", {})
+    put("batched_fp16_64_images_iter_s", b.get("images_iterations_per_s"), mid)
+    modes = forms.get("modes_cyl3d_mid") or forms
+    for k in ("csr_vector_trans", "merge_trans", "csr_vector_scatter", "merge_scatter", "fused"):
+        if isinstance(modes.get(k), dict) and "iterations_per_s" in modes[k]:
+            out[f"mid_{k}_iter_s"] = round(modes[k]["iterations_per_s"], 1)
+    sv = forms.get("serving")
+    if sv:
+        out["serving"] = {k: (round(sv[k], 4) if isinstance(sv[k], float) else sv[k])
+                          for k in ("requests", "p50_latency_s", "p99_latency_s", "reconstructions_per_s",
+                                    "serial_fp32_reconstructions_per_s", "serial_fp32_sample") if k in sv}
+    sy = forms.get("symmetry", {}).get("fp32")
+    if sy:
+        out["symmetry_matrix_hat_fp32_iter_s"] = round(sy["autotuned"]["iterations_per_s"], 1)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -761,14 +844,13 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.values == "f32" else f"{args.values} values, f32 accumulation",
         "data": "synthetic (seeded multi-ray Siddon matrix, ellipsoid phantom, Poisson sinogram)",
-        "config": {"workload": name, "rows": m.rows, "cols": m.cols, "nnz": m.nnz, "iterations_per_step": iters,
-                   "form": (f"fp32 plain: {args.spmv} SpMV, {args.bp} BP, {args.layout} layout"
-                            if args.values == "f32" and not args.compress else
-                            f"{args.values} values{', D16 indices' if args.compress else ''}: {args.spmv} SpMV, "
-                            f"{args.bp} BP, {args.layout} layout"),
-                   "l2": "inputs larger than L2 "
-                   f"({(m.device_bytes) / 1e9:.1f} GB resident matrix)", "replicas": world,
-                   "matrix_generation_s": round(t_gen, 2)},
+        "config": workload_config(name, m.rows, m.cols, m.nnz, world, args.values),
+        "iterations_per_step": iters,
+        "form": (f"fp32 plain: {args.spmv} SpMV, {args.bp} BP, {args.layout} layout"
+                 if args.values == "f32" and not args.compress else
+                 f"{args.values} values{', D16 indices' if args.compress else ''}: {args.spmv} SpMV, "
+                 f"{args.bp} BP, {args.layout} layout"),
+        "device_bytes": m.device_bytes, "matrix_generation_s": round(t_gen, 2),
         "e2e": {"value": e2e_value, "unit": "iter/s", "h2d_bytes_per_step": int(4 * m.rows + 4 * m.cols),
                 "d2h_bytes_per_step": int(4 * m.cols)},
         "gpu_launches": int(launches),
@@ -803,15 +885,20 @@ def main():
             line["forms"]["serving"] = run_serving(pkg, torch, fp32_iter_s=rates)
         line["forms"]["symmetry"] = run_symmetry(pkg, torch, name)
     if rank == 0 and not args.no_cpu:
-        cb = cpu_baseline(pkg, name, WORKLOADS[name]["cpu_stride"])
-        full_nnz = line["config"]["nnz"]
-        sec_full = cb["seconds"] * full_nnz / cb["nnz"]
-        line["cpu_baseline"] = {"value": 1.0 / sec_full, "unit": "iter/s", "cores": cb["cores"], "kind": "port",
-                                "cpu_model": cpu_model(),
-                                "one_thread_value": 1.0 / (cb["seconds_one_thread"] * full_nnz / cb["nnz"]),
-                                "sample": f"every {cb['stride']}th LOR row of the same matrix ({cb['rows']} rows, "
-                                          f"{cb['nnz']} nnz), 1 OpenMP MLEM iteration (FP32 values, FP64 "
-                                          f"accumulation), time scaled by {full_nnz}/{cb['nnz']} nnz"}
+        P = cpu_problem(pkg, name)
+        line["cpu_baseline"] = cpu_baseline(P)
+        del P
+    if "forms" in line:
+        # the per-variant detail goes to a file; the line ends with the headline of each form
+        forms = line.pop("forms")
+        detail = ROOT / "gpurun_out" / f"bench_forms_{name}.json"
+        try:
+            detail.parent.mkdir(exist_ok=True)
+            detail.write_text(json.dumps(forms, indent=1))
+            line["forms_detail"] = str(detail.relative_to(ROOT))
+        except OSError:
+            line["forms"] = forms
+        line["forms_summary"] = forms_summary(forms, value / world)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -286,11 +286,12 @@ mlem_status mlem_merge_path_search(const uint64_t* rowptr_dev, uint32_t rows, ui
  * device array inside the library, held by every GPU that loads the library
  * until exit, which limits rows + nnz to about 220 million at secsize 5
  * (larger inputs return MLEM_EINVAL with the limit in the message).  The
- * first call on a device looks the array up (cudaGetSymbolAddress); make that
- * first call before any stream capture.  All calls share the array: calls
- * that overlap on the GPU race, so serialise them.  Device pointers in, ratio
- * f32[rows] out; requires col[e] < cols; secsize 1..125; asynchronous on
- * `stream`. */
+ * first call on a device looks the array up (cudaGetSymbolAddress), and again
+ * after the device's context was re-created (cudaDeviceReset); make that first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race, so serialise them.  Device pointers in, ratio
+ * f32[rows] out; nnz must equal rowptr_dev[rows] and col[e] < cols; secsize
+ * 1..125; asynchronous on `stream`. */
 mlem_status mlem_forward_project_merge_noalloc(const uint64_t* rowptr_dev, const uint32_t* col_dev,
                                                const float* val_dev, uint32_t rows, uint32_t cols,
                                                uint64_t nnz, const float* x_dev, const int32_t* g_dev,

@@ -22,6 +22,8 @@
 #include <omp.h>
 #endif
 
+int oracle_max_threads(void);
+
 static inline float madd(float acc, float a, float b, int use_fma) {
     return use_fma ? fmaf(a, b, acc) : acc + a * b;
 }
@@ -218,6 +220,18 @@ void oracle_colsum_f64(const uint64_t* rowptr, const uint32_t* col, const float*
     free(acc);
 }
 
+/* The same FP64 column sums from the rows of Aᵀ (OpenMP over columns).  A
+ * stable transpose lists each column's entries in increasing row order, the
+ * order oracle_colsum_f64 adds them in, so both give the same bits. */
+void oracle_colsum_f64_t(const uint64_t* rowptrT, const float* valT, uint32_t cols, float* norm) {
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t c = 0; c < (int64_t)cols; ++c) {
+        double s = 0.0;
+        for (uint64_t e = rowptrT[c]; e < rowptrT[c + 1]; ++e) s += (double)valT[e];
+        norm[c] = (float)s;
+    }
+}
+
 /* Initial image value (main.cu:83-97): FP32 running sum of norm, int sum of
  * g, init = sum_g / sum_norm. */
 float oracle_initial_value(const int32_t* g, uint32_t rows, const float* norm, uint32_t cols) {
@@ -339,18 +353,18 @@ void oracle_mlem_omp(const uint64_t* rowptr, const uint32_t* col, const float* v
                      const uint64_t* rowptrT, const uint32_t* colT, const float* valT,
                      const int32_t* g, const float* norm, float* f, uint32_t rows, uint32_t cols,
                      uint32_t iterations, int nthreads) {
-#ifdef _OPENMP
-    if (nthreads > 0) omp_set_num_threads(nthreads);
-#endif
+    /* the thread count applies to this call only (num_threads clauses), so a
+     * one-thread run leaves the process default untouched */
+    const int T = nthreads > 0 ? nthreads : oracle_max_threads();
     float* ratio = (float*)malloc(sizeof(float) * (rows ? rows : 1));
     for (uint32_t it = 0; it < iterations; ++it) {
-#pragma omp parallel for schedule(dynamic, 1024)
+#pragma omp parallel for num_threads(T) schedule(dynamic, 1024)
         for (int64_t r = 0; r < (int64_t)rows; ++r) {
             double s = 0.0;
             for (uint64_t e = rowptr[r]; e < rowptr[r + 1]; ++e) s += (double)val[e] * (double)f[col[e]];
             ratio[r] = s != 0.0 ? (float)((double)g[r] / s) : 0.0f;
         }
-#pragma omp parallel for schedule(dynamic, 1024)
+#pragma omp parallel for num_threads(T) schedule(dynamic, 1024)
         for (int64_t c = 0; c < (int64_t)cols; ++c) {
             double s = 0.0;
             for (uint64_t e = rowptrT[c]; e < rowptrT[c + 1]; ++e) s += (double)valT[e] * (double)ratio[colT[e]];
@@ -367,4 +381,15 @@ int oracle_max_threads(void) {
 #else
     return 1;
 #endif
+}
+
+/* y = A·x in FP64 (OpenMP over rows): the expected counts of a phantom. */
+void oracle_project_f64(const uint64_t* rowptr, const uint32_t* col, const float* val, const float* x,
+                        uint32_t rows, double* y) {
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t r = 0; r < (int64_t)rows; ++r) {
+        double s = 0.0;
+        for (uint64_t e = rowptr[r]; e < rowptr[r + 1]; ++e) s += (double)val[e] * (double)x[col[e]];
+        y[r] = s;
+    }
 }

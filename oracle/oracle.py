@@ -32,6 +32,11 @@ _SIGS = {
     "oracle_mlem_f64_t": (None, [_P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P]),
     "oracle_mlem_omp": (None, [_P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
     "oracle_max_threads": (C.c_int, []),
+    "oracle_colsum_f64_t": (None, [_P, _P, C.c_uint32, _P]),
+    "oracle_project_f64": (None, [_P, _P, _P, _P, C.c_uint32, _P]),
+    "oracle_siddon_rows": (C.c_uint64, [_P]),
+    "oracle_siddon_count": (C.c_int, [_P, _P]),
+    "oracle_siddon_fill": (C.c_int, [_P, _P, _P, _P]),
 }
 _REF_SIGS = {
     "ref_sptrans": (None, [C.c_int, C.c_uint32, C.c_uint32, C.c_uint64, _P, _P, _P, _P, _P, _P]),
@@ -146,6 +151,14 @@ def colsum(rowptr, col, val, cols, f64=True):
     return out
 
 
+def colsum_t(AT, cols):
+    """FP64 column sums from the rows of Aᵀ (parallel; the same bits as colsum)."""
+    rpt, vt = c64(AT[0]), f32(AT[2])
+    out = np.zeros(cols, np.float32)
+    lib().oracle_colsum_f64_t(P(rpt), P(vt), cols, P(out))
+    return out
+
+
 def initial_value(g, norm):
     g, norm = i32(g), f32(norm)
     return lib().oracle_initial_value(P(g), len(g), P(norm), len(norm))
@@ -197,6 +210,50 @@ def mlem_omp(A, AT, g, norm, f0, iterations, nthreads=0):
     lib().oracle_mlem_omp(P(rp), P(c), P(v), P(rpt), P(ct), P(vt), P(g), P(norm), P(f), len(rp) - 1, len(norm),
                           iterations, nthreads)
     return f
+
+
+class Geometry(C.Structure):
+    """Scanner description of the synthetic matrices (the field layout of the
+    library's mlem_geometry)."""
+    _fields_ = [("det_per_ring", C.c_uint32), ("n_rings", C.c_uint32), ("radius", C.c_float),
+                ("ring_pitch", C.c_float), ("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32),
+                ("vx", C.c_float), ("vy", C.c_float), ("vz", C.c_float), ("row_stride", C.c_uint32),
+                ("row_phase", C.c_uint32), ("sub_t", C.c_uint32), ("sub_z", C.c_uint32),
+                ("width_t", C.c_float), ("width_z", C.c_float)]
+
+
+def geometry_of(geo) -> Geometry:
+    """An oracle Geometry from any object with the same attribute names."""
+    return Geometry(*[getattr(geo, n) for n, _ in Geometry._fields_])
+
+
+def siddon(geo):
+    """The synthetic system matrix of a scanner, generated on the host CPU
+    (OpenMP).  Returns (rowptr u64[rows+1], col u32[nnz], val f32[nnz], cols)."""
+    G = geometry_of(geo)
+    rows = int(lib().oracle_siddon_rows(C.byref(G)))
+    if rows == 0 and not (G.det_per_ring and G.n_rings):
+        raise ValueError("invalid geometry")
+    rp = np.zeros(rows + 1, np.uint64)
+    if lib().oracle_siddon_count(C.byref(G), P(rp)) != 0:
+        raise ValueError("invalid geometry")
+    nnz = int(rp[-1])
+    col = np.empty(max(nnz, 1), np.uint32)
+    val = np.empty(max(nnz, 1), np.float32)
+    lib().oracle_siddon_fill(C.byref(G), P(rp), P(col), P(val))
+    return rp, col[:nnz], val[:nnz], int(G.nx * G.ny * G.nz)
+
+
+def project_f64(rowptr, col, val, x):
+    """A·x in FP64 (OpenMP over rows)."""
+    rowptr, col, val, x = c64(rowptr), c32(col), f32(val), f32(x)
+    y = np.zeros(len(rowptr) - 1, np.float64)
+    lib().oracle_project_f64(P(rowptr), P(col), P(val), P(x), len(rowptr) - 1, P(y))
+    return y
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())
 
 
 def rel_l2(a, b):

@@ -2,8 +2,9 @@
 oracle/_ref/mlemref_kernels.cubin.
 
 Test infrastructure: the library pins the oracle (mlem_oracle.c) against the
-reference itself.  It needs the reference checkout at REF (default
-/root/reference) and x86 g++ (sptrans.h includes immintrin.h); it is built
+reference itself.  It needs the reference checkout (the directory named by
+the MLEM_REFERENCE environment variable, else a checkout named `reference`
+beside this repository) and x86 g++ (sptrans.h includes immintrin.h); it is built
 only where the reference is present and never shipped or imported by the
 product.  Sources compiled directly from where they lie:
   kernel.cu                                   (as C++, CUDA built-ins emulated
@@ -20,7 +21,7 @@ import subprocess
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF = Path(os.environ.get("MLEM_REFERENCE", "/root/reference"))
+REF = Path(os.environ["MLEM_REFERENCE"]) if os.environ.get("MLEM_REFERENCE") else HERE.parent.parent / "reference"
 OUT = HERE / "_ref" / "libmlemref.so"
 
 

@@ -79,3 +79,42 @@ def test_full_size_symmetric_against_fp64_oracle(pkg, O, cuda, name):
           f"image rel L2 FP32 {e32:.3e}, FP16 {e16:.3e}; log-likelihood max rel error FP32 {l32:.3e}")
     assert e32 < 1e-5 and l32 < 1e-6
     assert e16 < 1e-3
+
+
+def test_batched_fp16_at_its_configured_scale_against_fp64_oracle(pkg, O, cuda):
+    """The batched form where FP16 error would grow: the 3-D mid matrix with
+    FP16 values (locality layout), sinograms of the batched workload (phantom
+    seeds 1000 + k, totals log-uniform in [1e5, 1e9] drawn with seed 7), 200
+    iterations.  The instances with the smallest, the median and the largest
+    total run in one batch with five more of the workload, and each image is
+    compared with the FP64 oracle on the FP32 matrix.  Bar: 1e-3 relative L2."""
+    from mlem_gb300 import synth
+    torch = cuda
+    geo = pkg.preset("cyl3d_mid")
+    iters = 200
+    totals = np.exp(np.random.Generator(np.random.PCG64(7)).uniform(np.log(1e5), np.log(1e9), 64))
+    order = np.argsort(totals)
+    picks = [int(order[0]), int(order[32]), int(order[-1])] + [int(k) for k in order[1:64:13][:5]]
+    m32 = pkg.Matrix.generate(geo, layout=pkg.LAYOUT_LOCALITY)
+    dz = torch.zeros(m32.rows, dtype=torch.int32, device="cuda")
+    ratio = torch.zeros(m32.rows, dtype=torch.float32, device="cuda")
+    fp = torch.zeros(m32.rows, dtype=torch.float32, device="cuda")
+    G = []
+    for k in picks:
+        xt = torch.from_numpy(synth.phantom(geo, 20, seed=1000 + k)).cuda()
+        m32.forward_project(xt.data_ptr(), dz.data_ptr(), ratio.data_ptr(), fp.data_ptr())
+        torch.cuda.synchronize()
+        G.append(synth.poisson_sinogram(fp.cpu().numpy().astype(np.float64), totals[k], seed=2000 + k))
+    G = np.stack(G)
+    F0 = np.stack([np.full(m32.cols, m32.initial_value(g), np.float32) for g in G])
+    A, AT, norm = m32.csr(), m32.transpose(), m32.norm()
+    m32.close()
+    m16 = pkg.Matrix.generate(geo, value_type=pkg.VAL_F16, layout=pkg.LAYOUT_LOCALITY)
+    out = m16.batch_run(G, np.full(len(G), iters, np.uint32), f0=F0)
+    m16.close()
+    for j, label in enumerate(("smallest", "median", "largest")):
+        ref = O.mlem_f64_t(A, AT, G[j], norm, F0[j], iters)
+        err = O.rel_l2(out[j], ref)
+        print(f"\nbatched FP16, {label} total {totals[picks[j]]:.3g}, {iters} iterations: "
+              f"image rel L2 vs FP64 oracle {err:.3e}")
+        assert err < 1e-3

@@ -7,10 +7,14 @@ On the same inputs the library's image must agree with the reference's
 within the FP32 tolerance (1e-5 relative L2); the reference's own
 run-to-run spread (its FP32 atomics) is printed as the noise floor.  Skipped
 where the cubin was not built (it needs the reference sources)."""
+import sys
+from pathlib import Path
+
 import numpy as np
 import pytest
 
-from conftest import golden_csr, problem
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+from conftest import golden_csr, problem  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -63,6 +67,36 @@ def test_reference_cuda_kernels_match_golden_fixtures(pkg, golden, refcuda, O, s
                 want = golden[f"{name}/mlem_s{spmv}_t{using_trans}_ss5x5_it{iters}"]
                 got = R.run(g, norm, f0, iters, spmv=spmv, using_trans=using_trans)
                 assert O.rel_l2(got, want) < TOL_F32, (name, iters)
+
+
+@pytest.mark.parametrize("name", ["cyl3d_mid", "cyl3d_12gb"])
+def test_library_matches_reference_cuda_kernels_full_size(pkg, O, cuda, refcuda, name):
+    """The configured matrices at full size (3-D mid: 662,976 x 784,000,
+    208 M nonzeros; 12 GB class: 2,653,056 x 2,560,000, 1.43 B nonzeros; both
+    dimensions multiples of 32, so every mode of the reference may run), 100
+    iterations in all four argv[7]/argv[8] modes: the library in its
+    benchmark layout (locality) against the reference's kernels on the natural
+    matrix, same sinogram, sensitivity and initial image."""
+    from test_gpu_full_size import WORKLOADS, _sinogram
+    geo = pkg.preset(name)
+    iters = 100
+    m = pkg.Matrix.generate(geo, layout=pkg.LAYOUT_LOCALITY)
+    g = _sinogram(pkg, m, geo, WORKLOADS[name], cuda)
+    f0 = np.full(m.cols, m.initial_value(g), np.float32)
+    norm = m.norm().astype(np.float32)
+    got = {mode: m.run(g, iters, f0=f0, spmv=mode[0], bp_mode=mode[1]) for mode in MODES}
+    A, AT = m.csr(), m.transpose()
+    m.close()
+    with refcuda.ReferenceCudaMLEM(A, len(norm), AT) as R:
+        del A, AT
+        for spmv, using_trans in MODES:
+            assert R.csr_vector_ok(using_trans)
+            ref = R.run(g, norm, f0, iters, spmv=spmv, using_trans=using_trans)
+            ref_again = R.run(g, norm, f0, iters, spmv=spmv, using_trans=using_trans)
+            err = O.rel_l2(got[(spmv, using_trans)], ref)
+            print(f"\n{name} spmv={spmv} trans={using_trans}, {iters} iterations: library vs reference CUDA "
+                  f"{err:.2e}, reference run-to-run {O.rel_l2(ref_again, ref):.2e}")
+            assert err < TOL_F32
 
 
 def test_reference_cuda_timing_runs(pkg, O, refcuda):
