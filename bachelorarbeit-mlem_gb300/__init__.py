@@ -51,7 +51,7 @@ class MatrixOpts(C.Structure):
     _fields_ = [("value_type", C.c_int), ("build_transpose", C.c_uint32), ("norm", C.c_void_p),
                 ("device", C.c_int), ("compress_indices", C.c_uint32), ("interleave", C.c_uint32),
                 ("layout", C.c_uint32), ("grid_nx", C.c_uint32), ("grid_ny", C.c_uint32), ("grid_nz", C.c_uint32),
-                ("symmetry", C.c_uint32)]
+                ("symmetry", C.c_uint32), ("sym_det_per_ring", C.c_uint32), ("sym_rings", C.c_uint32)]
 
 
 class MatrixInfo(C.Structure):
@@ -101,7 +101,8 @@ class Geometry(C.Structure):
 
 
 class BatchOpts(C.Structure):
-    _fields_ = [("tile", C.c_uint32), ("use_graph", C.c_uint32), ("order_by_iterations", C.c_uint32)]
+    _fields_ = [("tile", C.c_uint32), ("use_graph", C.c_uint32), ("order_by_iterations", C.c_uint32),
+                ("form", C.c_uint32)]
 
 
 class ServerOpts(C.Structure):
@@ -312,13 +313,21 @@ class Matrix:
 
     @classmethod
     def from_csr(cls, rowptr, col, val, cols: int, value_type=VAL_F32, build_transpose=True, norm=None,
-                 device=0, compress=False, interleave=False, layout=LAYOUT_NATURAL, grid=None) -> "Matrix":
-        """grid = (nx, ny, nz) of the voxel columns, needed by the locality layout."""
+                 device=0, compress=False, interleave=False, layout=LAYOUT_NATURAL, grid=None,
+                 symmetry=None) -> "Matrix":
+        """grid = (nx, ny, nz) of the voxel columns, needed by the locality layout
+        and by symmetry.  symmetry = (det_per_ring, rings): the rows are the
+        detector pairs of that ring scanner and the matrix is exactly invariant
+        under its 16 symmetries (checked; MlemError EINVAL otherwise); the
+        compact symmetric operands are built beside the unchanged matrix."""
         rowptr = _arr(rowptr, np.uint64)
         col = _arr(col, np.uint32)
         val = _arr(val, np.float32)
         csr = CsrHost(len(rowptr) - 1, cols, len(col), _ptr(rowptr), _ptr(col), _ptr(val))
-        o, keep = cls._opts(value_type, build_transpose, norm, device, compress, interleave, layout, grid)
+        o, keep = cls._opts(value_type, build_transpose, norm, device, compress, interleave, layout, grid,
+                            symmetry=symmetry is not None)
+        if symmetry is not None:
+            o.sym_det_per_ring, o.sym_rings = (int(v) for v in symmetry)
         h = C.c_void_p()
         _check(load_library().mlem_matrix_create(C.byref(csr), C.byref(o), C.byref(h)))
         return cls(h.value)
@@ -448,19 +457,21 @@ class Matrix:
                                                 C.byref(ro), C.c_void_p(stream or None)))
 
     def batch_run(self, g, iterations, f0=None, tile=0, use_graph=True, order_by_iterations=True,
-                  stats=False):
+                  stats=False, form=0):
         """Reconstructs g[count][rows] with per-instance iteration counts (mlem_batch_run).
 
         The tile's slots (8/16/32; 0 = autotuned) form a pool that the instances
         enter longest first (order_by_iterations); an image is bit-identical in
-        every tile and slot, and to the same sinogram run alone."""
+        every tile and slot, and to the same sinogram run alone.  form: 0 =
+        autotuned, 1 = one CUDA graph per iteration, 2 = persistent (the
+        iterations between two refills in one cooperative launch)."""
         g = _arr(g, np.int32)
         count = g.shape[0]
         its = _arr(iterations, np.uint32)
         assert its.size == count
         f0a = None if f0 is None else _arr(f0, np.float32)
         out = np.zeros((count, self.cols), np.float32)
-        o = BatchOpts(tile, int(use_graph), int(order_by_iterations))
+        o = BatchOpts(tile, int(use_graph), int(order_by_iterations), int(form))
         st = Stats()
         _check(load_library().mlem_batch_run(self._h, count, _ptr(g), _ptr(its), _ptr(f0a), C.byref(o),
                                              _ptr(out), C.byref(st)))

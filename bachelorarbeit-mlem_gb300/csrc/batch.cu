@@ -29,9 +29,18 @@ namespace {
 // Row sums of one warp's 32/W rows (segment seg of W lanes holds row `row`,
 // `ok` = the row exists).  On return the lanes sl < W/4 of each segment hold
 // instances 4*sl..4*sl+3 of their row.
-template <typename V, int W>
+// NC: the gathered state is read through the read-only path (__ldg), which is
+// right only when no block of the same launch writes it; the persistent loop
+// below, whose phases write what the next phase gathers, uses plain loads.
+template <bool NC>
+__device__ __forceinline__ float4 load_state(const float* p) {
+    if (NC) return __ldg(reinterpret_cast<const float4*>(p));
+    return *reinterpret_cast<const float4*>(p);
+}
+
+template <typename V, int W, bool NC = true>
 __device__ __forceinline__ void batch_rows(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
-                                           const V* __restrict__ val, const float* __restrict__ x, uint32_t BT,
+                                           const V* __restrict__ val, const float* x, uint32_t BT,
                                            uint32_t row, bool ok, int lane, float4& acc) {
     constexpr int LPN = W / 4;  // lanes per nonzero
     constexpr int E = 32 / W;   // entries per lane per 32-entry chunk
@@ -72,7 +81,7 @@ __device__ __forceinline__ void batch_rows(const uint64_t* __restrict__ rowptr, 
             const uint32_t ck = __shfl_sync(0xffffffffu, c[(4 * q) / W], src);
             const float vk = __shfl_sync(0xffffffffu, v[(4 * q) / W], src);
             if (4 * q < r) {
-                const float4 xv = __ldg(reinterpret_cast<const float4*>(x + (uint64_t)ck * BT + q4));
+                const float4 xv = load_state<NC>(x + (uint64_t)ck * BT + q4);
                 acc.x = fmaf(vk, xv.x, acc.x);
                 acc.y = fmaf(vk, xv.y, acc.y);
                 acc.z = fmaf(vk, xv.z, acc.z);
@@ -198,6 +207,107 @@ __global__ void k_batch_tick(uint32_t* remaining, uint32_t BT) {
     if (threadIdx.x < BT && remaining[threadIdx.x] > 0) remaining[threadIdx.x] -= 1;
 }
 
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide barrier of a cooperative launch: barrier k of the launch is
+// passed once `count` (zeroed before the launch) reaches k * gridDim.x.  Every
+// wait is bounded: after kBarrierWaitNs, or as soon as another block has given
+// up, the block sets *err and the caller returns, so a failure ends the launch
+// with an error flag the host reads instead of a hang.
+constexpr uint64_t kBarrierWaitNs = 2000000000ull;  // 2 s; a phase takes milliseconds
+
+__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned k, int* err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(count, 1u);
+        const unsigned target = k * gridDim.x;
+        const uint64_t t0 = globaltimer_ns();
+        int ok = 1;
+        while (ld_acquire_u32(count) < target) {
+            if (*(volatile int*)err != 0 || globaltimer_ns() - t0 > kBarrierWaitNs) {
+                atomicExch(err, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Persistent batched MLEM: `steps` iterations of the tile in one cooperative
+// launch (every block resident).  Per iteration: forward projection and
+// correlation over all rows of A, grid barrier, back projection and update
+// over all rows of Aᵀ for the slots with iterations left, grid barrier, tick
+// of the per-slot counters by block 0.  The warps of the grid stride over
+// row groups; each row is summed exactly as by k_batch_fp / k_batch_bp (same
+// chains, same order), so an instance's bits do not depend on which kernel
+// form runs it.
+template <typename V, int W>
+__global__ void __launch_bounds__(256, 6)
+k_batch_loop(const uint64_t* __restrict__ rp, const uint32_t* __restrict__ ix, const V* __restrict__ vl,
+             uint32_t rows, const uint64_t* __restrict__ rpT, const uint32_t* __restrict__ ixT,
+             const V* __restrict__ vlT, uint32_t cols, const float* __restrict__ norm, uint32_t BT,
+             const int32_t* __restrict__ g, float* f, float* ratio, uint32_t* remaining, uint32_t steps,
+             unsigned* count, int* err) {
+    constexpr uint32_t RPW = 32 / W;  // rows per warp
+    const int lane = threadIdx.x & 31, sl = lane % W;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned k = 0;
+    for (uint32_t step = 0; step < steps; ++step) {
+        for (uint64_t first = warp * RPW; first < rows; first += nwarps * RPW) {
+            const uint64_t row = first + lane / W;
+            const bool ok = row < rows;
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            batch_rows<V, W, false>(rp, ix, vl, f, BT, (uint32_t)row, ok, lane, acc);
+            if (ok && sl < W / 4) {
+                const uint64_t o = row * BT + sl * 4;
+                const int4 gg = *reinterpret_cast<const int4*>(g + o);
+                *reinterpret_cast<float4*>(ratio + o) = make_float4(correl1(gg.x, acc.x), correl1(gg.y, acc.y),
+                                                                    correl1(gg.z, acc.z), correl1(gg.w, acc.w));
+            }
+        }
+        if (!grid_barrier(count, ++k, err)) return;
+        for (uint64_t first = warp * RPW; first < cols; first += nwarps * RPW) {
+            const uint64_t c = first + lane / W;
+            const bool ok = c < cols;
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            batch_rows<V, W, false>(rpT, ixT, vlT, ratio, BT, (uint32_t)c, ok, lane, acc);
+            if (ok && sl < W / 4) {
+                const uint64_t o = c * BT + sl * 4;
+                const uint4 rem = *reinterpret_cast<const uint4*>(remaining + sl * 4);
+                const float n = norm[c];
+                float4 fv = *reinterpret_cast<const float4*>(f + o);
+                if (rem.x) fv.x = update1(fv.x, acc.x, n);
+                if (rem.y) fv.y = update1(fv.y, acc.y, n);
+                if (rem.z) fv.z = update1(fv.z, acc.z, n);
+                if (rem.w) fv.w = update1(fv.w, acc.w, n);
+                *reinterpret_cast<float4*>(f + o) = fv;
+            }
+        }
+        if (!grid_barrier(count, ++k, err)) return;
+        // every block has read `remaining` for this iteration; the tick is seen
+        // by the next back projection through the next barrier
+        if (blockIdx.x == 0 && threadIdx.x < BT && remaining[threadIdx.x] > 0) remaining[threadIdx.x] -= 1;
+    }
+}
+
 template <int W, typename V>
 void fp_w(const DevCsr& A, const BatchArgs& b, L2Window win, cudaStream_t s) {
     launch_ex(k_batch_fp<V, W>, dim3(ceil_div_u((uint64_t)A.nrows * W, 256)), dim3(256), 0, s, win, A.rowptr,
@@ -295,6 +405,65 @@ void launch_batch_bp_update(const DevCsr& AT, const float* norm, const BatchArgs
         case MLEM_VAL_F32: bp_v<float>(AT, norm, b, win, s); break;
         case MLEM_VAL_F16: bp_v<__half>(AT, norm, b, win, s); break;
         default: bp_v<__nv_bfloat16>(AT, norm, b, win, s);
+    }
+}
+
+namespace {
+
+template <typename V, int W>
+void loop_w(const DevCsr& A, const DevCsr& AT, const float* norm, const BatchArgs& b, uint32_t steps,
+            unsigned* count, int* err, cudaStream_t s) {
+    auto kern = k_batch_loop<V, W>;
+    // one resident wave: every block must be on the GPU at once for the barriers
+    static const int bps = [kern] {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 256, 0) != cudaSuccess) {
+            cudaGetLastError();
+            b = 0;
+        }
+        return b;
+    }();
+    int dev = 0, sms = 0;
+    MLEM_CUDA(cudaGetDevice(&dev));
+    MLEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    MLEM_REQUIRE(bps >= 1, MLEM_EUNSUPPORTED, "persistent batch kernel does not fit on an SM");
+    MLEM_CUDA(cudaMemsetAsync(count, 0, sizeof(unsigned), s));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(bps * sms));
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    MLEM_CUDA(cudaLaunchKernelEx(&cfg, kern, (const uint64_t*)A.rowptr, (const uint32_t*)A.idx,
+                                 static_cast<const V*>(A.val), A.nrows, (const uint64_t*)AT.rowptr,
+                                 (const uint32_t*)AT.idx, static_cast<const V*>(AT.val), AT.nrows, norm, b.tile,
+                                 b.g, b.f, b.ratio, b.remaining, steps, count, err));
+    count_launch();
+}
+
+template <typename V>
+void loop_v(const DevCsr& A, const DevCsr& AT, const float* norm, const BatchArgs& b, uint32_t steps,
+            unsigned* count, int* err, cudaStream_t s) {
+    switch (b.width()) {
+        case 4: loop_w<V, 4>(A, AT, norm, b, steps, count, err, s); break;
+        case 8: loop_w<V, 8>(A, AT, norm, b, steps, count, err, s); break;
+        case 16: loop_w<V, 16>(A, AT, norm, b, steps, count, err, s); break;
+        default: loop_w<V, 32>(A, AT, norm, b, steps, count, err, s);
+    }
+}
+
+}  // namespace
+
+void launch_batch_loop(const DevCsr& A, const DevCsr& AT, const float* norm, const BatchArgs& b, uint32_t steps,
+                       unsigned* count, int* err, cudaStream_t s) {
+    if (steps == 0 || A.nrows == 0) return;
+    switch (A.vt) {
+        case MLEM_VAL_F32: loop_v<float>(A, AT, norm, b, steps, count, err, s); break;
+        case MLEM_VAL_F16: loop_v<__half>(A, AT, norm, b, steps, count, err, s); break;
+        default: loop_v<__nv_bfloat16>(A, AT, norm, b, steps, count, err, s);
     }
 }
 

@@ -102,7 +102,7 @@ struct MergePlan {
     size_t smem = 0;
     // true: the row-parallel tile kernel (library-owned, padded operands);
     // false: the per-thread walk over shared-memory products (any arrays)
-    bool rows_kernel = false;
+    int rows_kernel = 0;         // 0: per-thread walk (k_merge_tile), 1: rows to groups, 2: nonzero-balanced
     void release();
 };
 // Builds the tile partition of `op` for a section size (device allocations).
@@ -178,6 +178,14 @@ void check_symmetric_geometry(const mlem_geometry& geo);
 // A^ (symmetrised from the canonical rows), its transpose, and the compact
 // operands; A and AT must be empty.
 void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y, cudaStream_t s);
+// The same from a caller's matrix (host CSR c, already uploaded as `user`):
+// its rows must be the D(D-1)/2 detector pairs of a ring scanner with dpr
+// detectors per ring and `rings` rings, its columns an n x n x nz grid.  A^ is
+// built from the canonical rows of c and must equal `user` bit for bit (the
+// matrix is invariant under the 16 transformations); otherwise MLEM_EINVAL.
+// A, AT and y are filled either way and owned by the caller.
+void build_symmetric_checked(const mlem_csr_host& c, const DevCsr& user, uint32_t n, uint32_t nz, uint32_t dpr,
+                             uint32_t rings, DevCsr& A, DevCsr& AT, SymOps& y, cudaStream_t s);
 void lower_symmetric_values(SymOps& y, mlem_value_type vt, cudaStream_t s);
 // Forward (transposed = false: Correl or Raw epilogue) or back projection
 // (true: Update or Raw) through the compact operands; natural order in and out.
@@ -232,6 +240,12 @@ inline uint32_t batch_width(uint32_t tile, uint32_t active) {
     a.active = active;
     return a.width();
 }
+// `steps` whole iterations of the tile (FP, BP + update, tick) in one
+// persistent cooperative launch with grid-wide barriers; count (one word,
+// zeroed here before the launch) carries the barriers, *err becomes 1 if a
+// barrier wait ran out (the launch then ends early).  Needs Aᵀ.
+void launch_batch_loop(const DevCsr& A, const DevCsr& AT, const float* norm, const BatchArgs& b, uint32_t steps,
+                       unsigned* count, int* err, cudaStream_t s);
 // ratio[r][b] = g[r][b] / (A f_b)[r] for the slots b < width().
 void launch_batch_fp(const DevCsr& A, const BatchArgs& b, L2Window win, cudaStream_t s);
 // f_b = f_b * (Aᵀ ratio_b) / norm for slots b < width() with remaining > 0.

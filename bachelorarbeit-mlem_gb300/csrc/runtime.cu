@@ -60,7 +60,10 @@ void BatchState::alloc(uint32_t rows, uint32_t cols, uint32_t t, bool scatter) {
     MLEM_CUDA(cudaMemset(g, 0, sizeof(int32_t) * R * t));
     MLEM_CUDA(cudaMemset(f, 0, sizeof(float) * C * t));
     MLEM_CUDA(cudaMemset(remaining, 0, sizeof(uint32_t) * 32));
-    bytes = (sizeof(int32_t) + sizeof(float)) * R * t + sizeof(float) * C * t + 4 * R + 4 * C + 128;
+    MLEM_CUDA(cudaMalloc(&bar, 64));
+    MLEM_CUDA(cudaMemset(bar, 0, 64));
+    err = reinterpret_cast<int*>(reinterpret_cast<char*>(bar) + 32);
+    bytes = (sizeof(int32_t) + sizeof(float)) * R * t + sizeof(float) * C * t + 4 * R + 4 * C + 192;
     if (scatter) {
         MLEM_CUDA(cudaMalloc(&bp, sizeof(float) * C * t));
         MLEM_CUDA(cudaMemset(bp, 0, sizeof(float) * C * t));
@@ -78,6 +81,7 @@ void BatchState::release() {
     cudaFree(remaining);
     cudaFree(stage_g);
     cudaFree(stage_f);
+    cudaFree(bar);
     *this = BatchState();
 }
 
@@ -162,8 +166,57 @@ const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
     auto it = plans.find(secsize);
     if (it != plans.end()) return it->second;
     MergePlan p;
-    merge_plan_build(transposed ? m->AT : m->A, secsize, p, m->stream);
-    MLEM_CUDA(cudaStreamSynchronize(m->stream));
+    const DevCsr& op = transposed ? m->AT : m->A;
+    cudaStream_t s = m->stream;
+    merge_plan_build(op, secsize, p, s);
+    MLEM_CUDA(cudaStreamSynchronize(s));
+    if (p.rows_kernel && op.nnz) {
+        // the faster of the two row-parallel tile kernels (rows handed to lane
+        // groups, or nonzeros cut evenly between them) on this operand, timed
+        // with a Raw epilogue on an image of ones
+        float *x = nullptr, *y = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        float best = 1e30f;
+        int pick = p.rows_kernel;
+        try {
+            MLEM_CUDA(cudaMalloc(&x, sizeof(float) * std::max<uint32_t>(op.ncols, 1)));
+            MLEM_CUDA(cudaMalloc(&y, sizeof(float) * std::max<uint32_t>(op.nrows, 1)));
+            std::vector<float> ones(std::max<uint32_t>(op.ncols, 1), 1.0f);
+            MLEM_CUDA(cudaMemcpyAsync(x, ones.data(), sizeof(float) * ones.size(), cudaMemcpyHostToDevice, s));
+            MLEM_CUDA(cudaEventCreate(&e0));
+            MLEM_CUDA(cudaEventCreate(&e1));
+            EpiArgs e;
+            e.kind = Epi::Raw;
+            e.out = y;
+            for (int kind : {1, 2}) {
+                p.rows_kernel = kind;
+                launch_merge_spmv(op, p, x, e, L2Window{}, s);
+                MLEM_CUDA(cudaEventRecord(e0, s));
+                for (int q = 0; q < 2; ++q) launch_merge_spmv(op, p, x, e, L2Window{}, s);
+                MLEM_CUDA(cudaEventRecord(e1, s));
+                MLEM_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                MLEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    pick = kind;
+                }
+            }
+        } catch (...) {
+            cudaStreamSynchronize(s);
+            cudaFree(x);
+            cudaFree(y);
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            p.release();
+            throw;
+        }
+        cudaFree(x);
+        cudaFree(y);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        p.rows_kernel = pick;
+    }
     return plans.emplace(secsize, p).first->second;
 }
 
@@ -741,6 +794,8 @@ static void upload_csr(const mlem_csr_host* c, DevCsr& A, cudaStream_t s) {
 }
 
 mlem_matrix* create_matrix_filled(const mlem_matrix_opts& o, const std::function<void(mlem_matrix*)>& fill) {
+    MLEM_REQUIRE(!o.symmetry, MLEM_EUNSUPPORTED,
+                 "symmetry: create the matrix from host CSR arrays (mlem_matrix_create) or a geometry");
     DeviceGuard dg(o.device);
     mlem_matrix* m = new_matrix(o);
     try {
@@ -786,6 +841,7 @@ void mlem_matrix_opts_default(mlem_matrix_opts* o) {
     o->layout = MLEM_LAYOUT_NATURAL;
     o->grid_nx = o->grid_ny = o->grid_nz = 0;
     o->symmetry = 0;
+    o->sym_det_per_ring = o->sym_rings = 0;
 }
 
 void mlem_run_opts_default(mlem_run_opts* o) {
@@ -817,8 +873,28 @@ mlem_status mlem_matrix_create(const mlem_csr_host* csr, const mlem_matrix_opts*
         mlem_matrix* m = new_matrix(o);
         try {
             upload_csr(csr, m->A, m->stream);
-            maybe_apply_layout(m, o, o.grid_nx, o.grid_ny, o.grid_nz, {});
-            postprocess_matrix(m, o);
+            if (o.symmetry) {
+                MLEM_REQUIRE(o.layout == MLEM_LAYOUT_NATURAL, MLEM_EUNSUPPORTED,
+                             "symmetry keeps the natural layout (the symmetric operands are compact already)");
+                MLEM_REQUIRE(o.grid_nx == o.grid_ny, MLEM_EUNSUPPORTED, "symmetry needs a square voxel grid");
+                DevCsr hat;
+                try {
+                    build_symmetric_checked(*csr, m->A, o.grid_nx, o.grid_nz, o.sym_det_per_ring, o.sym_rings, hat,
+                                            m->AT, m->sym, m->stream);
+                } catch (...) {
+                    free_csr(hat);
+                    throw;
+                }
+                free_csr(hat);  // equal to the caller's matrix, which stays
+                m->has_t = true;
+                postprocess_matrix(m, o);
+                lower_symmetric_values(m->sym, o.value_type, m->stream);
+                sym_set_norm(m->sym, m->norm, m->stream);
+                MLEM_CUDA(cudaStreamSynchronize(m->stream));
+            } else {
+                maybe_apply_layout(m, o, o.grid_nx, o.grid_ny, o.grid_nz, {});
+                postprocess_matrix(m, o);
+            }
         } catch (...) {
             destroy_matrix(m);
             throw;

@@ -83,6 +83,8 @@ struct BatchState {
     uint32_t* remaining = nullptr;  // [tile]
     int32_t* stage_g = nullptr;  // [rows] contiguous staging
     float* stage_f = nullptr;    // [cols] contiguous staging
+    unsigned* bar = nullptr;     // barrier word of the persistent form
+    int* err = nullptr;          // set by the persistent form when a barrier wait ran out
     cudaGraphExec_t graph[4] = {};  // one iteration per projection width 4/8/16/32
     uint64_t graph_nodes[4] = {};
     uint64_t bytes = 0;
@@ -133,6 +135,7 @@ struct mlem_matrix {
     mlem::Workspace ws;
     std::map<uint32_t, mlem::MergePlan> plan_A, plan_AT;
     uint32_t batch_tile = 0;          // autotuned batch tile (0 = not yet)
+    uint32_t batch_form = 0;          // autotuned batch form: 1 graphs, 2 persistent (0 = not yet)
     bool tuned[2] = {false, false};   // csr-vector configuration of A / Aᵀ measured
     mlem::ProjCfg proj[2];
     std::mutex mu;

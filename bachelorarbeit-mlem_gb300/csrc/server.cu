@@ -25,6 +25,9 @@
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <numeric>
 #include <thread>
 #include <unordered_map>
@@ -57,7 +60,32 @@ void batch_get_slot(const mlem_matrix* m, const BatchState& b, uint32_t slot, fl
 
 static uint64_t batch_state_bytes(uint32_t rows, uint32_t cols, uint32_t tile, bool scatter) {
     const uint64_t R = std::max<uint32_t>(rows, 1), C = std::max<uint32_t>(cols, 1);
-    return 8ull * R * tile + 4ull * C * tile * (scatter ? 2 : 1) + 4 * R + 4 * C + 128;
+    return 8ull * R * tile + 4ull * C * tile * (scatter ? 2 : 1) + 4 * R + 4 * C + 192;
+}
+
+// Persistent launches of a device never run at the same time: a cooperative
+// launch fills the GPU, and two of them partly resident could wait on each
+// other's blocks.  mlem_batch_run holds this lock for the whole run when it
+// uses the persistent form.
+static std::mutex& persistent_lock(int dev) {
+    static std::mutex mu;
+    static std::map<int, std::unique_ptr<std::mutex>> locks;
+    std::lock_guard<std::mutex> lk(mu);
+    auto& p = locks[dev];
+    if (!p) p.reset(new std::mutex());
+    return *p;
+}
+
+// Reads and clears the error word of the persistent form (after the stream
+// has drained).
+static void check_persistent(const BatchState& b, cudaStream_t s) {
+    int e = 0;
+    MLEM_CUDA(cudaMemcpyAsync(&e, b.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MLEM_CUDA(cudaStreamSynchronize(s));
+    if (e) {
+        MLEM_CUDA(cudaMemsetAsync(b.err, 0, sizeof(int), s));
+        fail(MLEM_ETIMEOUT, "persistent batch kernel: a grid barrier wait ran out");
+    }
 }
 
 // Replays one iteration of the tile as a CUDA graph (one per projection
@@ -141,6 +169,47 @@ static uint32_t autotune_tile(mlem_matrix* m, cudaStream_t s) {
     return best;
 }
 
+// Picks the faster form at the matrix's tile: per-iteration launches or the
+// persistent loop (same data as autotune_tile, every slot idle).
+static uint32_t autotune_form(mlem_matrix* m, uint32_t tile, cudaStream_t s) {
+    if (m->batch_form) return m->batch_form;
+    if (!m->has_t) return m->batch_form = 1;  // the persistent form needs Aᵀ
+    const uint32_t rows = m->A.nrows, cols = m->A.ncols;
+    BatchState b;
+    cudaEvent_t e[3] = {};
+    float ms_graph = 0.f, ms_loop = 0.f;
+    try {
+        b.alloc(rows, cols, tile, false);
+        std::vector<float> ones((uint64_t)std::max(cols, 1u) * tile, 1.0f);
+        std::vector<int32_t> cnt((uint64_t)std::max(rows, 1u) * tile, 1);
+        MLEM_CUDA(cudaMemcpyAsync(b.f, ones.data(), sizeof(float) * ones.size(), cudaMemcpyHostToDevice, s));
+        MLEM_CUDA(cudaMemcpyAsync(b.g, cnt.data(), sizeof(int32_t) * cnt.size(), cudaMemcpyHostToDevice, s));
+        for (auto& ev : e) MLEM_CUDA(cudaEventCreate(&ev));
+        std::lock_guard<std::mutex> lk(persistent_lock(m->device));
+        enqueue_batch_iteration(m, b, s, tile);
+        launch_batch_loop(m->A, m->AT, m->norm, b.args(tile), 1, b.bar, b.err, s);  // warm-up
+        MLEM_CUDA(cudaEventRecord(e[0], s));
+        for (int q = 0; q < 3; ++q) enqueue_batch_iteration(m, b, s, tile);
+        MLEM_CUDA(cudaEventRecord(e[1], s));
+        launch_batch_loop(m->A, m->AT, m->norm, b.args(tile), 3, b.bar, b.err, s);
+        MLEM_CUDA(cudaEventRecord(e[2], s));
+        MLEM_CUDA(cudaEventSynchronize(e[2]));
+        cudaEventElapsedTime(&ms_graph, e[0], e[1]);
+        cudaEventElapsedTime(&ms_loop, e[1], e[2]);
+        check_persistent(b, s);
+    } catch (...) {
+        cudaStreamSynchronize(s);
+        for (auto& ev : e)
+            if (ev) cudaEventDestroy(ev);
+        b.release();
+        throw;
+    }
+    for (auto& ev : e) cudaEventDestroy(ev);
+    b.release();
+    m->batch_form = ms_loop < ms_graph ? 2 : 1;
+    return m->batch_form;
+}
+
 }  // namespace mlem
 
 using namespace mlem;
@@ -148,16 +217,54 @@ using namespace mlem;
 // ------------------------------------------------------------------ server
 namespace {
 
-enum class ReqState { Queued, Running, Done, Cancelled };
+enum class ReqState { Queued, Running, Finishing, Done, Cancelled };
+
+// Page-locked host buffers of one size (a sinogram or an image of one
+// matrix), handed out to requests and returned when a request is done with
+// them.  At most `cap` buffers exist; beyond that requests use pageable
+// memory.  Guarded by the server mutex.
+struct PinnedPool {
+    size_t bytes = 0;
+    uint32_t cap = 0, made = 0;
+    std::vector<void*> free_list, all;
+    // a free buffer, or nullptr with `make` set when the caller should
+    // allocate a new one (outside the lock), or nullptr when the pool is full
+    void* take(bool& make) {
+        make = false;
+        if (!free_list.empty()) {
+            void* p = free_list.back();
+            free_list.pop_back();
+            return p;
+        }
+        if (made < cap) {
+            ++made;
+            make = true;
+        }
+        return nullptr;
+    }
+    void give(void* p) {
+        if (p) free_list.push_back(p);
+    }
+    void release() {
+        for (void* p : all) cudaFreeHost(p);
+        all.clear();
+        free_list.clear();
+        made = 0;
+    }
+};
 
 struct Request {
     uint64_t id = 0;
     uint32_t mid = 0;
-    std::vector<int32_t> g;
+    std::vector<int32_t> g;       // the sinogram when no pinned buffer was free
+    int32_t* pin_g = nullptr;     // the sinogram in a pinned buffer of the matrix's pool
+    float init = 0.f;             // reference initial value, computed at submit
     uint32_t iters = 0;
     std::chrono::steady_clock::time_point t_submit, t_done;
     ReqState state = ReqState::Queued;
-    std::vector<float> result;
+    std::vector<float> result;    // the image when no pinned buffer was free
+    float* pin_f = nullptr;       // the image in a pinned buffer (copy in flight while Finishing)
+    cudaEvent_t copied = nullptr; // recorded after the image's device-to-host copy
 };
 
 struct MatrixSlots {
@@ -170,6 +277,7 @@ struct MatrixSlots {
     std::vector<uint64_t> slot_req;   // 0 = free
     std::vector<uint32_t> slot_left;
     uint32_t tile = 0;
+    PinnedPool pin_g, pin_f;          // staging of sinograms in and images out
     bool active() const { return active_slots() > 0; }
     // one past the highest occupied slot
     uint32_t active_slots() const {
@@ -196,10 +304,34 @@ struct mlem_server {
     uint64_t budget = 0, in_use = 0;
     mlem_server_stats st{};
     std::string worker_error;
+    std::vector<uint64_t> finishing;    // requests whose image copy is in flight
+    std::vector<cudaEvent_t> spare_events;
 
     void run();
     bool admit_locked();
+    void finish_locked();
 };
+
+// Requests whose image copy to pinned memory has completed become Done.
+void mlem_server::finish_locked() {
+    for (size_t k = 0; k < finishing.size();) {
+        Request& r = reqs[finishing[k]];
+        const cudaError_t q = cudaEventQuery(r.copied);
+        if (q == cudaErrorNotReady) {
+            ++k;
+            continue;
+        }
+        MLEM_CUDA(q);
+        spare_events.push_back(r.copied);
+        r.copied = nullptr;
+        r.t_done = std::chrono::steady_clock::now();
+        r.state = ReqState::Done;
+        ++st.completed;
+        finishing[k] = finishing.back();
+        finishing.pop_back();
+        cv_done.notify_all();
+    }
+}
 
 bool mlem_server::admit_locked() {
     bool any = false;
@@ -241,11 +373,13 @@ bool mlem_server::admit_locked() {
             ++it;
             continue;
         }
-        MLEM_CUDA(cudaMemcpyAsync(ms.bs.stage_g, r.g.data(), sizeof(int32_t) * rows, cudaMemcpyHostToDevice,
-                                  ms.stream));
-        const float init = reference_initial_value(ms.m, r.g.data());
-        batch_put_slot(ms.m, ms.bs, (uint32_t)slot, ms.bs.stage_g, init, nullptr, r.iters, ms.stream);
-        MLEM_CUDA(cudaStreamSynchronize(ms.stream));  // stage_g is reused by the next admission
+        // Stream order makes the staging safe without waiting: the next
+        // admission's copy into stage_g runs after this slot's put kernel.
+        // A pinned sinogram is copied asynchronously; a pageable one is
+        // consumed before cudaMemcpyAsync returns.
+        MLEM_CUDA(cudaMemcpyAsync(ms.bs.stage_g, r.pin_g ? (const void*)r.pin_g : (const void*)r.g.data(),
+                                  sizeof(int32_t) * rows, cudaMemcpyHostToDevice, ms.stream));
+        batch_put_slot(ms.m, ms.bs, (uint32_t)slot, ms.bs.stage_g, r.init, nullptr, r.iters, ms.stream);
         ms.slot_req[slot] = r.id;
         ms.slot_left[slot] = r.iters;
         r.state = ReqState::Running;
@@ -281,19 +415,51 @@ void mlem_server::run() {
                     ++st.iterations_done;
                     if (--ms.slot_left[b] > 0) continue;
                     Request& r = reqs[ms.slot_req[b]];
+                    // the sinogram's copy completed before this iteration ran
+                    ms.pin_g.give(r.pin_g);
+                    r.pin_g = nullptr;
                     batch_get_slot(ms.m, ms.bs, b, ms.bs.stage_f, ms.stream);
-                    r.result.resize(cols);
-                    MLEM_CUDA(cudaMemcpyAsync(r.result.data(), ms.bs.stage_f, sizeof(float) * cols,
-                                              cudaMemcpyDeviceToHost, ms.stream));
-                    MLEM_CUDA(cudaStreamSynchronize(ms.stream));
-                    r.t_done = std::chrono::steady_clock::now();
-                    r.state = ReqState::Done;
+                    bool make = false;
+                    r.pin_f = static_cast<float*>(ms.pin_f.take(make));
+                    if (make) {
+                        void* p = nullptr;
+                        if (cudaHostAlloc(&p, ms.pin_f.bytes, cudaHostAllocPortable) == cudaSuccess) {
+                            ms.pin_f.all.push_back(p);
+                            r.pin_f = static_cast<float*>(p);
+                        } else {
+                            cudaGetLastError();
+                            --ms.pin_f.made;
+                        }
+                    }
+                    if (r.pin_f) {
+                        // asynchronous: the request is Done once the copy's event fires
+                        MLEM_CUDA(cudaMemcpyAsync(r.pin_f, ms.bs.stage_f, sizeof(float) * cols,
+                                                  cudaMemcpyDeviceToHost, ms.stream));
+                        if (spare_events.empty()) {
+                            cudaEvent_t e = nullptr;
+                            MLEM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+                            spare_events.push_back(e);
+                        }
+                        r.copied = spare_events.back();
+                        spare_events.pop_back();
+                        MLEM_CUDA(cudaEventRecord(r.copied, ms.stream));
+                        r.state = ReqState::Finishing;
+                        finishing.push_back(r.id);
+                    } else {
+                        r.result.resize(cols);
+                        MLEM_CUDA(cudaMemcpyAsync(r.result.data(), ms.bs.stage_f, sizeof(float) * cols,
+                                                  cudaMemcpyDeviceToHost, ms.stream));
+                        MLEM_CUDA(cudaStreamSynchronize(ms.stream));
+                        r.t_done = std::chrono::steady_clock::now();
+                        r.state = ReqState::Done;
+                        ++st.completed;
+                        cv_done.notify_all();
+                    }
                     ms.slot_req[b] = 0;
                     --st.active;
-                    ++st.completed;
-                    cv_done.notify_all();
                 }
             }
+            finish_locked();
             // 2. admissions into free slots of idle matrices
             admit_locked();
             // 3. next iteration of every idle matrix with work
@@ -305,6 +471,7 @@ void mlem_server::run() {
                 }
                 any_inflight |= ms.inflight;
             }
+            any_inflight |= !finishing.empty();
             if (!any_inflight) {
                 cv_work.wait_for(lk, std::chrono::milliseconds(20));
                 continue;
@@ -321,6 +488,7 @@ void mlem_batch_opts_default(mlem_batch_opts* o) {
     o->tile = 0;
     o->use_graph = 1;
     o->order_by_iterations = 1;
+    o->form = 0;
 }
 
 mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, const uint32_t* iterations,
@@ -333,11 +501,16 @@ mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, con
         if (opts) o = *opts;
         MLEM_REQUIRE(o.tile == 0 || o.tile == 8 || o.tile == 16 || o.tile == 32, MLEM_EINVAL,
                      "batch tile must be 0 (autotune), 8, 16 or 32");
+        MLEM_REQUIRE(o.form <= 2, MLEM_EINVAL, "batch form must be 0 (autotune), 1 (graphs) or 2 (persistent)");
+        MLEM_REQUIRE(o.form != 2 || m->has_t, MLEM_EINVAL, "the persistent batch form needs the transpose");
         std::lock_guard<std::mutex> lk(m->mu);
         DeviceGuard dg(m->device);
         cudaStream_t s = m->stream;
         const uint32_t rows = m->A.nrows, cols = m->A.ncols;
         const uint32_t tile = o.tile ? o.tile : autotune_tile(m, s);
+        const bool persistent = (o.form ? o.form : autotune_form(m, tile, s)) == 2;
+        std::unique_lock<std::mutex> plk(persistent_lock(m->device), std::defer_lock);
+        if (persistent) plk.lock();
         std::vector<uint32_t> order(count);
         std::iota(order.begin(), order.end(), 0u);
         if (o.order_by_iterations)
@@ -455,8 +628,17 @@ mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, con
                 for (uint32_t b = 0; b < tile; ++b)
                     if (slot_inst[b] >= 0) act = b + 1;
                 if (act == 0) break;
-                batch_step(m, bs, s, o.use_graph != 0, act);
-                ++step;
+                if (persistent) {
+                    // every iteration up to the next slot refill in one launch
+                    uint64_t n = ~0ull;
+                    for (uint32_t b = 0; b < act; ++b)
+                        if (slot_inst[b] >= 0) n = std::min(n, slot_end[b] - step);
+                    launch_batch_loop(m->A, m->AT, m->norm, bs.args(act), (uint32_t)n, bs.bar, bs.err, s);
+                    step += n;
+                } else {
+                    batch_step(m, bs, s, o.use_graph != 0, act);
+                    ++step;
+                }
                 for (uint32_t b = 0; b < act; ++b) {
                     while (slot_inst[b] >= 0 && slot_end[b] == step) {
                         hand_back(b);
@@ -466,6 +648,7 @@ mlem_status mlem_batch_run(mlem_matrix* m, uint32_t count, const int32_t* g, con
             }
             MLEM_CUDA(cudaEventRecord(e1, s));
             MLEM_CUDA(cudaStreamSynchronize(s));
+            if (persistent) check_persistent(bs, s);
             for (uint32_t j = 0; j < kRing; ++j) drain_f(j);
             float ms = 0.f;
             cudaEventElapsedTime(&ms, e0, e1);
@@ -548,6 +731,10 @@ mlem_status mlem_server_add_matrix(mlem_server* s, mlem_matrix* m, uint32_t* mat
         ms.tile = s->opts.slots_per_matrix ? s->opts.slots_per_matrix : autotune_tile(m, m->stream);
         ms.slot_req.assign(ms.tile, 0);
         ms.slot_left.assign(ms.tile, 0);
+        // pinned staging for up to two slot-fulls of sinograms and images
+        ms.pin_g.bytes = sizeof(int32_t) * (size_t)std::max<uint32_t>(m->A.nrows, 1);
+        ms.pin_f.bytes = sizeof(float) * (size_t)std::max<uint32_t>(m->A.ncols, 1);
+        ms.pin_g.cap = ms.pin_f.cap = 2 * ms.tile;
         // smaller matrices can get higher stream priority, so their short
         // iterations are scheduled ahead of the CTAs of large ones.  The
         // default raises only small matrices: a matrix with requests in flight
@@ -571,22 +758,53 @@ mlem_status mlem_server_add_matrix(mlem_server* s, mlem_matrix* m, uint32_t* mat
 mlem_status mlem_server_submit(mlem_server* s, uint32_t matrix_id, const int32_t* g, uint32_t iterations,
                                uint64_t* request_id) {
     return guarded([&] {
+        const auto t_submit = std::chrono::steady_clock::now();
         MLEM_REQUIRE(s && g && request_id, MLEM_EINVAL, "NULL argument");
         MLEM_REQUIRE(iterations > 0, MLEM_EINVAL, "iterations must be > 0");
-        std::lock_guard<std::mutex> lk(s->mu);
-        MLEM_REQUIRE(matrix_id < s->mats.size(), MLEM_EINVAL, "unknown matrix id");
-        if (!s->worker_error.empty()) fail(MLEM_ECUDA, "server worker stopped: " + s->worker_error);
-        if (s->queue.size() >= s->opts.queue_capacity) {
-            ++s->st.rejected;
-            fail(MLEM_EBUSY, "server queue full");
+        uint32_t rows = 0;
+        const mlem_matrix* mat = nullptr;
+        int32_t* pin = nullptr;
+        bool make = false;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            MLEM_REQUIRE(matrix_id < s->mats.size(), MLEM_EINVAL, "unknown matrix id");
+            if (!s->worker_error.empty()) fail(MLEM_ECUDA, "server worker stopped: " + s->worker_error);
+            if (s->queue.size() >= s->opts.queue_capacity) {
+                ++s->st.rejected;
+                fail(MLEM_EBUSY, "server queue full");
+            }
+            MatrixSlots& ms = s->mats[matrix_id];
+            mat = ms.m;
+            rows = ms.m->A.nrows;
+            pin = static_cast<int32_t*>(ms.pin_g.take(make));
         }
+        // Outside the lock, so the worker keeps running: the sinogram goes to
+        // a pinned buffer of the matrix (an asynchronous copy at admission) or,
+        // when the pool is used up, to pageable memory; its sum gives the
+        // reference initial value.
         Request r;
-        r.id = s->next_id++;
+        if (make) {
+            DeviceGuard dg(s->device);
+            void* p = nullptr;
+            if (cudaHostAlloc(&p, sizeof(int32_t) * (size_t)rows, cudaHostAllocPortable) == cudaSuccess)
+                pin = static_cast<int32_t*>(p);
+            else
+                cudaGetLastError();
+        }
+        if (pin) std::memcpy(pin, g, sizeof(int32_t) * (size_t)rows);
+        else r.g.assign(g, g + rows);
+        r.pin_g = pin;
+        r.init = reference_initial_value(mat, g);
         r.mid = matrix_id;
-        const uint32_t rows = s->mats[matrix_id].m->A.nrows;
-        r.g.assign(g, g + rows);
         r.iters = iterations;
-        r.t_submit = std::chrono::steady_clock::now();
+        r.t_submit = t_submit;
+        std::lock_guard<std::mutex> lk(s->mu);
+        MatrixSlots& ms = s->mats[matrix_id];
+        if (make) {
+            if (pin) ms.pin_g.all.push_back(pin);
+            else --ms.pin_g.made;
+        }
+        r.id = s->next_id++;
         *request_id = r.id;
         s->queue.push_back(r.id);
         s->reqs.emplace(r.id, std::move(r));
@@ -629,9 +847,19 @@ mlem_status mlem_server_wait(mlem_server* s, uint64_t request_id, float* f_out, 
             if (!s->worker_error.empty()) fail(MLEM_ECUDA, "server worker stopped: " + s->worker_error);
             MLEM_REQUIRE(ok, MLEM_ETIMEOUT, "request not finished within the timeout");
         }
-        if (f_out) std::memcpy(f_out, r.result.data(), sizeof(float) * r.result.size());
         if (latency_s) *latency_s = std::chrono::duration<double>(r.t_done - r.t_submit).count();
+        const uint32_t mid = r.mid;
+        const size_t cols = s->mats[mid].m->A.ncols;
+        float* pin = r.pin_f;
+        std::vector<float> result = std::move(r.result);
         s->reqs.erase(request_id);
+        // the image leaves the pinned buffer outside the lock
+        lk.unlock();
+        if (f_out) std::memcpy(f_out, pin ? pin : result.data(), sizeof(float) * cols);
+        if (pin) {
+            lk.lock();
+            s->mats[mid].pin_f.give(pin);
+        }
     });
 }
 
@@ -643,6 +871,8 @@ mlem_status mlem_server_cancel(mlem_server* s, uint64_t request_id) {
         MLEM_REQUIRE(it != s->reqs.end(), MLEM_EINVAL, "unknown request id");
         MLEM_REQUIRE(it->second.state == ReqState::Queued, MLEM_EINVAL, "request is not queued");
         s->queue.erase(std::remove(s->queue.begin(), s->queue.end(), request_id), s->queue.end());
+        s->mats[it->second.mid].pin_g.give(it->second.pin_g);
+        it->second.pin_g = nullptr;
         it->second.state = ReqState::Cancelled;
         --s->st.queued;
         ++s->st.cancelled;
@@ -672,9 +902,14 @@ mlem_status mlem_server_destroy(mlem_server* s) {
         for (auto& ms : s->mats) {
             if (ms.stream) cudaStreamSynchronize(ms.stream);
             ms.bs.release();
+            ms.pin_g.release();
+            ms.pin_f.release();
             if (ms.done) cudaEventDestroy(ms.done);
             if (ms.stream) cudaStreamDestroy(ms.stream);
         }
+        for (auto& kv : s->reqs)
+            if (kv.second.copied) cudaEventDestroy(kv.second.copied);
+        for (cudaEvent_t e : s->spare_events) cudaEventDestroy(e);
         delete s;
     });
 }

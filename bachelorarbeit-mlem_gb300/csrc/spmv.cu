@@ -262,11 +262,59 @@ k_csrvec_pipe(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ 
     }
 }
 
+// One 16-byte reduction into bp[4g .. 4g+3]: red.global.add.v4.f32 (one L2
+// atomic operation for four floats) where the group lies inside bp and bp is
+// 16-byte aligned (a caller's output pointer may not be), else the components
+// that carry a product one by one.
+__device__ __forceinline__ void red_group(float* __restrict__ bp, uint32_t ncols, uint32_t g, const float a[4],
+                                          unsigned used) {
+    const uint32_t c0 = g << 2;
+    if (c0 + 3 < ncols && (reinterpret_cast<uintptr_t>(bp) & 15u) == 0) {
+        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(bp + c0), "f"(a[0]), "f"(a[1]),
+                     "f"(a[2]), "f"(a[3])
+                     : "memory");
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (used & (1u << j)) atomicAdd(bp + c0 + j, a[j]);
+    }
+}
+
+// Scatters the products p[k] of four consecutive entries of a row (those
+// with base + k in [s, t)) into bp.  A row's columns ascend, so entries whose
+// columns share a 16-byte group (column >> 2) are adjacent: each group goes
+// out as one vector reduction, with zeros in its unused components (adding
+// +0.0 leaves a sum unchanged).  Duplicate columns are summed first.  In the
+// 3-D scanners about 0.6 reductions are issued per nonzero instead of 1.
+__device__ __forceinline__ void scatter4(float* __restrict__ bp, uint32_t ncols, const uint4& c, const float p[4],
+                                         uint64_t base, uint64_t s, uint64_t t) {
+    const uint32_t cs[4] = {c.x, c.y, c.z, c.w};
+    float a[4] = {0.f, 0.f, 0.f, 0.f};
+    unsigned used = 0;
+    uint32_t grp = 0xffffffffu;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (!in_row(base + k, s, t)) continue;
+        const uint32_t g = cs[k] >> 2, j = cs[k] & 3u;
+        if (g != grp) {
+            if (used) red_group(bp, ncols, grp, a, used);
+            a[0] = a[1] = a[2] = a[3] = 0.f;
+            used = 0;
+            grp = g;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (j == (uint32_t)q) a[q] = __fadd_rn(a[q], p[k]);
+        used |= 1u << j;
+    }
+    if (used) red_group(bp, ncols, grp, a, used);
+}
+
 template <typename V, int LPR>
 __global__ void __launch_bounds__(256)
 k_scatter(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
           const V* __restrict__ val, const float* __restrict__ ratio, uint32_t nrows,
-          float* __restrict__ bp) {
+          float* __restrict__ bp, uint32_t ncols) {
     const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t row = gt / LPR;
     const int sub = threadIdx.x & (LPR - 1);
@@ -278,11 +326,10 @@ k_scatter(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
     for (uint64_t v = (s >> 2) + sub; v < ((t + 3) >> 2); v += LPR) {
         Vec4<V> p;
         p.load(idx4, val, v);
-        const uint64_t b = v << 2;
-        const uint32_t cs[4] = {p.c.x, p.c.y, p.c.z, p.c.w};
+        float prod[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (in_row(b + k, s, t)) atomicAdd(bp + cs[k], __fmul_rn(p.a[k], r));
+        for (int k = 0; k < 4; ++k) prod[k] = __fmul_rn(p.a[k], r);
+        scatter4(bp, ncols, p.c, prod, v << 2, s, t);
     }
 }
 
@@ -293,7 +340,7 @@ template <typename V>
 __global__ void __launch_bounds__(256)
 k_fused(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
         const V* __restrict__ val, const float* __restrict__ x, const int32_t* __restrict__ g,
-        uint32_t nrows, float* __restrict__ bp, float* __restrict__ fwproj) {
+        uint32_t nrows, float* __restrict__ bp, float* __restrict__ fwproj, uint32_t ncols) {
     constexpr int Q = 4;
     const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -333,21 +380,19 @@ k_fused(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
     for (int q = 0; q < Q; ++q) {
         const uint64_t v = v0 + lane + 32 * q;
         if (v < v1) {
-            const uint64_t b = v << 2;
-            const uint32_t cs[4] = {keep[q].c.x, keep[q].c.y, keep[q].c.z, keep[q].c.w};
+            float prod[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (in_row(b + k, s, t)) atomicAdd(bp + cs[k], __fmul_rn(keep[q].a[k], r));
+            for (int k = 0; k < 4; ++k) prod[k] = __fmul_rn(keep[q].a[k], r);
+            scatter4(bp, ncols, keep[q].c, prod, v << 2, s, t);
         }
     }
     for (uint64_t v = v0 + lane + 32 * Q; v < v1; v += 32) {
         Vec4<V> p;
         p.load(idx4, val, v);
-        const uint64_t b = v << 2;
-        const uint32_t cs[4] = {p.c.x, p.c.y, p.c.z, p.c.w};
+        float prod[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (in_row(b + k, s, t)) atomicAdd(bp + cs[k], __fmul_rn(p.a[k], r));
+        for (int k = 0; k < 4; ++k) prod[k] = __fmul_rn(p.a[k], r);
+        scatter4(bp, ncols, p.c, prod, v << 2, s, t);
     }
 }
 
@@ -521,7 +566,7 @@ void scatter_dispatch(const DevCsr& A, const float* ratio, float* bp, int lanes,
     auto go = [&](auto kern, int lpr) {
         const uint64_t threads = (uint64_t)A.nrows * lpr;
         launch_ex(kern, dim3(ceil_div_u(threads, 256)), dim3(256), 0, s, win, A.rowptr, A.idx, val,
-                  ratio, A.nrows, bp);
+                  ratio, A.nrows, bp, A.ncols);
     };
     if (lanes >= 32) go(k_scatter<V, 32>, 32);
     else if (lanes >= 16) go(k_scatter<V, 16>, 16);
@@ -591,15 +636,15 @@ void launch_fused_fp_scatter(const DevCsr& A, const float* x, const int32_t* g, 
     switch (A.vt) {
         case MLEM_VAL_F32:
             launch_ex(k_fused<float>, grid, block, 0, s, win, A.rowptr, A.idx,
-                      (const float*)A.val, x, g, A.nrows, bp, fwproj);
+                      (const float*)A.val, x, g, A.nrows, bp, fwproj, A.ncols);
             break;
         case MLEM_VAL_F16:
             launch_ex(k_fused<__half>, grid, block, 0, s, win, A.rowptr, A.idx,
-                      (const __half*)A.val, x, g, A.nrows, bp, fwproj);
+                      (const __half*)A.val, x, g, A.nrows, bp, fwproj, A.ncols);
             break;
         default:
             launch_ex(k_fused<__nv_bfloat16>, grid, block, 0, s, win, A.rowptr, A.idx,
-                      (const __nv_bfloat16*)A.val, x, g, A.nrows, bp, fwproj);
+                      (const __nv_bfloat16*)A.val, x, g, A.nrows, bp, fwproj, A.ncols);
     }
 }
 

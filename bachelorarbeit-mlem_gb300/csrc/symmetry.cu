@@ -39,7 +39,10 @@
 #include "kernels.cuh"
 
 #include <algorithm>
+#include <cstring>
+#include <functional>
 #include <map>
+#include <string>
 #include <vector>
 
 namespace mlem {
@@ -611,14 +614,16 @@ void check_symmetric_geometry(const mlem_geometry& g) {
     MLEM_REQUIRE(g.vx == g.vy, MLEM_EUNSUPPORTED, "symmetry needs square voxels in the transaxial plane");
 }
 
-void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y, cudaStream_t s) {
-    check_symmetric_geometry(geo);
-    SymMaps M;
-    M.n = geo.nx;
-    M.nz = geo.nz;
-    M.dpr = geo.det_per_ring;
-    M.rings = geo.n_rings;
-    M.D = M.dpr * M.rings;
+namespace {
+
+// The rows of the given canonical LORs (host CSR over the full column range).
+using CanonicalRows = std::function<void(const std::vector<uint64_t>& lors, std::vector<uint64_t>& rowptr,
+                                         std::vector<uint32_t>& col, std::vector<float>& val)>;
+
+// A^ from the canonical rows that rows_of supplies (averaged over the
+// transformations that fix their LOR), its transpose and the compact operands.
+void build_symmetric_impl(const SymMaps& M, const CanonicalRows& rows_of, DevCsr& A, DevCsr& AT, SymOps& y,
+                          cudaStream_t s) {
     const uint64_t D = M.D, nlor = D * (D - 1) / 2, cols = (uint64_t)M.n * M.n * M.nz;
     MLEM_REQUIRE(nlor < (1ull << 32), MLEM_EUNSUPPORTED, "symmetry: too many LORs");
     uint8_t comp[16][16], inv[16];
@@ -698,7 +703,7 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
     std::vector<uint64_t> crp;
     std::vector<uint32_t> ccol;
     std::vector<float> cval;
-    siddon_rows_of_lors(geo, canon, crp, ccol, cval);
+    rows_of(canon, crp, ccol, cval);
     {
         std::vector<uint64_t> nrp(K + 1, 0);
         std::vector<uint32_t> ncol;
@@ -837,6 +842,99 @@ void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y,
     cudaFree(d_can);
     cudaFree(d_sym);
     cudaFree(len);
+}
+
+__global__ void k_count_diff(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint64_t n,
+                             unsigned long long* __restrict__ count) {
+    unsigned long long local = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        local += a[i] != b[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+}
+
+// Words that differ between two device arrays of n 32-bit words.
+uint64_t count_diff(const void* a, const void* b, uint64_t n, cudaStream_t s) {
+    if (n == 0) return 0;
+    unsigned long long* d = nullptr;
+    MLEM_CUDA(cudaMalloc(&d, sizeof(unsigned long long)));
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) {
+        k_count_diff<<<grid_of(n), 256, 0, s>>>(static_cast<const uint32_t*>(a), static_cast<const uint32_t*>(b), n, d);
+        count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d);
+    MLEM_CUDA(e);
+    return h;
+}
+
+SymMaps maps_of(uint32_t n, uint32_t nz, uint32_t dpr, uint32_t rings) {
+    SymMaps M;
+    M.n = n;
+    M.nz = nz;
+    M.dpr = dpr;
+    M.rings = rings;
+    M.D = dpr * rings;
+    return M;
+}
+
+}  // namespace
+
+void build_symmetric(const mlem_geometry& geo, DevCsr& A, DevCsr& AT, SymOps& y, cudaStream_t s) {
+    check_symmetric_geometry(geo);
+    build_symmetric_impl(
+        maps_of(geo.nx, geo.nz, geo.det_per_ring, geo.n_rings),
+        [&](const std::vector<uint64_t>& lors, std::vector<uint64_t>& rp, std::vector<uint32_t>& col,
+            std::vector<float>& val) { siddon_rows_of_lors(geo, lors, rp, col, val); },
+        A, AT, y, s);
+}
+
+void build_symmetric_checked(const mlem_csr_host& c, const DevCsr& user, uint32_t n, uint32_t nz, uint32_t dpr,
+                             uint32_t rings, DevCsr& A, DevCsr& AT, SymOps& y, cudaStream_t s) {
+    MLEM_REQUIRE(n >= 1 && nz >= 1, MLEM_EINVAL, "symmetry: grid_nx and grid_nz must be given");
+    MLEM_REQUIRE(dpr >= 4 && dpr % 4 == 0 && rings >= 1, MLEM_EUNSUPPORTED,
+                 "symmetry: needs a ring scanner with a multiple of 4 detectors per ring (sym_det_per_ring)");
+    const uint64_t D = (uint64_t)dpr * rings;
+    MLEM_REQUIRE(D <= 16384, MLEM_EUNSUPPORTED, "symmetry: too many detectors");
+    MLEM_REQUIRE((uint64_t)c.rows == D * (D - 1) / 2, MLEM_EINVAL,
+                 "symmetry: the rows must be the " + std::to_string(D * (D - 1) / 2) +
+                     " detector pairs (a < b, lexicographic) of the scanner");
+    MLEM_REQUIRE((uint64_t)c.cols == (uint64_t)n * n * nz, MLEM_EINVAL,
+                 "symmetry: the columns must be the grid_nx x grid_nx x grid_nz voxels");
+    build_symmetric_impl(
+        maps_of(n, nz, dpr, rings),
+        [&](const std::vector<uint64_t>& lors, std::vector<uint64_t>& rp, std::vector<uint32_t>& col,
+            std::vector<float>& val) {
+            rp.assign(lors.size() + 1, 0);
+            for (size_t k = 0; k < lors.size(); ++k) rp[k + 1] = rp[k] + (c.rowptr[lors[k] + 1] - c.rowptr[lors[k]]);
+            col.resize(rp.back());
+            val.resize(rp.back());
+            for (size_t k = 0; k < lors.size(); ++k) {
+                const uint64_t b = c.rowptr[lors[k]], e = c.rowptr[lors[k] + 1];
+                std::memcpy(col.data() + rp[k], c.col + b, sizeof(uint32_t) * (e - b));
+                std::memcpy(val.data() + rp[k], c.val + b, sizeof(float) * (e - b));
+            }
+        },
+        A, AT, y, s);
+    // A^ was built from the canonical rows alone; it equals the caller's
+    // matrix bit for bit exactly when that matrix is invariant under the 16
+    // transformations (with every row's columns ascending).
+    uint64_t diff = A.nnz == user.nnz ? 0 : ~0ull;
+    if (diff == 0) diff = count_diff(A.rowptr, user.rowptr, 2 * ((uint64_t)A.nrows + 1), s);
+    if (diff == 0) diff = count_diff(A.idx, user.idx, A.nnz, s) + count_diff(A.val, user.val, A.nnz, s);
+    if (diff != 0) {
+        fail(MLEM_EINVAL,
+             "symmetry: the matrix is not invariant under the 16 symmetries of the scanner (" +
+                 (A.nnz == user.nnz ? std::to_string(diff) + " words differ from"
+                                    : std::string("its nonzero count differs from")) +
+                 " the symmetric matrix built from its canonical rows; every row must list its columns in ascending "
+                 "order)");
+    }
 }
 
 void lower_symmetric_values(SymOps& y, mlem_value_type vt, cudaStream_t s) {

@@ -544,6 +544,13 @@ def run_batched(pkg, torch, fp32_mid_rate=None):
     out = {"images_iterations_per_s": float(its.sum()) / st["seconds_iterations"],
            "wall_images_iterations_per_s": float(its.sum()) / st["seconds_total"],
            "workload": "cyl3d_mid fp16, 64 sinograms, iterations U{10..200}"}
+    # each form explicitly: per-iteration graphs, and the persistent loop (the
+    # iterations between two refills in one cooperative launch)
+    for form, label in ((1, "graphs"), (2, "persistent")):
+        mb.batch_run(G[:8], np.full(8, 2, np.uint32), form=form)
+        _, st = mb.batch_run(G, its, stats=True, form=form)
+        out[f"{label}_images_iterations_per_s"] = float(its.sum()) / st["seconds_iterations"]
+        out[f"{label}_kernel_launches"] = int(st["kernel_launches"])
     if fp32_mid_rate:
         out["vs_fp32_plain_same_matrix"] = out["images_iterations_per_s"] / fp32_mid_rate
     mb.close()
@@ -602,9 +609,13 @@ def run_symmetry(pkg, torch, name):
     return out
 
 
-def run_serving(pkg, torch, n_requests=300, rate=50.0, fp32_iter_s=None):
+def run_serving(pkg, torch, n_requests=2000, rate=50.0, serial_every=10):
     """Serving form: three resident matrices (2-D ring FP32, 3-D mid FP32,
-    12 GB class FP16), Poisson arrivals, continuous batching in the server."""
+    12 GB class FP16), Poisson arrivals, continuous batching in the server.
+    Then the serial plain-FP32 baseline, measured: every serial_every-th
+    request of the same list run one at a time through mlem_run (host
+    sinogram in, host image out) on FP32 matrices (the 12 GB class in FP32
+    too)."""
     import threading as th
     from mlem_gb300 import synth
     s = torch.cuda.current_stream()
@@ -656,25 +667,36 @@ def run_serving(pkg, torch, n_requests=300, rate=50.0, fp32_iter_s=None):
         wall = time.perf_counter() - t0
         stats = srv.stats()
     lat = np.array(lat)
-    for m in mats:
-        m.close()
     out = {"requests": n_requests, "arrival_rate_per_s": rate, "p50_latency_s": float(np.percentile(lat, 50)),
            "p99_latency_s": float(np.percentile(lat, 99)), "mean_latency_s": float(lat.mean()),
+           "p99_tail_samples": int((lat >= np.percentile(lat, 99)).sum()),
            "reconstructions_per_s": n_requests / wall, "wall_s": wall,
            "iterations_done": int(stats["iterations_done"]),
            "mix": "ring2d fp32 0.5 / cyl3d_mid fp32 0.35 / cyl3d_12gb fp16 0.15, counts log-U[1e5,1e9], "
                   "iterations U{20..100}, autotuned slots per matrix, projections over the occupied slots, "
-                  "small matrices (< 16 M nonzeros) on a high-priority stream"}
+                  "small matrices (< 16 M nonzeros) on a high-priority stream, pinned staging of sinograms "
+                  "and images"}
     for j, (name, _, _) in enumerate(specs):
         sel = which == j
         if sel.any():
             out[f"p50_latency_s_{name}"] = float(np.percentile(lat[sel], 50))
             out[f"p99_latency_s_{name}"] = float(np.percentile(lat[sel], 99))
-    if fp32_iter_s:
-        # serial plain FP32 execution of the same request mix: one reconstruction at a time
-        serial_s = sum(float(iters[i]) / fp32_iter_s[specs[which[i]][0]] for i in range(n_requests))
-        out["serial_fp32_reconstructions_per_s"] = n_requests / serial_s
-        out["serial_fp32_busy_s"] = serial_s
+    # serial plain FP32: the same requests one at a time through mlem_run
+    mats[2].close()
+    mats[2] = pkg.Matrix.generate(pkg.preset("cyl3d_12gb"), value_type=pkg.VAL_F32, layout=LAYOUT)
+    sample = list(range(0, n_requests, serial_every))
+    for j in range(3):  # tuning and plans settled outside the timed loop
+        mats[j].run(sinos[int(np.argmax(which == j))], 2)
+    t0 = time.perf_counter()
+    for i in sample:
+        mats[which[i]].run(sinos[i], int(iters[i]))
+    serial_s = time.perf_counter() - t0
+    out["serial_fp32_reconstructions_per_s"] = len(sample) / serial_s
+    out["serial_fp32_sample"] = f"every {serial_every}th request of the list ({len(sample)} requests), " \
+                                f"one at a time through mlem_run, FP32 matrices, {serial_s:.1f} s"
+    out["vs_serial_fp32"] = out["reconstructions_per_s"] / out["serial_fp32_reconstructions_per_s"]
+    for m in mats:
+        m.close()
     return out
 
 
@@ -694,6 +716,8 @@ def forms_summary(forms, fp32_rate):
     put("mid_fp32_plain_iter_s", mid)
     b = forms.get("batched_fp16_64", {})
     put("batched_fp16_64_images_iter_s", b.get("images_iterations_per_s"), mid)
+    put("batched_persistent_images_iter_s", b.get("persistent_images_iterations_per_s"))
+    put("batched_graphs_images_iter_s", b.get("graphs_images_iterations_per_s"))
     modes = forms.get("modes_cyl3d_mid") or forms
     for k in ("csr_vector_trans", "merge_trans", "csr_vector_scatter", "merge_scatter", "fused"):
         if isinstance(modes.get(k), dict) and "iterations_per_s" in modes[k]:
@@ -702,7 +726,8 @@ def forms_summary(forms, fp32_rate):
     if sv:
         out["serving"] = {k: (round(sv[k], 4) if isinstance(sv[k], float) else sv[k])
                           for k in ("requests", "p50_latency_s", "p99_latency_s", "reconstructions_per_s",
-                                    "serial_fp32_reconstructions_per_s", "serial_fp32_sample") if k in sv}
+                                    "serial_fp32_reconstructions_per_s", "vs_serial_fp32", "p99_tail_samples")
+                          if k in sv}
     sy = forms.get("symmetry", {}).get("fp32")
     if sy:
         out["symmetry_matrix_hat_fp32_iter_s"] = round(sy["autotuned"]["iterations_per_s"], 1)
@@ -716,7 +741,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cyl3d_12gb", choices=sorted(WORKLOADS))
-    ap.add_argument("--forms", default="all", choices=["all", "none", "modes", "symmetry", "batched"],
+    ap.add_argument("--forms", default="all", choices=["all", "none", "modes", "symmetry", "batched", "serving"],
                     help="all: FP16, batched, serving, symmetry and the modes on the smaller matrices; modes: only "
                          "the reference's switch combinations, the fused pass and a batched run on --workload; "
                          "symmetry: only the symmetry-compressed operands on --workload")
@@ -875,14 +900,12 @@ def main():
         line["forms"] = {"symmetry": run_symmetry(pkg, torch, name)}
     if args.forms == "batched":
         line["forms"] = {"batched_fp16_64": run_batched(pkg, torch)}
+    if args.forms == "serving":
+        line["forms"] = {"serving": run_serving(pkg, torch)}
     if args.forms == "all":
         line["forms"] = run_forms(pkg, torch, args)
         line["forms"]["fp32_plain"] = {"images_iterations_per_s": value / world}
-        rates = {name: value / world, "cyl3d_mid": line["forms"].get("fp32_plain_cyl3d_mid", {}).get(
-            "images_iterations_per_s"), "ring2d": line["forms"].get("fp32_plain_ring2d", {}).get(
-            "images_iterations_per_s")}
-        if all(rates.values()):
-            line["forms"]["serving"] = run_serving(pkg, torch, fp32_iter_s=rates)
+        line["forms"]["serving"] = run_serving(pkg, torch)
         line["forms"]["symmetry"] = run_symmetry(pkg, torch, name)
     if rank == 0 and not args.no_cpu:
         P = cpu_problem(pkg, name)

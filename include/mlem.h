@@ -92,16 +92,26 @@ typedef struct {
     uint32_t grid_nx, grid_ny, grid_nz; /* voxel grid of the columns (column = x + nx*(y + ny*z),
                                    scannerconfig.cpp:30-35) for the locality layout of
                                    mlem_matrix_create; csr4 files and geometries carry their own */
-    uint32_t symmetry;          /* mlem_matrix_generate only: 1 = use the 16 symmetries of the scanner
-                                   (mirror y -> -y, rotations by 90 degrees, axial flip; needs
-                                   det_per_ring % 4 == 0, nx == ny, vx == vy, row_stride 1, natural
-                                   layout).  The matrix becomes A^, built from the canonical LOR rows
-                                   (averaged over the symmetries that fix their LOR) so that it is
-                                   exactly symmetric; it stays the matrix of every mode and getter.
-                                   Beside it: compact operands holding 1/16 of the nonzeros for the
-                                   csr-vector projections (kernel SYM, an autotuner candidate).  No
-                                   counterpart in the reference (its csr4 symmetry flags are not
-                                   expanded, csr4matrix.cpp:72-75). */
+    uint32_t symmetry;          /* 1 = use the 16 symmetries of the scanner (mirror y -> -y, rotations
+                                   by 90 degrees, axial flip) through compact operands holding 1/16 of
+                                   the nonzeros for the csr-vector projections (kernel SYM, an
+                                   autotuner candidate); natural layout only.
+                                   mlem_matrix_generate (needs det_per_ring % 4 == 0, nx == ny,
+                                   vx == vy, row_stride 1): the matrix becomes A^, built from the
+                                   canonical LOR rows (averaged over the symmetries that fix their
+                                   LOR) so that it is exactly symmetric; it stays the matrix of every
+                                   mode and getter.
+                                   mlem_matrix_create: the caller's matrix is kept unchanged; its rows
+                                   must be the detector pairs (a < b, lexicographic; detector
+                                   ring * sym_det_per_ring + k at angle 2 pi k / sym_det_per_ring) of
+                                   a ring scanner, its columns the grid_nx x grid_nx x grid_nz voxels
+                                   of a grid centred on the axis, and it must be exactly invariant
+                                   under the 16 transformations (checked bit for bit against the
+                                   symmetric matrix rebuilt from its canonical rows; MLEM_EINVAL
+                                   otherwise).  No counterpart in the reference (its csr4 symmetry
+                                   flags are not expanded, csr4matrix.cpp:72-75). */
+    uint32_t sym_det_per_ring;  /* mlem_matrix_create with symmetry: detectors per ring (multiple of 4) */
+    uint32_t sym_rings;         /* mlem_matrix_create with symmetry: rings */
 } mlem_matrix_opts;
 
 /* Device layout of a matrix.  LOCALITY stores A' = P_L A P_Vᵀ: columns
@@ -397,6 +407,12 @@ typedef struct {
     uint32_t tile;              /* instances per batch tile: 0 = autotune, else 8/16/32 */
     uint32_t use_graph;
     uint32_t order_by_iterations; /* 1: instances enter the pool longest first */
+    uint32_t form;              /* 0 = autotuned per matrix; 1 = one CUDA graph per iteration (forward
+                                   and back projection launches); 2 = persistent: the iterations
+                                   between two slot refills run in one cooperative launch, forward
+                                   and back projection separated by grid-wide barriers (needs Aᵀ;
+                                   a barrier wait that runs out returns MLEM_ETIMEOUT).  Every form
+                                   gives the same bits. */
 } mlem_batch_opts;
 
 void mlem_batch_opts_default(mlem_batch_opts* o);

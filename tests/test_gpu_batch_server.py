@@ -77,6 +77,41 @@ def test_batch_bits_independent_of_tile_and_width(pkg, O):
     m.close()
 
 
+@pytest.mark.parametrize("vt", ["f32", "f16"])
+def test_batch_persistent_form_is_bit_identical(pkg, O, vt):
+    """The persistent form (the iterations between two refills in one
+    cooperative launch, grid barriers between the projections) gives the
+    bits of the per-iteration graphs, in every tile and with uneven counts
+    (widths shrink as the pool empties); the autotuned form is one of them."""
+    p = problem(pkg, O, "cyl3d_tiny")
+    m = pkg.Matrix.from_csr(p["rp"], p["col"], p["val"], p["cols"],
+                            value_type=pkg.VAL_F32 if vt == "f32" else pkg.VAL_F16)
+    G = sinograms(pkg, p, 21)
+    its = np.random.Generator(np.random.PCG64(4)).integers(1, 40, len(G)).astype(np.uint32)
+    its[3] = 0
+    for tile in (8, 16, 32):
+        graphs = m.batch_run(G, its, tile=tile, form=1)
+        loop = m.batch_run(G, its, tile=tile, form=2)
+        assert np.array_equal(graphs, loop), tile
+    auto = m.batch_run(G, its, tile=16)
+    assert np.array_equal(auto, graphs)
+    for k in (0, 7):
+        single = m.run(G[k], int(its[k]))
+        assert O.rel_l2(loop[k], single) < 1e-5
+    m.close()
+
+
+def test_batch_persistent_form_needs_the_transpose(pkg, O):
+    p = problem(pkg, O, "ring2d_tiny")
+    m = pkg.Matrix.from_csr(p["rp"], p["col"], p["val"], p["cols"], build_transpose=False)
+    with pytest.raises(pkg.MlemError) as e:
+        m.batch_run(p["g"][None, :], np.array([3], np.uint32), form=2)
+    assert e.value.status == "EINVAL"
+    out = m.batch_run(p["g"][None, :], np.array([3], np.uint32))  # autotuned: the graph form
+    assert O.rel_l2(out[0], m.run(p["g"], 3)) < 1e-5
+    m.close()
+
+
 def test_batch_instance_independent_of_company(pkg, O):
     p = problem(pkg, O, "ring2d")
     m = pkg.Matrix.from_csr(p["rp"], p["col"], p["val"], p["cols"])
