@@ -102,7 +102,7 @@ struct MergePlan {
     size_t smem = 0;
     // true: the row-parallel tile kernel (library-owned, padded operands);
     // false: the per-thread walk over shared-memory products (any arrays)
-    int rows_kernel = 0;         // 0: per-thread walk (k_merge_tile), 1: rows to groups, 2: nonzero-balanced
+    bool rows_kernel = false;
     void release();
 };
 // Builds the tile partition of `op` for a section size (device allocations).

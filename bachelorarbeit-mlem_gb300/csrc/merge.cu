@@ -326,114 +326,10 @@ k_merge_rows(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ i
     }
 }
 
-// Nonzero-balanced tile: the same stretch of the merge path as k_merge_rows,
-// but its nonzeros [J0, J1) are cut into 16 equal parts, one per 16-lane
-// group, whatever the rows' lengths (the voxel rows of Aᵀ vary several-fold
-// in length, so handing whole rows to groups left most groups idle while one
-// finished a long row).  A group sums every row piece of its part with 16-byte
-// vector loads; rows that lie wholly inside its part (and inside the tile) get
-// their epilogue there.  The first and last piece of every group are combined
-// by one thread in group order (fixed, so the result is deterministic): a row
-// that ends inside the tile gets its epilogue, the tile's first row goes to
-// head[k] and the row still open at the tile's end to carry[k], for the same
-// fix-up kernel.  Rows without nonzeros inside the tile get their epilogue
-// (of 0) from a separate pass.
-template <typename V, int LPR>
-__global__ void __launch_bounds__(256, 8)
-k_merge_bal(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx, const V* __restrict__ val,
-            const float* __restrict__ x, uint32_t rows, const uint32_t* __restrict__ ti,
-            const uint64_t* __restrict__ tj, float* __restrict__ carry, uint32_t* __restrict__ carry_row,
-            float* __restrict__ head, EpiDev epi) {
-    constexpr uint32_t NG = 256 / LPR;
-    __shared__ float s_val[2 * NG];
-    __shared__ uint32_t s_row[2 * NG];
-    const uint64_t k = blockIdx.x;
-    const uint32_t I0 = ti[k], I1 = ti[k + 1];
-    const uint64_t J0 = tj[k], J1 = tj[k + 1];
-    const uint64_t nj = J1 - J0;
-    const uint32_t grp = threadIdx.x / LPR;
-    const int sub = threadIdx.x & (LPR - 1);
-    const unsigned mask = LPR == 32 ? 0xffffffffu : (((1u << LPR) - 1u) << ((threadIdx.x & 31) & ~(LPR - 1)));
-    const uint64_t a = J0 + nj * grp / NG, b = J0 + nj * (grp + 1) / NG;
-    float first_v = 0.f, last_v = 0.f;
-    uint32_t first_r = 0xffffffffu, last_r = 0xffffffffu;
-    if (a < b) {
-        // the row holding nonzero a: the last row of [I0, I1] starting at or before a
-        uint32_t lo = I0, hi = I1;
-        while (lo < hi) {
-            const uint32_t mid = lo + (hi - lo + 1) / 2;
-            if (rowptr[mid] <= a) lo = mid;
-            else hi = mid - 1;
-        }
-        for (uint32_t r = lo; r < rows; ++r) {
-            const uint64_t rs = rowptr[r], rt = rowptr[r + 1];
-            if (rs >= b) break;
-            if (rs == rt) continue;  // an empty row: the separate pass
-            const uint64_t ps = rs > a ? rs : a, pt = rt < b ? rt : b;
-            float acc = group_part_dot<V, LPR>(idx, val, x, ps, pt, sub);
-#pragma unroll
-            for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(mask, acc, o);
-            if (first_r == 0xffffffffu) {
-                first_r = r;
-                first_v = acc;
-            } else {
-                if (last_r != 0xffffffffu && sub == 0) epi(last_r, last_v);  // whole row inside the part
-                last_r = r;
-                last_v = acc;
-            }
-        }
-    }
-    if (sub == 0) {
-        s_row[2 * grp] = first_r;
-        s_val[2 * grp] = first_v;
-        s_row[2 * grp + 1] = last_r;
-        s_val[2 * grp + 1] = last_v;
-    }
-    // rows without nonzeros that end inside the tile
-    for (uint32_t r = I0 + 1 + threadIdx.x; r < I1; r += blockDim.x)
-        if (rowptr[r] == rowptr[r + 1]) epi(r, 0.f);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        bool head_done = false, carry_done = false;
-        uint32_t cur = 0xffffffffu;
-        float sum = 0.f;
-        auto finish = [&]() {
-            if (cur == 0xffffffffu) return;
-            if (cur == I1) {  // still open at the tile's end (also when the tile lies inside one row)
-                carry[k] = sum;
-                carry_done = true;
-            } else if (cur == I0) {
-                head[k] = sum;
-                head_done = true;
-            } else {
-                epi(cur, sum);
-            }
-        };
-        for (uint32_t q = 0; q < 2 * NG; ++q) {
-            const uint32_t r = s_row[q];
-            if (r == 0xffffffffu) continue;
-            if (r == cur) {
-                sum += s_val[q];
-            } else {
-                finish();
-                cur = r;
-                sum = s_val[q];
-            }
-        }
-        finish();
-        if (!carry_done) carry[k] = 0.f;
-        carry_row[k] = I1;
-        if (!head_done && I0 != I1) head[k] = 0.f;
-    }
-}
-
 template <typename V>
 void merge_launch_t(const DevCsr& op, const MergePlan& p, const float* x, const EpiDev& e,
                     L2Window win, cudaStream_t s) {
-    if (p.rows_kernel == 2)
-        launch_ex(k_merge_bal<V, 16>, dim3((unsigned)p.ntiles), dim3(256), 0, s, win, op.rowptr, op.idx,
-                  static_cast<const V*>(op.val), x, op.nrows, p.tile_i, p.tile_j, p.carry, p.carry_row, p.head, e);
-    else if (p.rows_kernel == 1)
+    if (p.rows_kernel)
         launch_ex(k_merge_rows<V, 16>, dim3((unsigned)p.ntiles), dim3(256), 0, s, win, op.rowptr, op.idx,
                   static_cast<const V*>(op.val), x, op.nrows, p.tile_i, p.tile_j, p.carry, p.carry_row, p.head, e);
     else
@@ -480,7 +376,7 @@ void merge_plan_build(const DevCsr& op, uint32_t secsize, MergePlan& plan, cudaS
     // one 1024-thread block of the reference covers (1024 * secsize items),
     // and enough items for about 32 average rows so that the CTA's 8 warps
     // share the tile's rows evenly; at most 65536 items.
-    plan.rows_kernel = 2;  // the caller may time both row-parallel kernels and keep the faster
+    plan.rows_kernel = true;
     plan.threads = 256;
     const uint64_t items = (uint64_t)op.nrows + op.nnz;
     const uint64_t per_row = op.nrows ? (items + op.nrows - 1) / op.nrows : 1;

@@ -161,62 +161,60 @@ static void cols_out(const mlem_matrix* m, float* dst, const float* src, cudaStr
 }
 static bool permuted(const mlem_matrix* m) { return m->lor_of || m->vox_of; }
 
+// Lanes per row of A for the scatter back projection: 8, 16 or 32 around the
+// row length, timed once per matrix (ratio 1 into a scratch image).
+int scatter_lanes(mlem_matrix* m) {
+    if (m->scatter_lanes) return m->scatter_lanes;
+    const DevCsr& A = m->A;
+    cudaStream_t s = m->stream;
+    float *r = nullptr, *bp = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int best_l = pick_lanes(A.nnz, A.nrows) < 8 ? 8 : pick_lanes(A.nnz, A.nrows);
+    float best = 1e30f;
+    try {
+        MLEM_CUDA(cudaMalloc(&r, sizeof(float) * std::max<uint32_t>(A.nrows, 1)));
+        MLEM_CUDA(cudaMalloc(&bp, sizeof(float) * std::max<uint32_t>(A.ncols, 1)));
+        std::vector<float> ones(std::max<uint32_t>(A.nrows, 1), 1.0f);
+        MLEM_CUDA(cudaMemcpyAsync(r, ones.data(), sizeof(float) * ones.size(), cudaMemcpyHostToDevice, s));
+        MLEM_CUDA(cudaMemsetAsync(bp, 0, sizeof(float) * std::max<uint32_t>(A.ncols, 1), s));
+        MLEM_CUDA(cudaEventCreate(&e0));
+        MLEM_CUDA(cudaEventCreate(&e1));
+        for (int lanes : {8, 16, 32}) {
+            launch_scatter(A, r, bp, lanes, {}, s);
+            MLEM_CUDA(cudaEventRecord(e0, s));
+            for (int q = 0; q < 2; ++q) launch_scatter(A, r, bp, lanes, {}, s);
+            MLEM_CUDA(cudaEventRecord(e1, s));
+            MLEM_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            MLEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                best_l = lanes;
+            }
+        }
+    } catch (...) {
+        cudaStreamSynchronize(s);
+        cudaFree(r);
+        cudaFree(bp);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        throw;
+    }
+    cudaFree(r);
+    cudaFree(bp);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    m->scatter_lanes = best_l;
+    return best_l;
+}
+
 const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
     auto& plans = transposed ? m->plan_AT : m->plan_A;
     auto it = plans.find(secsize);
     if (it != plans.end()) return it->second;
     MergePlan p;
-    const DevCsr& op = transposed ? m->AT : m->A;
-    cudaStream_t s = m->stream;
-    merge_plan_build(op, secsize, p, s);
-    MLEM_CUDA(cudaStreamSynchronize(s));
-    if (p.rows_kernel && op.nnz) {
-        // the faster of the two row-parallel tile kernels (rows handed to lane
-        // groups, or nonzeros cut evenly between them) on this operand, timed
-        // with a Raw epilogue on an image of ones
-        float *x = nullptr, *y = nullptr;
-        cudaEvent_t e0 = nullptr, e1 = nullptr;
-        float best = 1e30f;
-        int pick = p.rows_kernel;
-        try {
-            MLEM_CUDA(cudaMalloc(&x, sizeof(float) * std::max<uint32_t>(op.ncols, 1)));
-            MLEM_CUDA(cudaMalloc(&y, sizeof(float) * std::max<uint32_t>(op.nrows, 1)));
-            std::vector<float> ones(std::max<uint32_t>(op.ncols, 1), 1.0f);
-            MLEM_CUDA(cudaMemcpyAsync(x, ones.data(), sizeof(float) * ones.size(), cudaMemcpyHostToDevice, s));
-            MLEM_CUDA(cudaEventCreate(&e0));
-            MLEM_CUDA(cudaEventCreate(&e1));
-            EpiArgs e;
-            e.kind = Epi::Raw;
-            e.out = y;
-            for (int kind : {1, 2}) {
-                p.rows_kernel = kind;
-                launch_merge_spmv(op, p, x, e, L2Window{}, s);
-                MLEM_CUDA(cudaEventRecord(e0, s));
-                for (int q = 0; q < 2; ++q) launch_merge_spmv(op, p, x, e, L2Window{}, s);
-                MLEM_CUDA(cudaEventRecord(e1, s));
-                MLEM_CUDA(cudaEventSynchronize(e1));
-                float ms = 0.f;
-                MLEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                if (ms < best) {
-                    best = ms;
-                    pick = kind;
-                }
-            }
-        } catch (...) {
-            cudaStreamSynchronize(s);
-            cudaFree(x);
-            cudaFree(y);
-            if (e0) cudaEventDestroy(e0);
-            if (e1) cudaEventDestroy(e1);
-            p.release();
-            throw;
-        }
-        cudaFree(x);
-        cudaFree(y);
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        p.rows_kernel = pick;
-    }
+    merge_plan_build(transposed ? m->AT : m->A, secsize, p, m->stream);
+    MLEM_CUDA(cudaStreamSynchronize(m->stream));
     return plans.emplace(secsize, p).first->second;
 }
 
@@ -499,7 +497,7 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
             }
             project(m, true, w.ratio, be, o, wr, s);
         } else {
-            launch_scatter(A, w.ratio, w.bp, pick_lanes(A.nnz, A.nrows), wr, s);
+            launch_scatter(A, w.ratio, w.bp, scatter_lanes(m), wr, s);
             launch_update_zero(w.f, w.bp, m->norm, A.ncols, s);
         }
         if (timer) timer->record(s);
@@ -571,6 +569,7 @@ static void run_iterations(mlem_matrix* m, const mlem_run_opts& o, uint32_t iter
             merge_plan(m, false, o.secsize_fp);
             if (o.bp_mode == MLEM_BP_TRANS) merge_plan(m, true, o.secsize_bp);
         }
+        if (o.bp_mode == MLEM_BP_SCATTER) scatter_lanes(m);
         cudaStream_t cs = m->stream;
         cudaGraph_t graph = nullptr;
         const uint64_t l0 = g_launches.load();
@@ -1283,7 +1282,7 @@ mlem_status mlem_back_project(mlem_matrix* m, const float* ratio_dev, float* bp_
             project(m, true, r, be, o, {}, s);
         } else {
             MLEM_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * m->A.ncols, s));
-            launch_scatter(m->A, r, out, pick_lanes(m->A.nnz, m->A.nrows), {}, s);
+            launch_scatter(m->A, r, out, scatter_lanes(m), {}, s);
         }
         if (perm) cols_out(m, bp_dev, out, s);
     });

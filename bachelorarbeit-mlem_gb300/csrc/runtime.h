@@ -136,6 +136,7 @@ struct mlem_matrix {
     std::map<uint32_t, mlem::MergePlan> plan_A, plan_AT;
     uint32_t batch_tile = 0;          // autotuned batch tile (0 = not yet)
     uint32_t batch_form = 0;          // autotuned batch form: 1 graphs, 2 persistent (0 = not yet)
+    int scatter_lanes = 0;            // autotuned lanes per row of the scatter back projection (0 = not yet)
     bool tuned[2] = {false, false};   // csr-vector configuration of A / Aᵀ measured
     mlem::ProjCfg proj[2];
     std::mutex mu;

@@ -108,7 +108,7 @@ def test_batch_persistent_form_needs_the_transpose(pkg, O):
         m.batch_run(p["g"][None, :], np.array([3], np.uint32), form=2)
     assert e.value.status == "EINVAL"
     out = m.batch_run(p["g"][None, :], np.array([3], np.uint32))  # autotuned: the graph form
-    assert O.rel_l2(out[0], m.run(p["g"], 3)) < 1e-5
+    assert O.rel_l2(out[0], m.run(p["g"], 3, bp_mode=pkg.BP_SCATTER)) < 1e-5
     m.close()
 
 
