@@ -319,9 +319,10 @@ k_scatter(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
     const uint32_t row = gt / LPR;
     const int sub = threadIdx.x & (LPR - 1);
     if (row >= nrows) return;
+    // the ratio and the row bounds are loaded together (one round trip, not two)
     const float r = ratio[row];
-    if (r == 0.0f) return;  // adds of val*0 leave bp unchanged
     const uint64_t s = rowptr[row], t = rowptr[row + 1];
+    if (r == 0.0f) return;  // adds of val*0 leave bp unchanged
     const uint4* idx4 = reinterpret_cast<const uint4*>(idx);
     for (uint64_t v = (s >> 2) + sub; v < ((t + 3) >> 2); v += LPR) {
         Vec4<V> p;
