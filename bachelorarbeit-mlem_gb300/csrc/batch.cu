@@ -259,7 +259,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned k, int* e
 // chains, same order), so an instance's bits do not depend on which kernel
 // form runs it.
 template <typename V, int W>
-__global__ void __launch_bounds__(256, 6)
+__global__ void __launch_bounds__(256, W == 32 ? 8 : 6)
 k_batch_loop(const uint64_t* __restrict__ rp, const uint32_t* __restrict__ ix, const V* __restrict__ vl,
              uint32_t rows, const uint64_t* __restrict__ rpT, const uint32_t* __restrict__ ixT,
              const V* __restrict__ vlT, uint32_t cols, const float* __restrict__ norm, uint32_t BT,
@@ -267,30 +267,31 @@ k_batch_loop(const uint64_t* __restrict__ rp, const uint32_t* __restrict__ ix, c
              unsigned* count, int* err) {
     constexpr uint32_t RPW = 32 / W;  // rows per warp
     const int lane = threadIdx.x & 31, sl = lane % W;
-    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    // 32-bit row counters (rows, cols < 2^32; a resident grid has < 2^16 warps)
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t stride = ((gridDim.x * blockDim.x) >> 5) * RPW;
     unsigned k = 0;
     for (uint32_t step = 0; step < steps; ++step) {
-        for (uint64_t first = warp * RPW; first < rows; first += nwarps * RPW) {
-            const uint64_t row = first + lane / W;
+        for (uint32_t first = warp * RPW; first < rows; first += stride) {
+            const uint32_t row = first + lane / W;
             const bool ok = row < rows;
             float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-            batch_rows<V, W, false>(rp, ix, vl, f, BT, (uint32_t)row, ok, lane, acc);
+            batch_rows<V, W, false>(rp, ix, vl, f, BT, row, ok, lane, acc);
             if (ok && sl < W / 4) {
-                const uint64_t o = row * BT + sl * 4;
+                const uint64_t o = (uint64_t)row * BT + sl * 4;
                 const int4 gg = *reinterpret_cast<const int4*>(g + o);
                 *reinterpret_cast<float4*>(ratio + o) = make_float4(correl1(gg.x, acc.x), correl1(gg.y, acc.y),
                                                                     correl1(gg.z, acc.z), correl1(gg.w, acc.w));
             }
         }
         if (!grid_barrier(count, ++k, err)) return;
-        for (uint64_t first = warp * RPW; first < cols; first += nwarps * RPW) {
-            const uint64_t c = first + lane / W;
+        for (uint32_t first = warp * RPW; first < cols; first += stride) {
+            const uint32_t c = first + lane / W;
             const bool ok = c < cols;
             float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-            batch_rows<V, W, false>(rpT, ixT, vlT, ratio, BT, (uint32_t)c, ok, lane, acc);
+            batch_rows<V, W, false>(rpT, ixT, vlT, ratio, BT, c, ok, lane, acc);
             if (ok && sl < W / 4) {
-                const uint64_t o = c * BT + sl * 4;
+                const uint64_t o = (uint64_t)c * BT + sl * 4;
                 const uint4 rem = *reinterpret_cast<const uint4*>(remaining + sl * 4);
                 const float n = norm[c];
                 float4 fv = *reinterpret_cast<const float4*>(f + o);
