@@ -25,7 +25,8 @@ LIB_PATH = PKG / "lib" / "libmlem_gb300.so"
 CLI_PATH = PKG / "bin" / "mlem_gb300"
 
 SPMV_MERGE, SPMV_CSR_VECTOR = 0, 1
-KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO, KERNEL_D16, KERNEL_ILV, KERNEL_ORDERED, KERNEL_SYM = range(8)
+(KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO, KERNEL_D16, KERNEL_ILV, KERNEL_ORDERED, KERNEL_SYM,
+ KERNEL_LOOP) = range(9)
 LAYOUT_NATURAL, LAYOUT_LOCALITY = 0, 1
 VAL_F32, VAL_F16, VAL_BF16 = 0, 1, 2
 BP_TRANS, BP_SCATTER, BP_FUSED = 0, 1, 2

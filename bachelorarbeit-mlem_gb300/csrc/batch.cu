@@ -207,49 +207,6 @@ __global__ void k_batch_tick(uint32_t* remaining, uint32_t BT) {
     if (threadIdx.x < BT && remaining[threadIdx.x] > 0) remaining[threadIdx.x] -= 1;
 }
 
-__device__ __forceinline__ uint64_t globaltimer_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Grid-wide barrier of a cooperative launch: barrier k of the launch is
-// passed once `count` (zeroed before the launch) reaches k * gridDim.x.  Every
-// wait is bounded: after kBarrierWaitNs, or as soon as another block has given
-// up, the block sets *err and the caller returns, so a failure ends the launch
-// with an error flag the host reads instead of a hang.
-constexpr uint64_t kBarrierWaitNs = 2000000000ull;  // 2 s; a phase takes milliseconds
-
-__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned k, int* err) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(count, 1u);
-        const unsigned target = k * gridDim.x;
-        const uint64_t t0 = globaltimer_ns();
-        int ok = 1;
-        while (ld_acquire_u32(count) < target) {
-            if (*(volatile int*)err != 0 || globaltimer_ns() - t0 > kBarrierWaitNs) {
-                atomicExch(err, 1);
-                ok = 0;
-                break;
-            }
-            __nanosleep(64);
-        }
-        __threadfence();
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
 // Persistent batched MLEM: `steps` iterations of the tile in one cooperative
 // launch (every block resident).  Per iteration: forward projection and
 // correlation over all rows of A, grid barrier, back projection and update

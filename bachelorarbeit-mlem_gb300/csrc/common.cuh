@@ -58,6 +58,49 @@ __device__ __forceinline__ uint4 ld_stream_u4(const uint4* p) { return __ldcs(p)
 __device__ __forceinline__ uint2 ld_stream_u2(const uint2* p) { return __ldcs(p); }
 __device__ __forceinline__ float4 ld_stream_f4(const float4* p) { return __ldcs(p); }
 
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide barrier of a cooperative launch: barrier k of the launch is
+// passed once `count` (zeroed before the launch) reaches k * gridDim.x.  Every
+// wait is bounded: after kBarrierWaitNs, or as soon as another block has given
+// up, the block sets *err and the caller returns, so a failure ends the launch
+// with an error flag the host reads instead of a hang.
+constexpr uint64_t kBarrierWaitNs = 2000000000ull;  // 2 s; a phase takes milliseconds
+
+__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned k, int* err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(count, 1u);
+        const unsigned target = k * gridDim.x;
+        const uint64_t t0 = globaltimer_ns();
+        int ok = 1;
+        while (ld_acquire_u32(count) < target) {
+            if (*(volatile int*)err != 0 || globaltimer_ns() - t0 > kBarrierWaitNs) {
+                atomicExch(err, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
 // Value storage types: load 4 consecutive values (element index 4*v .. 4*v+3).
 template <typename V>
 struct Val4;

@@ -714,6 +714,7 @@ def forms_summary(forms, fp32_rate):
     put("fp16_d16_images_iter_s", forms.get("fp16_trans", {}).get("images_iterations_per_s"), fp32_rate)
     mid = forms.get("fp32_plain_cyl3d_mid", {}).get("images_iterations_per_s")
     put("mid_fp32_plain_iter_s", mid)
+    put("ring2d_fp32_plain_iter_s", forms.get("fp32_plain_ring2d", {}).get("images_iterations_per_s"), nd=0)
     b = forms.get("batched_fp16_64", {})
     put("batched_fp16_64_images_iter_s", b.get("images_iterations_per_s"), mid)
     put("batched_persistent_images_iter_s", b.get("persistent_images_iterations_per_s"))
