@@ -62,7 +62,8 @@ class MatrixInfo(C.Structure):
                 ("sym_lor_rows", C.c_uint32), ("sym_voxel_rows", C.c_uint32),
                 ("sym_fp_nnz", C.c_uint64), ("sym_bp_nnz", C.c_uint64),
                 ("d16_slots", C.c_uint64), ("d16_slots_t", C.c_uint64),
-                ("d16_lanes", C.c_uint32), ("d16_lanes_t", C.c_uint32)]
+                ("d16_lanes", C.c_uint32), ("d16_lanes_t", C.c_uint32),
+                ("loop_iteration_ms", C.c_float), ("graph_iteration_ms", C.c_float)]
 
 
 class RunOpts(C.Structure):
@@ -290,6 +291,15 @@ class Matrix:
                          "fp_nnz": info.sym_fp_nnz, "bp_nnz": info.sym_bp_nnz} if info.sym_lor_rows else None
         self.d16 = {"slots": info.d16_slots, "slots_t": info.d16_slots_t, "lanes": info.d16_lanes,
                     "lanes_t": info.d16_lanes_t} if info.d16_slots else None
+
+    def loop_timing(self) -> dict | None:
+        """Per-iteration ms of the persistent loop and of per-iteration graphs,
+        once a run has timed them for this matrix (else None)."""
+        info = MatrixInfo()
+        _check(load_library().mlem_matrix_get_info(self._h, C.byref(info)))
+        if not info.loop_iteration_ms:
+            return None
+        return {"loop_ms": info.loop_iteration_ms, "graph_ms": info.graph_iteration_ms}
 
     # construction ---------------------------------------------------------
     @staticmethod

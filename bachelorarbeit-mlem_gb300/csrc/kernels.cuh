@@ -103,6 +103,7 @@ struct MergePlan {
     // true: the row-parallel tile kernel (library-owned, padded operands);
     // false: the per-thread walk over shared-memory products (any arrays)
     bool rows_kernel = false;
+    int rows_u = 1;              // row kernel: vectors per lane in flight (1: 8 blocks per SM, 2: 6)
     void release();
 };
 // Builds the tile partition of `op` for a section size (device allocations).

@@ -134,10 +134,10 @@ void loop_launch(const DevCsr& A, const DevCsr& AT, int lpr_fp, int lpr_bp, cons
     int dev = 0, sms = 0;
     MLEM_CUDA(cudaGetDevice(&dev));
     MLEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    // enough groups for the larger operand, at most a quarter of a resident
-    // wave, so that a few such launches on other streams fit beside each other
+    // enough groups for the larger operand, at most half a resident wave, so
+    // that two such launches on other streams fit beside each other
     const uint64_t need = std::max<uint64_t>((uint64_t)A.nrows * lpr_fp, (uint64_t)AT.nrows * lpr_bp);
-    const unsigned cap = (unsigned)std::max(1, bps * sms / 4);
+    const unsigned cap = (unsigned)std::max(1, bps * sms / 2);
     const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(cap, (need + 255) / 256));
     MLEM_CUDA(cudaMemsetAsync(count, 0, sizeof(unsigned), s));
     cudaLaunchConfig_t cfg = {};

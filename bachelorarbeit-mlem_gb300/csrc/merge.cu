@@ -265,18 +265,42 @@ __global__ void k_merge_fixup(const uint32_t* __restrict__ ti, const float* __re
 // epilogue here, the tile's first row (which began in an earlier tile) goes
 // to head[k] and the row still open at the tile's end to carry[k], for the
 // same fix-up kernel.  Deterministic.
-template <typename V, int LPR>
+template <typename V, int LPR, int U>
 __device__ __forceinline__ float group_part_dot(const uint32_t* __restrict__ idx, const V* __restrict__ val,
                                                 const float* __restrict__ x, uint64_t s, uint64_t t, int sub) {
     const uint4* idx4 = reinterpret_cast<const uint4*>(idx);
     const uint64_t v1 = (t + 3) >> 2;
     float acc = 0.f;
-    for (uint64_t v = (s >> 2) + sub; v < v1; v += LPR) {
+    // U = 2: two vectors per lane in flight; the FMAs still run in the lane's
+    // vector order, so the sums are those of one vector at a time
+    uint64_t v = (s >> 2) + sub;
+    if constexpr (U == 2)
+    for (; v + LPR < v1; v += 2 * LPR) {
+        const uint4 c0 = __ldcs(idx4 + v), c1 = __ldcs(idx4 + v + LPR);
+        float a0[4], a1[4];
+        Val4<V>::load(val, v, a0);
+        Val4<V>::load(val, v + LPR, a1);
+        const uint32_t cs0[4] = {c0.x, c0.y, c0.z, c0.w}, cs1[4] = {c1.x, c1.y, c1.z, c1.w};
+        // element 4v+k lies in [s, t) unless it is a masked head or tail element
+        const uint32_t lo = (uint32_t)(s > 4 * v ? s - 4 * v : 0);
+        const uint32_t hi1 = (uint32_t)(t - 4 * (v + LPR));  // the second vector starts past the head
+        float g0[4], g1[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) g0[k] = (k >= (int)lo) ? __ldg(x + cs0[k]) : 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) g1[k] = (k < (int)hi1) ? __ldg(x + cs1[k]) : 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k >= (int)lo) acc = fmaf(a0[k], g0[k], acc);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < (int)hi1) acc = fmaf(a1[k], g1[k], acc);
+    }
+    for (; v < v1; v += LPR) {
         const uint4 c = __ldcs(idx4 + v);
         float a[4];
         Val4<V>::load(val, v, a);
         const uint32_t cs[4] = {c.x, c.y, c.z, c.w};
-        // element 4v+k lies in [s, t) unless it is a masked head or tail element
         const uint32_t lo = (uint32_t)(s > 4 * v ? s - 4 * v : 0), hi = (uint32_t)(t - 4 * v);
         float g[4];
 #pragma unroll
@@ -288,8 +312,8 @@ __device__ __forceinline__ float group_part_dot(const uint32_t* __restrict__ idx
     return acc;
 }
 
-template <typename V, int LPR>
-__global__ void __launch_bounds__(256, 8)
+template <typename V, int LPR, int U>
+__global__ void __launch_bounds__(256, U == 1 ? 8 : 6)
 k_merge_rows(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx, const V* __restrict__ val,
              const float* __restrict__ x, uint32_t rows, const uint32_t* __restrict__ ti,
              const uint64_t* __restrict__ tj, float* __restrict__ carry, uint32_t* __restrict__ carry_row,
@@ -309,7 +333,7 @@ k_merge_rows(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ i
             uint64_t s = rowptr[r], t = rowptr[r + 1];
             s = s < J0 ? J0 : s;
             t = t > J1 ? J1 : t;
-            if (s < t) acc = group_part_dot<V, LPR>(idx, val, x, s, t, sub);
+            if (s < t) acc = group_part_dot<V, LPR, U>(idx, val, x, s, t, sub);
         }
 #pragma unroll
         for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(mask, acc, o);
@@ -329,8 +353,11 @@ k_merge_rows(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ i
 template <typename V>
 void merge_launch_t(const DevCsr& op, const MergePlan& p, const float* x, const EpiDev& e,
                     L2Window win, cudaStream_t s) {
-    if (p.rows_kernel)
-        launch_ex(k_merge_rows<V, 16>, dim3((unsigned)p.ntiles), dim3(256), 0, s, win, op.rowptr, op.idx,
+    if (p.rows_kernel && p.rows_u == 2)
+        launch_ex(k_merge_rows<V, 16, 2>, dim3((unsigned)p.ntiles), dim3(256), 0, s, win, op.rowptr, op.idx,
+                  static_cast<const V*>(op.val), x, op.nrows, p.tile_i, p.tile_j, p.carry, p.carry_row, p.head, e);
+    else if (p.rows_kernel)
+        launch_ex(k_merge_rows<V, 16, 1>, dim3((unsigned)p.ntiles), dim3(256), 0, s, win, op.rowptr, op.idx,
                   static_cast<const V*>(op.val), x, op.nrows, p.tile_i, p.tile_j, p.carry, p.carry_row, p.head, e);
     else
         launch_ex(k_merge_tile<V>, dim3((unsigned)p.ntiles), dim3(p.threads), p.smem, s, win,

@@ -216,8 +216,56 @@ const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
     auto it = plans.find(secsize);
     if (it != plans.end()) return it->second;
     MergePlan p;
-    merge_plan_build(transposed ? m->AT : m->A, secsize, p, m->stream);
-    MLEM_CUDA(cudaStreamSynchronize(m->stream));
+    const DevCsr& op = transposed ? m->AT : m->A;
+    cudaStream_t s = m->stream;
+    merge_plan_build(op, secsize, p, s);
+    MLEM_CUDA(cudaStreamSynchronize(s));
+    if (p.rows_kernel && op.nnz) {
+        // one or two vectors per lane in flight in the row kernel (6 or 8 blocks
+        // per SM), timed with a Raw epilogue on an image of ones; same sums
+        float *x = nullptr, *y = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        float best = 1e30f;
+        int pick = 1;
+        try {
+            MLEM_CUDA(cudaMalloc(&x, sizeof(float) * std::max<uint32_t>(op.ncols, 1)));
+            MLEM_CUDA(cudaMalloc(&y, sizeof(float) * std::max<uint32_t>(op.nrows, 1)));
+            std::vector<float> ones(std::max<uint32_t>(op.ncols, 1), 1.0f);
+            MLEM_CUDA(cudaMemcpyAsync(x, ones.data(), sizeof(float) * ones.size(), cudaMemcpyHostToDevice, s));
+            MLEM_CUDA(cudaEventCreate(&e0));
+            MLEM_CUDA(cudaEventCreate(&e1));
+            EpiArgs e;
+            e.kind = Epi::Raw;
+            e.out = y;
+            for (int u : {1, 2}) {
+                p.rows_u = u;
+                launch_merge_spmv(op, p, x, e, L2Window{}, s);
+                MLEM_CUDA(cudaEventRecord(e0, s));
+                for (int q = 0; q < 2; ++q) launch_merge_spmv(op, p, x, e, L2Window{}, s);
+                MLEM_CUDA(cudaEventRecord(e1, s));
+                MLEM_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                MLEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    pick = u;
+                }
+            }
+        } catch (...) {
+            cudaStreamSynchronize(s);
+            cudaFree(x);
+            cudaFree(y);
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            p.release();
+            throw;
+        }
+        cudaFree(x);
+        cudaFree(y);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        p.rows_u = pick;
+    }
     return plans.emplace(secsize, p).first->second;
 }
 
@@ -1108,6 +1156,8 @@ mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info) {
         info->d16_slots_t = m->has_t ? 8 * m->AT.dvec : 0;
         info->d16_lanes = (uint32_t)m->A.d16_lanes;
         info->d16_lanes_t = m->has_t ? (uint32_t)m->AT.d16_lanes : 0;
+        info->loop_iteration_ms = m->loop_ms;
+        info->graph_iteration_ms = m->loop_graph_ms;
     });
 }
 

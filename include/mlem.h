@@ -160,6 +160,9 @@ typedef struct {
      * value each) and the lanes per row their layout is built for */
     uint64_t d16_slots, d16_slots_t;
     uint32_t d16_lanes, d16_lanes_t;
+    /* once a run has timed the persistent loop (kernel LOOP) against per-iteration
+     * graphs for this matrix: the time of one iteration of each, in ms (else 0) */
+    float loop_iteration_ms, graph_iteration_ms;
 } mlem_matrix_info;
 
 mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info);
