@@ -25,8 +25,7 @@ LIB_PATH = PKG / "lib" / "libmlem_gb300.so"
 CLI_PATH = PKG / "bin" / "mlem_gb300"
 
 SPMV_MERGE, SPMV_CSR_VECTOR = 0, 1
-(KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO, KERNEL_D16, KERNEL_ILV, KERNEL_ORDERED, KERNEL_SYM,
- KERNEL_LOOP) = range(9)
+KERNEL_DIRECT, KERNEL_TMA, KERNEL_PERSISTENT, KERNEL_AUTO, KERNEL_D16, KERNEL_ILV, KERNEL_ORDERED, KERNEL_SYM = range(8)
 LAYOUT_NATURAL, LAYOUT_LOCALITY = 0, 1
 VAL_F32, VAL_F16, VAL_BF16 = 0, 1, 2
 BP_TRANS, BP_SCATTER, BP_FUSED = 0, 1, 2
@@ -62,8 +61,7 @@ class MatrixInfo(C.Structure):
                 ("sym_lor_rows", C.c_uint32), ("sym_voxel_rows", C.c_uint32),
                 ("sym_fp_nnz", C.c_uint64), ("sym_bp_nnz", C.c_uint64),
                 ("d16_slots", C.c_uint64), ("d16_slots_t", C.c_uint64),
-                ("d16_lanes", C.c_uint32), ("d16_lanes_t", C.c_uint32),
-                ("loop_iteration_ms", C.c_float), ("graph_iteration_ms", C.c_float)]
+                ("d16_lanes", C.c_uint32), ("d16_lanes_t", C.c_uint32)]
 
 
 class RunOpts(C.Structure):
@@ -291,15 +289,6 @@ class Matrix:
                          "fp_nnz": info.sym_fp_nnz, "bp_nnz": info.sym_bp_nnz} if info.sym_lor_rows else None
         self.d16 = {"slots": info.d16_slots, "slots_t": info.d16_slots_t, "lanes": info.d16_lanes,
                     "lanes_t": info.d16_lanes_t} if info.d16_slots else None
-
-    def loop_timing(self) -> dict | None:
-        """Per-iteration ms of the persistent loop and of per-iteration graphs,
-        once a run has timed them for this matrix (else None)."""
-        info = MatrixInfo()
-        _check(load_library().mlem_matrix_get_info(self._h, C.byref(info)))
-        if not info.loop_iteration_ms:
-            return None
-        return {"loop_ms": info.loop_iteration_ms, "graph_ms": info.graph_iteration_ms}
 
     # construction ---------------------------------------------------------
     @staticmethod

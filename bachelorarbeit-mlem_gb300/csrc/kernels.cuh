@@ -241,15 +241,6 @@ inline uint32_t batch_width(uint32_t tile, uint32_t active) {
     a.active = active;
     return a.width();
 }
-// `iters` whole MLEM iterations (csr-vector forward projection + correlation,
-// back projection over Aᵀ + update, the given lanes per row and vectors in
-// flight) in one persistent cooperative launch with bounded grid barriers;
-// bit-identical to the same configuration launched per iteration.  count is
-// zeroed here; *err becomes 1 if a barrier wait ran out.  For L2-resident
-// matrices, where launches dominate an iteration (loop.cu).
-void launch_mlem_loop(const DevCsr& A, const DevCsr& AT, int lanes_fp, int lanes_bp, int unroll, const int32_t* g,
-                      float* ratio, float* f, const float* norm, uint32_t iters, unsigned* count, int* err,
-                      cudaStream_t s);
 // `steps` whole iterations of the tile (FP, BP + update, tick) in one
 // persistent cooperative launch with grid-wide barriers; count (one word,
 // zeroed here before the launch) carries the barriers, *err becomes 1 if a

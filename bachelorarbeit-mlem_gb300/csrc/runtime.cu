@@ -43,7 +43,6 @@ void Workspace::release() {
     cudaFree(ll_part);
     cudaFree(ll_vals);
     cudaFree(err);
-    cudaFree(bar);
     cudaFree(tmp_rows);
     cudaFree(tmp_cols);
     *this = Workspace();
@@ -122,8 +121,6 @@ void ensure_workspace(mlem_matrix* m) {
     MLEM_CUDA(cudaMalloc(&w.ll_part, sizeof(double) * kLoglikParts));
     MLEM_CUDA(cudaMalloc(&w.err, sizeof(uint32_t)));
     MLEM_CUDA(cudaMemsetAsync(w.err, 0, sizeof(uint32_t), m->stream));
-    MLEM_CUDA(cudaMalloc(&w.bar, 64));
-    MLEM_CUDA(cudaMemsetAsync(w.bar, 0, 64, m->stream));
     MLEM_CUDA(cudaMemsetAsync(w.bp, 0, sizeof(float) * C, m->stream));
     MLEM_CUDA(cudaMemsetAsync(w.ratio, 0, sizeof(float) * R, m->stream));
     if (m->lor_of || m->vox_of) {
@@ -271,8 +268,8 @@ const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
 
 
 void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o) {
-    MLEM_REQUIRE(o.kernel <= MLEM_KERNEL_LOOP, MLEM_EINVAL,
-                 "kernel must be 0 direct, 1 tma, 2 persistent, 3 auto, 4 d16, 5 ilv, 6 ordered, 7 sym or 8 loop");
+    MLEM_REQUIRE(o.kernel <= MLEM_KERNEL_SYM, MLEM_EINVAL,
+                 "kernel must be 0 direct, 1 tma, 2 persistent, 3 auto, 4 d16, 5 ilv, 6 ordered or 7 sym");
     MLEM_REQUIRE(o.kernel != MLEM_KERNEL_SYM || m->sym.fp_rowptr != nullptr, MLEM_EINVAL,
                  "kernel SYM needs a matrix generated with symmetry = 1");
     MLEM_REQUIRE(o.lanes == 0 || o.lanes == 4 || o.lanes == 8 || o.lanes == 16 || o.lanes == 32, MLEM_EINVAL,
@@ -309,8 +306,7 @@ void check_device_error(mlem_matrix* m, cudaStream_t s) {
     if (h) {
         MLEM_CUDA(cudaMemsetAsync(w.err, 0, sizeof(uint32_t), s));
         MLEM_CUDA(cudaStreamSynchronize(s));
-        fail(MLEM_ETIMEOUT,
-             "a kernel gave up a bounded wait (pipelined copies or a grid barrier); results are invalid");
+        fail(MLEM_ETIMEOUT, "a pipelined projection kernel gave up waiting for its copies; results are invalid");
     }
 }
 
@@ -408,7 +404,7 @@ static void tune_projection(mlem_matrix* m, bool transposed) {
 void prepare_kernel(mlem_matrix* m, const mlem_run_opts& o) {
     if (o.kernel == MLEM_KERNEL_TMA) prepare_csr_tma(m->vt);
     else if (o.kernel == MLEM_KERNEL_PERSISTENT) prepare_csrvec_pipe(m->vt);
-    else if (o.kernel == MLEM_KERNEL_AUTO || o.kernel == MLEM_KERNEL_LOOP) {
+    else if (o.kernel == MLEM_KERNEL_AUTO) {
         tune_projection(m, false);
         if (m->has_t) tune_projection(m, true);
     }
@@ -418,7 +414,7 @@ void prepare_kernel(mlem_matrix* m, const mlem_run_opts& o) {
 static ProjCfg resolve_cfg(const mlem_matrix* m, bool transposed, const mlem_run_opts& o) {
     const DevCsr& op = transposed ? m->AT : m->A;
     ProjCfg c;
-    if (o.kernel == MLEM_KERNEL_AUTO || o.kernel == MLEM_KERNEL_LOOP) {
+    if (o.kernel == MLEM_KERNEL_AUTO) {
         MLEM_REQUIRE(m->tuned[transposed], MLEM_EINVAL, "internal: projection used before autotuning");
         c = m->proj[transposed];
     } else if (o.kernel == MLEM_KERNEL_PERSISTENT && (o.lanes >= 16 || pick_lanes(op.nnz, op.nrows) >= 16)) {
@@ -600,142 +596,8 @@ static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cud
     if (fused) sym_scatter_image(m->sym, m->ws.f, s);
 }
 
-// Matrices whose operands fit in L2 (here at most 48 MB of A and Aᵀ) may run
-// whole reconstructions in one persistent launch (loop.cu).
-constexpr uint64_t kLoopMaxBytes = 48ull << 20;
-
-// The persistent loop applies where the autotuned configuration is the plain
-// csr-vector kernel for both projections with the same vectors in flight; it
-// is used where, timed once per matrix against CUDA graphs of the same
-// kernels (scratch vectors, 32 iterations each), it is faster.
-// The two csr-vector configurations the loop runs: the autotuned ones, or
-// with kernel LOOP and lanes given, the plain kernel with those lanes and
-// vectors in flight for both operands.
-static void loop_cfgs(const mlem_matrix* m, const mlem_run_opts& o, ProjCfg& a, ProjCfg& b) {
-    if (o.kernel == MLEM_KERNEL_LOOP && o.lanes) {
-        a = ProjCfg{MLEM_KERNEL_DIRECT, (int)o.lanes, o.unroll ? (int)o.unroll : 2, 0.f, false, false};
-        b = a;
-    } else {
-        a = resolve_cfg(m, false, o);
-        b = resolve_cfg(m, true, o);
-    }
-}
-
-// kernel LOOP forces it (for any size) where it applies, else MLEM_EINVAL.
-static bool use_mlem_loop(mlem_matrix* m, const mlem_run_opts& o, bool fused) {
-    const bool forced = o.kernel == MLEM_KERNEL_LOOP;
-    if (forced)
-        MLEM_REQUIRE(!fused && o.spmv == MLEM_SPMV_CSR_VECTOR && o.bp_mode == MLEM_BP_TRANS && m->has_t, MLEM_EINVAL,
-                     "kernel LOOP needs csr-vector SpMV and the transposed back projection");
-    if (!forced && (fused || o.kernel != MLEM_KERNEL_AUTO || o.spmv != MLEM_SPMV_CSR_VECTOR ||
-                    o.bp_mode != MLEM_BP_TRANS || !m->has_t || csr_bytes(m->A) + csr_bytes(m->AT) > kLoopMaxBytes))
-        return false;
-    prepare_kernel(m, o);  // the autotuner's choice for both operands
-    ProjCfg a, b;
-    loop_cfgs(m, o, a, b);
-    const bool applies = a.kind == MLEM_KERNEL_DIRECT && b.kind == MLEM_KERNEL_DIRECT && !a.ordered && !b.ordered &&
-                         !a.pipelined && !b.pipelined && a.unroll == b.unroll;
-    if (forced) {
-        MLEM_REQUIRE(applies, MLEM_EINVAL,
-                     "kernel LOOP needs the autotuned plain csr-vector kernel for both projections with the same "
-                     "vectors in flight");
-        return true;
-    }
-    if (!applies) return false;
-    if (m->loop_choice) return m->loop_choice == 2;
-    const uint32_t R = std::max<uint32_t>(m->A.nrows, 1), C = std::max<uint32_t>(m->A.ncols, 1);
-    cudaStream_t s = m->stream;
-    int32_t* g = nullptr;
-    float *f = nullptr, *ratio = nullptr;
-    cudaStream_t cs = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    cudaEvent_t e[3] = {};
-    float ms_graph = 0.f, ms_loop = 0.f;
-    ensure_workspace(m);
-    try {
-        MLEM_CUDA(cudaMalloc(&g, sizeof(int32_t) * R));
-        MLEM_CUDA(cudaMalloc(&f, sizeof(float) * C));
-        MLEM_CUDA(cudaMalloc(&ratio, sizeof(float) * R));
-        std::vector<int32_t> ones_g(R, 1);
-        std::vector<float> ones_f(C, 1.0f);
-        MLEM_CUDA(cudaMemcpyAsync(g, ones_g.data(), sizeof(int32_t) * R, cudaMemcpyHostToDevice, s));
-        MLEM_CUDA(cudaMemcpyAsync(f, ones_f.data(), sizeof(float) * C, cudaMemcpyHostToDevice, s));
-        MLEM_CUDA(cudaStreamSynchronize(s));
-        EpiArgs fe, be;
-        fe.kind = Epi::Correl;
-        fe.g = g;
-        fe.out = ratio;
-        be.kind = Epi::Update;
-        be.f = f;
-        be.norm = m->norm;
-        MLEM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        const uint64_t l0 = g_launches.load();
-        MLEM_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        for (int q = 0; q < 8; ++q) {
-            launch_cfg(m, m->A, f, fe, a, {}, cs);
-            launch_cfg(m, m->AT, ratio, be, b, {}, cs);
-        }
-        MLEM_CUDA(cudaStreamEndCapture(cs, &graph));
-        g_launches.fetch_sub(g_launches.load() - l0);
-        MLEM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-        for (auto& ev : e) MLEM_CUDA(cudaEventCreate(&ev));
-        MLEM_CUDA(cudaGraphLaunch(exec, s));  // warm-up
-        launch_mlem_loop(m->A, m->AT, a.lanes, b.lanes, a.unroll, g, ratio, f, m->norm, 8, m->ws.bar,
-                         reinterpret_cast<int*>(m->ws.err), s);
-        MLEM_CUDA(cudaEventRecord(e[0], s));
-        for (int q = 0; q < 4; ++q) MLEM_CUDA(cudaGraphLaunch(exec, s));
-        MLEM_CUDA(cudaEventRecord(e[1], s));
-        launch_mlem_loop(m->A, m->AT, a.lanes, b.lanes, a.unroll, g, ratio, f, m->norm, 32, m->ws.bar,
-                         reinterpret_cast<int*>(m->ws.err), s);
-        MLEM_CUDA(cudaEventRecord(e[2], s));
-        MLEM_CUDA(cudaEventSynchronize(e[2]));
-        MLEM_CUDA(cudaEventElapsedTime(&ms_graph, e[0], e[1]));
-        MLEM_CUDA(cudaEventElapsedTime(&ms_loop, e[1], e[2]));
-        check_device_error(m, s);
-    } catch (...) {
-        if (cs) {
-            cudaGraph_t dangling = nullptr;
-            cudaStreamEndCapture(cs, &dangling);
-            if (dangling) cudaGraphDestroy(dangling);
-        }
-        cudaStreamSynchronize(s);
-        for (auto& ev : e)
-            if (ev) cudaEventDestroy(ev);
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        if (cs) cudaStreamDestroy(cs);
-        cudaFree(g);
-        cudaFree(f);
-        cudaFree(ratio);
-        throw;
-    }
-    for (auto& ev : e) cudaEventDestroy(ev);
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
-    cudaStreamDestroy(cs);
-    cudaFree(g);
-    cudaFree(f);
-    cudaFree(ratio);
-    m->loop_choice = ms_loop < ms_graph ? 2 : 1;
-    m->loop_ms = ms_loop / 32;
-    m->loop_graph_ms = ms_graph / 32;
-    return m->loop_choice == 2;
-}
-
 static void run_iterations(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
                            double* ll_dev, StageTimer* timer, bool fused) {
-    if (o.kernel == MLEM_KERNEL_LOOP)
-        MLEM_REQUIRE(o.loglik_every == 0 && !timer, MLEM_EINVAL,
-                     "kernel LOOP runs without per-iteration log-likelihood and stage timing");
-    if (o.loglik_every == 0 && !timer && (o.kernel == MLEM_KERNEL_LOOP || (o.use_graph && iters >= 2)) &&
-        use_mlem_loop(m, o, fused)) {
-        ProjCfg a, b;
-        loop_cfgs(m, o, a, b);
-        launch_mlem_loop(m->A, m->AT, a.lanes, b.lanes, a.unroll, m->ws.g, m->ws.ratio, m->ws.f, m->norm, iters,
-                         m->ws.bar, reinterpret_cast<int*>(m->ws.err), s);
-        return;
-    }
     if (o.loglik_every > 0 || !o.use_graph || timer) {
         for (uint32_t it = 0; it < iters; ++it) {
             double* slot = (o.loglik_every > 0 && it % o.loglik_every == 0) ? ll_dev + it : nullptr;
@@ -1156,8 +1018,6 @@ mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info) {
         info->d16_slots_t = m->has_t ? 8 * m->AT.dvec : 0;
         info->d16_lanes = (uint32_t)m->A.d16_lanes;
         info->d16_lanes_t = m->has_t ? (uint32_t)m->AT.d16_lanes : 0;
-        info->loop_iteration_ms = m->loop_ms;
-        info->graph_iteration_ms = m->loop_graph_ms;
     });
 }
 

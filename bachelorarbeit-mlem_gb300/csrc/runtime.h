@@ -66,7 +66,6 @@ struct Workspace {
     double* ll_vals = nullptr; // [ll_cap]
     uint32_t ll_cap = 0;
     uint32_t* err = nullptr;   // set by kernels whose bounded waits expired
-    unsigned* bar = nullptr;   // barrier word of the persistent MLEM loop
     float* tmp_rows = nullptr; // [rows] staging in natural order (locality layout only)
     float* tmp_cols = nullptr; // [cols] staging in natural order (locality layout only)
     std::map<RunKey, cudaGraphExec_t> graphs;
@@ -138,8 +137,6 @@ struct mlem_matrix {
     uint32_t batch_tile = 0;          // autotuned batch tile (0 = not yet)
     uint32_t batch_form = 0;          // autotuned batch form: 1 graphs, 2 persistent (0 = not yet)
     int scatter_lanes = 0;            // autotuned lanes per row of the scatter back projection (0 = not yet)
-    int loop_choice = 0;              // persistent MLEM loop for small matrices: 1 no, 2 yes (0 = not timed yet)
-    float loop_ms = 0.f, loop_graph_ms = 0.f;  // per iteration when it was timed: loop, per-iteration graphs
     bool tuned[2] = {false, false};   // csr-vector configuration of A / Aᵀ measured
     mlem::ProjCfg proj[2];
     std::mutex mu;

@@ -500,16 +500,6 @@ def run_forms(pkg, torch, args):
         b.record(s)
         b.synchronize()
         res[f"fp32_plain_{small}"] = {"images_iterations_per_s": 3 * its / (a.elapsed_time(b) * 1e-3)}
-        if small == "ring2d":
-            # the persistent loop forced (the default keeps the faster of it and the graphs)
-            a.record(s)
-            for _ in range(3):
-                fs.copy_(f0s)
-                msm.run_device(gsd.data_ptr(), fs.data_ptr(), its, stream=s.cuda_stream, kernel=pkg.KERNEL_LOOP)
-            b.record(s)
-            b.synchronize()
-            res["fp32_loop_ring2d"] = {"iterations_per_s": 3 * its / (a.elapsed_time(b) * 1e-3),
-                                       "timed_once": msm.loop_timing()}
         if small == "cyl3d_mid":
             # the reference's four switch combinations (argv[8] merge/csr-vector x argv[7]
             # transposed/scatter) and the fused single pass, FP32, 100 iterations each
@@ -725,7 +715,6 @@ def forms_summary(forms, fp32_rate):
     mid = forms.get("fp32_plain_cyl3d_mid", {}).get("images_iterations_per_s")
     put("mid_fp32_plain_iter_s", mid)
     put("ring2d_fp32_plain_iter_s", forms.get("fp32_plain_ring2d", {}).get("images_iterations_per_s"), nd=0)
-    put("ring2d_fp32_loop_iter_s", forms.get("fp32_loop_ring2d", {}).get("iterations_per_s"), nd=0)
     b = forms.get("batched_fp16_64", {})
     put("batched_fp16_64_images_iter_s", b.get("images_iterations_per_s"), mid)
     put("batched_persistent_images_iter_s", b.get("persistent_images_iterations_per_s"))

@@ -160,9 +160,6 @@ typedef struct {
      * value each) and the lanes per row their layout is built for */
     uint64_t d16_slots, d16_slots_t;
     uint32_t d16_lanes, d16_lanes_t;
-    /* once a run has timed the persistent loop (kernel LOOP) against per-iteration
-     * graphs for this matrix: the time of one iteration of each, in ms (else 0) */
-    float loop_iteration_ms, graph_iteration_ms;
 } mlem_matrix_info;
 
 mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info);
@@ -224,16 +221,7 @@ typedef enum {
     MLEM_KERNEL_ILV = 5,  /* lane-interleaved copy (matrix created with interleave = 1) */
     MLEM_KERNEL_ORDERED = 6, /* DIRECT with rows in locality order (generated matrices:
                                LORs in 4x4 detector tubes, voxels in 4x2x2 bricks) */
-    MLEM_KERNEL_SYM = 7,  /* symmetry-compressed operands (generated with symmetry = 1) */
-    MLEM_KERNEL_LOOP = 8  /* the autotuned csr-vector kernels, all iterations of a reconstruction
-                             in one persistent launch (grid-wide barriers between the
-                             projections; bit-identical to AUTO).  AUTO itself picks it for
-                             matrices of at most 48 MB (A + Aᵀ) where, timed once, it is faster
-                             than per-iteration graphs.  Needs csr-vector, transposed BP and an
-                             autotuned choice of the plain csr-vector kernel with the same
-                             vectors in flight for both operands (MLEM_EINVAL otherwise); with
-                             `lanes` (and `unroll`) given, the plain kernel with those lanes for
-                             both operands instead (bit-identical to DIRECT with them). */
+    MLEM_KERNEL_SYM = 7   /* symmetry-compressed operands (generated with symmetry = 1) */
 } mlem_kernel;
 
 /* Defaults: CSR_VECTOR, BP_TRANS, secsize 5/5, graphs on, no log-likelihood, L2 window on,
