@@ -70,8 +70,9 @@ void launch_csrvec_pipe(const DevCsr& op, const float* x, const EpiArgs& epi, in
 void prepare_csr_tma(mlem_value_type vt);
 void launch_csr_tma(const DevCsr& op, const float* x, const EpiArgs& epi, uint32_t* err, L2Window win,
                     cudaStream_t s);
-// bp[idx] += val * ratio[row] over the rows of A (calcBwProj_none_trans, kernel.cu:165-177).
-void launch_scatter(const DevCsr& A, const float* ratio, float* bp, int lanes, L2Window win,
+// bp[idx] += val * ratio[row] over the rows of A (calcBwProj_none_trans, kernel.cu:165-177);
+// lanes per row 8/16/32, unroll = 16-byte vectors per lane in flight (1 or 2).
+void launch_scatter(const DevCsr& A, const float* ratio, float* bp, int lanes, int unroll, L2Window win,
                     cudaStream_t s);
 // One pass over A: sum = A[r,:]·x, ratio = g[r]/sum, bp[idx] += val*ratio.
 void launch_fused_fp_scatter(const DevCsr& A, const float* x, const int32_t* g, float* bp,

@@ -161,15 +161,16 @@ static void cols_out(const mlem_matrix* m, float* dst, const float* src, cudaStr
 }
 static bool permuted(const mlem_matrix* m) { return m->lor_of || m->vox_of; }
 
-// Lanes per row of A for the scatter back projection: 8, 16 or 32 around the
-// row length, timed once per matrix (ratio 1 into a scratch image).
+// Lanes per row of A (8, 16 or 32) and 16-byte vectors per lane in flight (1
+// or 2) for the scatter back projection, timed once per matrix (ratio 1 into a
+// scratch image).  Returns the lanes; m->scatter_unroll holds the vectors.
 int scatter_lanes(mlem_matrix* m) {
     if (m->scatter_lanes) return m->scatter_lanes;
     const DevCsr& A = m->A;
     cudaStream_t s = m->stream;
     float *r = nullptr, *bp = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    int best_l = pick_lanes(A.nnz, A.nrows) < 8 ? 8 : pick_lanes(A.nnz, A.nrows);
+    int best_l = pick_lanes(A.nnz, A.nrows) < 8 ? 8 : pick_lanes(A.nnz, A.nrows), best_u = 1;
     float best = 1e30f;
     try {
         MLEM_CUDA(cudaMalloc(&r, sizeof(float) * std::max<uint32_t>(A.nrows, 1)));
@@ -179,19 +180,21 @@ int scatter_lanes(mlem_matrix* m) {
         MLEM_CUDA(cudaMemsetAsync(bp, 0, sizeof(float) * std::max<uint32_t>(A.ncols, 1), s));
         MLEM_CUDA(cudaEventCreate(&e0));
         MLEM_CUDA(cudaEventCreate(&e1));
-        for (int lanes : {8, 16, 32}) {
-            launch_scatter(A, r, bp, lanes, {}, s);
-            MLEM_CUDA(cudaEventRecord(e0, s));
-            for (int q = 0; q < 2; ++q) launch_scatter(A, r, bp, lanes, {}, s);
-            MLEM_CUDA(cudaEventRecord(e1, s));
-            MLEM_CUDA(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            MLEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            if (ms < best) {
-                best = ms;
-                best_l = lanes;
+        for (int lanes : {8, 16, 32})
+            for (int u : {1, 2}) {
+                launch_scatter(A, r, bp, lanes, u, {}, s);
+                MLEM_CUDA(cudaEventRecord(e0, s));
+                for (int q = 0; q < 2; ++q) launch_scatter(A, r, bp, lanes, u, {}, s);
+                MLEM_CUDA(cudaEventRecord(e1, s));
+                MLEM_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                MLEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    best_l = lanes;
+                    best_u = u;
+                }
             }
-        }
     } catch (...) {
         cudaStreamSynchronize(s);
         cudaFree(r);
@@ -204,6 +207,7 @@ int scatter_lanes(mlem_matrix* m) {
     cudaFree(bp);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    m->scatter_unroll = best_u;
     m->scatter_lanes = best_l;
     return best_l;
 }
@@ -545,7 +549,8 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
             }
             project(m, true, w.ratio, be, o, wr, s);
         } else {
-            launch_scatter(A, w.ratio, w.bp, scatter_lanes(m), wr, s);
+            const int sl = scatter_lanes(m);  // sets m->scatter_unroll on the first call
+            launch_scatter(A, w.ratio, w.bp, sl, m->scatter_unroll, wr, s);
             launch_update_zero(w.f, w.bp, m->norm, A.ncols, s);
         }
         if (timer) timer->record(s);
@@ -1330,7 +1335,8 @@ mlem_status mlem_back_project(mlem_matrix* m, const float* ratio_dev, float* bp_
             project(m, true, r, be, o, {}, s);
         } else {
             MLEM_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * m->A.ncols, s));
-            launch_scatter(m->A, r, out, scatter_lanes(m), {}, s);
+            const int sl = scatter_lanes(m);  // sets m->scatter_unroll on the first call
+            launch_scatter(m->A, r, out, sl, m->scatter_unroll, {}, s);
         }
         if (perm) cols_out(m, bp_dev, out, s);
     });

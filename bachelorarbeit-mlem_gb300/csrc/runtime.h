@@ -137,6 +137,7 @@ struct mlem_matrix {
     uint32_t batch_tile = 0;          // autotuned batch tile (0 = not yet)
     uint32_t batch_form = 0;          // autotuned batch form: 1 graphs, 2 persistent (0 = not yet)
     int scatter_lanes = 0;            // autotuned lanes per row of the scatter back projection (0 = not yet)
+    int scatter_unroll = 1;           // and its 16-byte vectors per lane in flight
     bool tuned[2] = {false, false};   // csr-vector configuration of A / Aᵀ measured
     mlem::ProjCfg proj[2];
     std::mutex mu;

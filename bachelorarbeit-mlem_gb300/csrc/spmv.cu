@@ -310,7 +310,9 @@ __device__ __forceinline__ void scatter4(float* __restrict__ bp, uint32_t ncols,
     if (used) red_group(bp, ncols, grp, a, used);
 }
 
-template <typename V, int LPR>
+// LPR lanes per row of A; each lane loads U 16-byte vectors of (column,
+// value) before it scatters them (U loads per lane in flight).
+template <typename V, int LPR, int U>
 __global__ void __launch_bounds__(256)
 k_scatter(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
           const V* __restrict__ val, const float* __restrict__ ratio, uint32_t nrows,
@@ -324,13 +326,22 @@ k_scatter(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
     const uint64_t s = rowptr[row], t = rowptr[row + 1];
     if (r == 0.0f) return;  // adds of val*0 leave bp unchanged
     const uint4* idx4 = reinterpret_cast<const uint4*>(idx);
-    for (uint64_t v = (s >> 2) + sub; v < ((t + 3) >> 2); v += LPR) {
-        Vec4<V> p;
-        p.load(idx4, val, v);
-        float prod[4];
+    const uint64_t v1 = (t + 3) >> 2;
+    for (uint64_t v = (s >> 2) + sub; v < v1; v += (uint64_t)LPR * U) {
+        Vec4<V> p[U];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) prod[k] = __fmul_rn(p.a[k], r);
-        scatter4(bp, ncols, p.c, prod, v << 2, s, t);
+        for (int u = 0; u < U; ++u)
+            if (v + (uint64_t)u * LPR < v1) p[u].load(idx4, val, v + (uint64_t)u * LPR);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t vu = v + (uint64_t)u * LPR;
+            if (vu < v1) {
+                float prod[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) prod[k] = __fmul_rn(p[u].a[k], r);
+                scatter4(bp, ncols, p[u].c, prod, vu << 2, s, t);
+            }
+        }
     }
 }
 
@@ -561,7 +572,7 @@ void csrvec_dispatch_lanes(const DevCsr& op, const float* x, const EpiArgs& e, i
 }
 
 template <typename V>
-void scatter_dispatch(const DevCsr& A, const float* ratio, float* bp, int lanes, L2Window win,
+void scatter_dispatch(const DevCsr& A, const float* ratio, float* bp, int lanes, int unroll, L2Window win,
                       cudaStream_t s) {
     const V* val = static_cast<const V*>(A.val);
     auto go = [&](auto kern, int lpr) {
@@ -569,9 +580,15 @@ void scatter_dispatch(const DevCsr& A, const float* ratio, float* bp, int lanes,
         launch_ex(kern, dim3(ceil_div_u(threads, 256)), dim3(256), 0, s, win, A.rowptr, A.idx, val,
                   ratio, A.nrows, bp, A.ncols);
     };
-    if (lanes >= 32) go(k_scatter<V, 32>, 32);
-    else if (lanes >= 16) go(k_scatter<V, 16>, 16);
-    else go(k_scatter<V, 8>, 8);
+    if (unroll >= 2) {
+        if (lanes >= 32) go(k_scatter<V, 32, 2>, 32);
+        else if (lanes >= 16) go(k_scatter<V, 16, 2>, 16);
+        else go(k_scatter<V, 8, 2>, 8);
+    } else {
+        if (lanes >= 32) go(k_scatter<V, 32, 1>, 32);
+        else if (lanes >= 16) go(k_scatter<V, 16, 1>, 16);
+        else go(k_scatter<V, 8, 1>, 8);
+    }
 }
 
 }  // namespace
@@ -620,13 +637,13 @@ void launch_csrvec_pipe(const DevCsr& op, const float* x, const EpiArgs& epi, in
     }
 }
 
-void launch_scatter(const DevCsr& A, const float* ratio, float* bp, int lanes, L2Window win,
+void launch_scatter(const DevCsr& A, const float* ratio, float* bp, int lanes, int unroll, L2Window win,
                     cudaStream_t s) {
     if (A.nrows == 0) return;
     switch (A.vt) {
-        case MLEM_VAL_F32: scatter_dispatch<float>(A, ratio, bp, lanes, win, s); break;
-        case MLEM_VAL_F16: scatter_dispatch<__half>(A, ratio, bp, lanes, win, s); break;
-        default: scatter_dispatch<__nv_bfloat16>(A, ratio, bp, lanes, win, s);
+        case MLEM_VAL_F32: scatter_dispatch<float>(A, ratio, bp, lanes, unroll, win, s); break;
+        case MLEM_VAL_F16: scatter_dispatch<__half>(A, ratio, bp, lanes, unroll, win, s); break;
+        default: scatter_dispatch<__nv_bfloat16>(A, ratio, bp, lanes, unroll, win, s);
     }
 }
 
