@@ -554,6 +554,24 @@ def run_batched(pkg, torch, fp32_mid_rate=None):
     if fp32_mid_rate:
         out["vs_fp32_plain_same_matrix"] = out["images_iterations_per_s"] / fp32_mid_rate
     mb.close()
+    # the same 64 reconstructions one after the other on the plain FP32 matrix
+    # (device-resident sinograms and images, CUDA events around all 64 runs)
+    m32 = pkg.Matrix.generate(geo_b, value_type=pkg.VAL_F32, layout=LAYOUT)
+    Gd = torch.from_numpy(G).cuda()
+    F0 = torch.from_numpy(np.stack([np.full(m32.cols, m32.initial_value(G[k]), np.float32) for k in range(64)])).cuda()
+    f = torch.empty(m32.cols, dtype=torch.float32, device="cuda")
+    f.copy_(F0[0])
+    m32.run_device(Gd[0].data_ptr(), f.data_ptr(), 5, stream=s.cuda_stream)  # tuning and graphs settled
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for k in range(64):
+        f.copy_(F0[k])
+        m32.run_device(Gd[k].data_ptr(), f.data_ptr(), int(its[k]), stream=s.cuda_stream)
+    b.record(s)
+    b.synchronize()
+    out["sequential_fp32_images_iterations_per_s"] = float(its.sum()) / (a.elapsed_time(b) * 1e-3)
+    out["vs_sequential_fp32"] = out["images_iterations_per_s"] / out["sequential_fp32_images_iterations_per_s"]
+    m32.close()
     return out
 
 
@@ -717,6 +735,8 @@ def forms_summary(forms, fp32_rate):
     put("ring2d_fp32_plain_iter_s", forms.get("fp32_plain_ring2d", {}).get("images_iterations_per_s"), nd=0)
     b = forms.get("batched_fp16_64", {})
     put("batched_fp16_64_images_iter_s", b.get("images_iterations_per_s"), mid)
+    put("sequential_fp32_64_images_iter_s", b.get("sequential_fp32_images_iterations_per_s"))
+    put("batched_vs_sequential_fp32", b.get("vs_sequential_fp32"), nd=3)
     put("batched_persistent_images_iter_s", b.get("persistent_images_iterations_per_s"))
     put("batched_graphs_images_iter_s", b.get("graphs_images_iterations_per_s"))
     modes = forms.get("modes_cyl3d_mid") or forms
