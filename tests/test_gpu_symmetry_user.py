@@ -42,6 +42,15 @@ def test_callers_symmetric_matrix_matches_plain_path(pkg, O, name):
     ref64 = O.mlem_f64(A, p["g"], p["norm"], p["f0"], iters)
     assert O.rel_l2(m.run(p["g"], iters, f0=p["f0"], kernel=pkg.KERNEL_SYM), ref64) < TOL_F32
     m.close()
+    # FP16 values: the compact operands hold the same rounded values as the matrix
+    h = pkg.Matrix.from_csr(*A, p["cols"], value_type=pkg.VAL_F16, **_sym_args(p["geo"]))
+    plain16 = pkg.Matrix.from_csr(*A, p["cols"], value_type=pkg.VAL_F16)
+    want16 = plain16.run(p["g"], iters, f0=p["f0"])
+    plain16.close()
+    got16 = h.run(p["g"], iters, f0=p["f0"], kernel=pkg.KERNEL_SYM)
+    h.close()
+    assert O.rel_l2(got16, want16) < TOL_F32
+    assert O.rel_l2(got16, ref64) < 1e-3
 
 
 def test_callers_matrix_at_full_size(pkg, O, cuda):
