@@ -252,8 +252,10 @@ def cpu_baseline(P, iters=3):
     sec = cpu_iterations(P, iters, threads)
     sec1 = cpu_iterations(P, 1, 1)
     assert O.max_threads() == threads  # the one-thread run leaves the default alone
+    fp_b, bp_b = algorithmic_bytes(P["rows"], P["cols"], P["nnz"], 4)
     return {"value": 1.0 / sec, "unit": "iter/s", "cores": threads, "kind": "port", "cpu_model": cpu_model(),
-            "one_thread_value": 1.0 / sec1,
+            "one_thread_value": 1.0 / sec1, "achieved_gbs": (fp_b + bp_b) / sec / 1e9,
+            "one_thread_gbs": (fp_b + bp_b) / sec1 / 1e9,
             "sample": f"full matrix ({P['rows']} rows, {P['nnz']} nnz): {iters} OpenMP MLEM iterations on "
                       f"{threads} threads after 1 warm-up, and 1 iteration on 1 thread (FP32 values and image, "
                       f"FP64 accumulation, transposed form)",
@@ -326,6 +328,7 @@ def run_reference(args):
         "form": "CPU CSR MLEM, transposed form, natural layout",
         "cpu_baseline": {"value": value, "unit": "iter/s", "cores": threads, "kind": "port",
                          "cpu_model": cpu_model(), "one_thread_value": 1.0 / sec1,
+                         "achieved_gbs": sum(algorithmic_bytes(P["rows"], P["cols"], P["nnz"], 4)) * value / 1e9,
                          "sample": f"full matrix ({P['rows']} rows, {P['nnz']} nnz), one MLEM iteration per step "
                                    f"on {threads} threads; one_thread_value: one iteration on 1 thread",
                          "step_ms": [round(x * 1e3, 2) for x in per_step], "input_prep_s": round(P["prep_s"], 1)},
