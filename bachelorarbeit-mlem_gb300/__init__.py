@@ -68,7 +68,8 @@ class RunOpts(C.Structure):
     _fields_ = [("spmv", C.c_int), ("bp_mode", C.c_int), ("secsize_fp", C.c_uint32),
                 ("secsize_bp", C.c_uint32), ("use_graph", C.c_uint32), ("loglik_every", C.c_uint32),
                 ("l2_window", C.c_uint32), ("kernel", C.c_uint32), ("lanes", C.c_uint32), ("unroll", C.c_uint32),
-                ("row_order", C.c_uint32), ("pipeline", C.c_uint32), ("kernel_timing", C.c_uint32)]
+                ("row_order", C.c_uint32), ("pipeline", C.c_uint32), ("kernel_timing", C.c_uint32),
+                ("loglik_rel_tol", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -408,7 +409,7 @@ class Matrix:
     @staticmethod
     def run_opts(spmv=SPMV_CSR_VECTOR, bp_mode=BP_TRANS, secsize_fp=5, secsize_bp=5, use_graph=True,
                  loglik_every=0, l2_window=True, kernel=KERNEL_AUTO, lanes=0, unroll=0,
-                 row_order=False, pipeline=False, kernel_timing=False) -> RunOpts:
+                 row_order=False, pipeline=False, kernel_timing=False, loglik_rel_tol=0.0) -> RunOpts:
         o = RunOpts()
         load_library().mlem_run_opts_default(C.byref(o))
         o.spmv, o.bp_mode, o.secsize_fp, o.secsize_bp = spmv, bp_mode, secsize_fp, secsize_bp
@@ -416,6 +417,7 @@ class Matrix:
         o.kernel, o.lanes, o.unroll, o.row_order = int(kernel), int(lanes), int(unroll), int(row_order)
         o.pipeline = int(pipeline)
         o.kernel_timing = int(kernel_timing)
+        o.loglik_rel_tol = float(loglik_rel_tol)
         return o
 
     def run(self, g, iterations: int, f0=None, loglik=False, stats=False, **opts):

@@ -297,6 +297,10 @@ void check_run_opts(const mlem_matrix* m, const mlem_run_opts& o) {
                  MLEM_EINVAL, "bp_mode must be 0 (transposed), 1 (scatter) or 2 (fused)");
     MLEM_REQUIRE(o.secsize_fp >= 1 && o.secsize_fp <= 512 && o.secsize_bp >= 1 && o.secsize_bp <= 512,
                  MLEM_EINVAL, "section sizes must be in 1..512");
+    MLEM_REQUIRE(o.loglik_rel_tol >= 0.0 && std::isfinite(o.loglik_rel_tol), MLEM_EINVAL,
+                 "loglik_rel_tol must be a finite value >= 0");
+    MLEM_REQUIRE(o.loglik_rel_tol == 0.0 || o.loglik_every > 0, MLEM_EINVAL,
+                 "loglik_rel_tol needs loglik_every > 0");
     MLEM_REQUIRE(o.bp_mode != MLEM_BP_TRANS || m->has_t, MLEM_EINVAL,
                  "transposed back projection needs a matrix created with build_transpose = 1");
 }
@@ -583,12 +587,13 @@ static void enable_l2_persisting(int dev) {
     cudaGetLastError();
 }
 
-static void run_iterations(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
-                           double* ll_dev, StageTimer* timer, bool fused);
+static uint32_t run_iterations(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
+                               double* ll_dev, StageTimer* timer, bool fused);
 
-// Runs `iters` iterations on the workspace (g and f already in place).
-static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
-                     double* ll_dev, StageTimer* timer = nullptr) {
+// Runs `iters` iterations on the workspace (g and f already in place);
+// returns the iterations run (fewer when the convergence stop ends the run).
+static uint32_t run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
+                         double* ll_dev, StageTimer* timer = nullptr) {
     // symmetry-compressed pair: the image and the sinogram are gathered into
     // orbit order once, the iterations stay in orbit order, and the image is
     // scattered back into natural order at the end
@@ -597,18 +602,31 @@ static void run_loop(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cud
         sym_gather_image(m->sym, m->ws.f, s);
         sym_gather_sinogram(m->sym, m->ws.g, s);
     }
-    run_iterations(m, o, iters, s, ll_dev, timer, fused);
+    const uint32_t ran = run_iterations(m, o, iters, s, ll_dev, timer, fused);
     if (fused) sym_scatter_image(m->sym, m->ws.f, s);
+    return ran;
 }
 
-static void run_iterations(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
-                           double* ll_dev, StageTimer* timer, bool fused) {
+static uint32_t run_iterations(mlem_matrix* m, const mlem_run_opts& o, uint32_t iters, cudaStream_t s,
+                               double* ll_dev, StageTimer* timer, bool fused) {
     if (o.loglik_every > 0 || !o.use_graph || timer) {
+        double prev = 0.0;
+        bool have_prev = false;
         for (uint32_t it = 0; it < iters; ++it) {
             double* slot = (o.loglik_every > 0 && it % o.loglik_every == 0) ? ll_dev + it : nullptr;
             enqueue_iteration(m, o, s, slot, timer, fused);
+            if (slot && o.loglik_rel_tol > 0.0) {
+                // the log-likelihood L is evaluated on the image entering this
+                // iteration; stop once an evaluation gains less than tol * |L|
+                double v = 0.0;
+                MLEM_CUDA(cudaMemcpyAsync(&v, slot, sizeof(double), cudaMemcpyDeviceToHost, s));
+                MLEM_CUDA(cudaStreamSynchronize(s));
+                if (have_prev && v - prev < o.loglik_rel_tol * std::fabs(v)) return it + 1;
+                prev = v;
+                have_prev = true;
+            }
         }
-        return;
+        return iters;
     }
     constexpr uint32_t kChunk = 8;
     auto get_graph = [&](uint32_t chunk) -> cudaGraphExec_t {
@@ -659,6 +677,7 @@ static void run_iterations(mlem_matrix* m, const mlem_run_opts& o, uint32_t iter
     };
     if (full) replay(kChunk, full);
     if (rest) replay(1, rest);
+    return iters;
 }
 
 static void postprocess_matrix(mlem_matrix* m, const mlem_matrix_opts& o) {
@@ -911,6 +930,7 @@ void mlem_run_opts_default(mlem_run_opts* o) {
     o->row_order = 0;
     o->pipeline = 0;
     o->kernel_timing = 0;
+    o->loglik_rel_tol = 0.0;
 }
 
 mlem_status mlem_matrix_create(const mlem_csr_host* csr, const mlem_matrix_opts* opts, mlem_matrix** out) {
@@ -1204,7 +1224,7 @@ mlem_status mlem_run(mlem_matrix* m, const int32_t* g, const float* f0, uint32_t
         const uint64_t l0 = g_launches.load();
         StageTimer timer;
         MLEM_CUDA(cudaEventRecord(e0, s));
-        run_loop(m, o, iterations, s, w.ll_vals, o.kernel_timing ? &timer : nullptr);
+        const uint32_t ran = run_loop(m, o, iterations, s, w.ll_vals, o.kernel_timing ? &timer : nullptr);
         MLEM_CUDA(cudaEventRecord(e1, s));
         const uint64_t l1 = g_launches.load();
         if (perm) {
@@ -1232,7 +1252,7 @@ mlem_status mlem_run(mlem_matrix* m, const int32_t* g, const float* f0, uint32_t
             stats->seconds_total =
                 std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             stats->seconds_iterations = ms * 1e-3;
-            stats->iterations = iterations;
+            stats->iterations = ran;
             stats->kernel_launches = (uint32_t)(l1 - l0);
             stats->bytes_h2d = h2d;
             stats->bytes_d2h = sizeof(float) * (uint64_t)cols;

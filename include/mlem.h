@@ -202,6 +202,13 @@ typedef struct {
     uint32_t kernel_timing;     /* mlem_run only: 1 = CUDA events around the forward and back
                                    projection stages of every iteration (eager launches, no graph
                                    replay); their means go to mlem_stats.fp_ms / bp_ms */
+    double loglik_rel_tol;      /* mlem_run with loglik_every > 0: 0 = run every iteration; t > 0 =
+                                   convergence stop: the run ends after the first evaluated
+                                   iteration whose log-likelihood gained less than t * |L| over the
+                                   previous evaluation (the host reads each evaluation back);
+                                   mlem_stats.iterations gives the iterations run, later
+                                   loglik_out entries stay NaN.  No counterpart in the reference,
+                                   which always runs argv[3] iterations. */
 } mlem_run_opts;
 
 /* Kernel variants of the csr-vector projections (same arithmetic; the order of
