@@ -28,7 +28,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr
 # the Siddon generator must not contract a*b+c into FMA on the device either,
 # so the host and device generators give bit-identical matrices
 PER_FILE = {"siddon.cu": ["-fmad=false"]}
-UNITS = ["spmv.cu", "spmv_tma.cu", "spmv_d16.cu", "spmv_ilv.cu", "merge.cu", "transpose.cu", "siddon.cu", "batch.cu", "runtime.cu",
+UNITS = ["spmv.cu", "spmv_tma.cu", "spmv_fused.cu", "spmv_d16.cu", "spmv_ilv.cu", "merge.cu", "transpose.cu", "siddon.cu", "batch.cu", "runtime.cu",
          "server.cu", "io.cu", "layout.cu", "symmetry.cu"]
 
 

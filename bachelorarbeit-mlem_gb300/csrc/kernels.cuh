@@ -77,6 +77,62 @@ void launch_scatter(const DevCsr& A, const float* ratio, float* bp, int lanes, i
 // One pass over A: sum = A[r,:]·x, ratio = g[r]/sum, bp[idx] += val*ratio.
 void launch_fused_fp_scatter(const DevCsr& A, const float* x, const int32_t* g, float* bp,
                              float* fwproj, L2Window win, cudaStream_t s);
+// The same pass by a group of `lanes` (8/16/32) per row that sums the row as
+// launch_csrvec does (unroll 1 or 2 vectors in flight per lane), then
+// re-walks it from L2 to scatter; ordered: rows in A.order.
+void launch_fused_rescan(const DevCsr& A, const float* x, const int32_t* g, float* bp, float* fwproj, int lanes,
+                         int unroll, bool ordered, L2Window win, cudaStream_t s);
+// ------------------------------------------------------------- spmv_fused.cu
+// The rows of A in chunks of whole rows for the staged fused pass: a chunk's
+// span of entries, aligned to 8, fits one shared-memory stage and holds at
+// most kFusedMaxRows rows; a row longer than a stage is a chunk of its own
+// ("wide", read from global memory).  The stage is worked in blocks of
+// kFusedBlk entries; a piece is the part of one row inside one block.
+constexpr int kFusedCap = 4096;     // entries per stage
+constexpr int kFusedMaxRows = 128;  // rows per chunk
+constexpr int kFusedBlk = 128;      // entries per block (32 lanes x 4)
+struct alignas(16) FusedChunk {
+    uint64_t a0;        // first entry of the staged span (multiple of 8)
+    uint64_t meta_off;  // the chunk's metadata in FusedPlan::meta (multiple of 4)
+    uint32_t n8;        // staged span in 8-entry units
+    uint32_t r0;        // first row
+    uint16_t nr;        // rows
+    uint16_t wide;      // 1: one row longer than a stage, not staged
+    uint32_t mlen;      // metadata words: rs[nr+1], pf[nr+1], bf[nb] (wide: rs[2])
+};
+// Metadata of a chunk (u32, relative to a0): rs[j] = start of row j (rs[nr]
+// = end of the last row); pf[j] = index of row j's first piece in the chunk's
+// piece order (pf[nr] = pieces); bf[b] = first row that ends after block b
+// starts (nb = blocks up to rs[nr]).
+struct FusedPlan {
+    uint64_t nchunks = 0;
+    FusedChunk* chunks = nullptr;  // [nchunks]
+    uint32_t* meta = nullptr;      // [meta_len]
+    uint64_t meta_len = 0;
+    bool built = false;
+    int staged_threads = 0;        // timed CTA size of the staged kernel (256 or 512; 0 = not yet)
+    float staged_ms = 0.f;         // and its time for one pass
+    void release();
+};
+// A form of the fused single pass.
+struct FusedForm {
+    int kind = 0;          // 0 register (k_fused), 1 staged (k_fused_staged), 2 rescan (k_fused_rescan)
+    int threads = 256;     // staged: CTA size
+    int lanes = 16;        // rescan: lanes per row
+    int unroll = 2;        // rescan: vectors per lane in flight
+    bool ordered = false;  // rescan: rows in locality order
+    float ms = 0.f;        // measured time of one pass
+};
+// Cuts the rows of A into chunks (host pass over the row pointers, once).
+void fused_plan_build(const DevCsr& A, FusedPlan& p, cudaStream_t s);
+// Kernel attributes and grid sizes, settled outside stream captures.
+void prepare_fused_staged(mlem_value_type vt);
+// The staged single pass: same results as launch_fused_fp_scatter up to the
+// order of the FP32 additions (products rounded before the row sum; the
+// scatter's atomic order is unordered in both).  *err is set when a bounded
+// wait expires.
+void launch_fused_staged(const DevCsr& A, const FusedPlan& p, int threads, const float* x, const int32_t* g,
+                         float* bp, float* fwproj, uint32_t* err, L2Window win, cudaStream_t s);
 // f = f*bp/norm (or f*bp), then bp = 0 — update of the scatter forms.
 void launch_update_zero(float* f, float* bp, const float* norm, uint32_t n, cudaStream_t s);
 // Σ_r g_r log(fp_r) - fp_r over rows with fp_r > 0, FP64, fixed reduction order.

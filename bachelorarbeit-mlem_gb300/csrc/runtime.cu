@@ -212,6 +212,114 @@ int scatter_lanes(mlem_matrix* m) {
     return best_l;
 }
 
+void launch_fused(mlem_matrix* m, const FusedForm& f, const float* x, const int32_t* g, float* bp, float* fwproj,
+                  L2Window win, cudaStream_t s) {
+    if (f.kind == 1) launch_fused_staged(m->A, m->fused, f.threads, x, g, bp, fwproj, m->ws.err, win, s);
+    else if (f.kind == 2) launch_fused_rescan(m->A, x, g, bp, fwproj, f.lanes, f.unroll, f.ordered, win, s);
+    else launch_fused_fp_scatter(m->A, x, g, bp, fwproj, win, s);
+}
+
+// Milliseconds of one fused pass of A in a form on an image and counts of
+// ones into a scratch image, after one warm-up launch.
+static float time_fused(mlem_matrix* m, const FusedForm& f) {
+    const DevCsr& A = m->A;
+    cudaStream_t s = m->stream;
+    float *x = nullptr, *bp = nullptr;
+    int32_t* g = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float ms = 0.f;
+    try {
+        const uint32_t R = std::max<uint32_t>(A.nrows, 1), C = std::max<uint32_t>(A.ncols, 1);
+        MLEM_CUDA(cudaMalloc(&x, sizeof(float) * C));
+        MLEM_CUDA(cudaMalloc(&bp, sizeof(float) * C));
+        MLEM_CUDA(cudaMalloc(&g, sizeof(int32_t) * R));
+        std::vector<float> ones(C, 1.0f);
+        std::vector<int32_t> gones(R, 1);
+        MLEM_CUDA(cudaMemcpyAsync(x, ones.data(), sizeof(float) * C, cudaMemcpyHostToDevice, s));
+        MLEM_CUDA(cudaMemcpyAsync(g, gones.data(), sizeof(int32_t) * R, cudaMemcpyHostToDevice, s));
+        MLEM_CUDA(cudaMemsetAsync(bp, 0, sizeof(float) * C, s));
+        MLEM_CUDA(cudaEventCreate(&e0));
+        MLEM_CUDA(cudaEventCreate(&e1));
+        launch_fused(m, f, x, g, bp, nullptr, {}, s);
+        MLEM_CUDA(cudaEventRecord(e0, s));
+        for (int q = 0; q < 2; ++q) launch_fused(m, f, x, g, bp, nullptr, {}, s);
+        MLEM_CUDA(cudaEventRecord(e1, s));
+        MLEM_CUDA(cudaEventSynchronize(e1));
+        MLEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        check_device_error(m, s);
+    } catch (...) {
+        cudaStreamSynchronize(s);
+        cudaFree(x);
+        cudaFree(bp);
+        cudaFree(g);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        throw;
+    }
+    cudaFree(x);
+    cudaFree(bp);
+    cudaFree(g);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms / 2;
+}
+
+// Form of the fused single pass for the run's kernel switch: TMA = staged
+// through shared memory (CTA size timed once per matrix), PERSISTENT = the
+// register form, AUTO = the fastest of every form and configuration (timed
+// once per matrix), any other = the rescan form with the run's lanes, vectors
+// in flight and row order.
+FusedForm fused_form(mlem_matrix* m, const mlem_run_opts& o) {
+    FusedPlan& p = m->fused;
+    FusedForm f;
+    auto staged = [&]() {
+        if (!p.staged_threads) {
+            ensure_workspace(m);
+            if (!p.built) fused_plan_build(m->A, p, m->stream);
+            prepare_fused_staged(m->A.vt);
+            FusedForm a, b;
+            a.kind = b.kind = 1;
+            a.threads = 256;
+            b.threads = 512;
+            const float ta = time_fused(m, a), tb = time_fused(m, b);
+            p.staged_threads = tb < ta ? 512 : 256;
+            p.staged_ms = std::min(ta, tb);
+        }
+        FusedForm r;
+        r.kind = 1;
+        r.threads = p.staged_threads;
+        r.ms = p.staged_ms;
+        return r;
+    };
+    if (o.kernel == MLEM_KERNEL_TMA) return staged();
+    if (o.kernel == MLEM_KERNEL_PERSISTENT) return f;  // register form
+    if (o.kernel != MLEM_KERNEL_AUTO) {
+        f.kind = 2;
+        f.lanes = o.lanes ? (int)std::max(8u, o.lanes) : std::max(8, pick_lanes(m->A.nnz, m->A.nrows));
+        f.unroll = o.unroll == 1 ? 1 : 2;
+        f.ordered = (o.kernel == MLEM_KERNEL_ORDERED || o.row_order) && m->A.order != nullptr;
+        return f;
+    }
+    if (m->fused_auto.ms > 0.f) return m->fused_auto;
+    FusedForm best = staged();
+    FusedForm reg;
+    reg.ms = time_fused(m, reg);
+    if (reg.ms < best.ms) best = reg;
+    for (int lanes : {8, 16, 32})
+        for (int u : {1, 2})
+            for (int ord = 0; ord <= (m->A.order ? 1 : 0); ++ord) {
+                FusedForm c;
+                c.kind = 2;
+                c.lanes = lanes;
+                c.unroll = u;
+                c.ordered = ord != 0;
+                c.ms = time_fused(m, c);
+                if (c.ms < best.ms) best = c;
+            }
+    m->fused_auto = best;
+    return best;
+}
+
 const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize) {
     auto& plans = transposed ? m->plan_AT : m->plan_A;
     auto it = plans.find(secsize);
@@ -516,8 +624,9 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
         wr = {w.ratio, sizeof(float) * (size_t)A.nrows};
     }
     if (o.bp_mode == MLEM_BP_FUSED) {
+        const FusedForm ff = fused_form(m, o);
         if (timer) timer->record(s);
-        launch_fused_fp_scatter(A, w.f, w.g, w.bp, want_ll ? w.fwproj : nullptr, wf, s);
+        launch_fused(m, ff, w.f, w.g, w.bp, want_ll ? w.fwproj : nullptr, wf, s);
         if (timer) {
             timer->record(s);
             timer->record(s);
@@ -641,6 +750,7 @@ static uint32_t run_iterations(mlem_matrix* m, const mlem_run_opts& o, uint32_t 
             if (o.bp_mode == MLEM_BP_TRANS) merge_plan(m, true, o.secsize_bp);
         }
         if (o.bp_mode == MLEM_BP_SCATTER) scatter_lanes(m);
+        if (o.bp_mode == MLEM_BP_FUSED) fused_form(m, o);
         cudaStream_t cs = m->stream;
         cudaGraph_t graph = nullptr;
         const uint64_t l0 = g_launches.load();
@@ -823,6 +933,7 @@ static void destroy_matrix(mlem_matrix* m) {
     m->ws.release();
     for (auto& kv : m->plan_A) kv.second.release();
     for (auto& kv : m->plan_AT) kv.second.release();
+    m->fused.release();
     free_csr(m->A);
     free_csr(m->AT);
     m->sym.release();
@@ -891,6 +1002,7 @@ uint64_t mlem_matrix::bytes() const {
     uint64_t b = csr_bytes(A) + csr_bytes(AT) + sizeof(float) * (uint64_t)A.ncols + sym.bytes();
     for (auto& kv : plan_A) b += kv.second.ntiles * 24;
     for (auto& kv : plan_AT) b += kv.second.ntiles * 24;
+    b += fused.nchunks * sizeof(FusedChunk) + fused.meta_len * sizeof(uint32_t);
     if (ws.ready) b += (uint64_t)A.nrows * 12 + (uint64_t)A.ncols * 8;
     return b;
 }

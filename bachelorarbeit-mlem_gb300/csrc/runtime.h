@@ -138,6 +138,8 @@ struct mlem_matrix {
     uint32_t batch_form = 0;          // autotuned batch form: 1 graphs, 2 persistent (0 = not yet)
     int scatter_lanes = 0;            // autotuned lanes per row of the scatter back projection (0 = not yet)
     int scatter_unroll = 1;           // and its 16-byte vectors per lane in flight
+    mlem::FusedPlan fused;            // chunks of the staged fused pass
+    mlem::FusedForm fused_auto;       // fastest form of the fused pass (timed once; ms = 0: not yet)
     bool tuned[2] = {false, false};   // csr-vector configuration of A / Aᵀ measured
     mlem::ProjCfg proj[2];
     std::mutex mu;
@@ -148,6 +150,11 @@ namespace mlem {
 // Shared by the single, batched and server paths.
 void ensure_workspace(mlem_matrix* m);
 const MergePlan& merge_plan(mlem_matrix* m, bool transposed, uint32_t secsize);
+// Form of the fused single pass for the run's options (timed once per matrix
+// where the options leave it open).
+FusedForm fused_form(mlem_matrix* m, const mlem_run_opts& o);
+void launch_fused(mlem_matrix* m, const FusedForm& f, const float* x, const int32_t* g, float* bp, float* fwproj,
+                  L2Window win, cudaStream_t s);
 // CUDA events around the forward and back projection stages of eager
 // iterations (mlem_run_opts.kernel_timing).
 struct StageTimer {

@@ -15,6 +15,7 @@
 // update are applied by the group leader in the same kernel, so an MLEM
 // iteration is two launches and never needs a memset.
 #include "kernels.cuh"
+#include "scatter.cuh"
 
 #include <algorithm>
 #include <map>
@@ -262,52 +263,15 @@ k_csrvec_pipe(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ 
     }
 }
 
-// One 16-byte reduction into bp[4g .. 4g+3]: red.global.add.v4.f32 (one L2
-// atomic operation for four floats) where the group lies inside bp and bp is
-// 16-byte aligned (a caller's output pointer may not be), else the components
-// that carry a product one by one.
-__device__ __forceinline__ void red_group(float* __restrict__ bp, uint32_t ncols, uint32_t g, const float a[4],
-                                          unsigned used) {
-    const uint32_t c0 = g << 2;
-    if (c0 + 3 < ncols && (reinterpret_cast<uintptr_t>(bp) & 15u) == 0) {
-        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(bp + c0), "f"(a[0]), "f"(a[1]),
-                     "f"(a[2]), "f"(a[3])
-                     : "memory");
-    } else {
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (used & (1u << j)) atomicAdd(bp + c0 + j, a[j]);
-    }
-}
-
 // Scatters the products p[k] of four consecutive entries of a row (those
-// with base + k in [s, t)) into bp.  A row's columns ascend, so entries whose
-// columns share a 16-byte group (column >> 2) are adjacent: each group goes
-// out as one vector reduction, with zeros in its unused components (adding
-// +0.0 leaves a sum unchanged).  Duplicate columns are summed first.  In the
-// 3-D scanners about 0.6 reductions are issued per nonzero instead of 1.
+// with base + k in [s, t)) into bp (vector reductions, scatter.cuh).
 __device__ __forceinline__ void scatter4(float* __restrict__ bp, uint32_t ncols, const uint4& c, const float p[4],
                                          uint64_t base, uint64_t s, uint64_t t) {
-    const uint32_t cs[4] = {c.x, c.y, c.z, c.w};
-    float a[4] = {0.f, 0.f, 0.f, 0.f};
-    unsigned used = 0;
-    uint32_t grp = 0xffffffffu;
+    unsigned use = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        if (!in_row(base + k, s, t)) continue;
-        const uint32_t g = cs[k] >> 2, j = cs[k] & 3u;
-        if (g != grp) {
-            if (used) red_group(bp, ncols, grp, a, used);
-            a[0] = a[1] = a[2] = a[3] = 0.f;
-            used = 0;
-            grp = g;
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (j == (uint32_t)q) a[q] = __fadd_rn(a[q], p[k]);
-        used |= 1u << j;
-    }
-    if (used) red_group(bp, ncols, grp, a, used);
+    for (int k = 0; k < 4; ++k)
+        if (in_row(base + k, s, t)) use |= 1u << k;
+    scatter4_mask(bp, ncols, c, p, use);
 }
 
 // LPR lanes per row of A; each lane loads U 16-byte vectors of (column,
@@ -404,6 +368,49 @@ k_fused(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
         float prod[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) prod[k] = __fmul_rn(p.a[k], r);
+        scatter4(bp, ncols, p.c, prod, v << 2, s, t);
+    }
+}
+
+// Fused single pass at the occupancy of the projection kernels: a group of
+// LPR lanes per row sums the row exactly as k_csrvec<V, LPR, U> does (same
+// order of additions), computes the ratio, then walks the row a second time
+// (its vectors were streamed a moment before, so L2 serves them) and
+// scatters val * ratio with the grouped vector reductions.  A crosses HBM
+// once per iteration.
+template <typename V, int LPR, int U, bool ORD>
+__global__ void __launch_bounds__(256)
+k_fused_rescan(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
+               const V* __restrict__ val, const float* __restrict__ x, uint32_t nrows,
+               const int32_t* __restrict__ g, float* __restrict__ bp, float* __restrict__ fwproj,
+               uint32_t ncols, const uint32_t* __restrict__ order) {
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t k = gt / LPR;
+    const int sub = threadIdx.x & (LPR - 1);
+    float acc = 0.f;
+    uint32_t row = k;
+    uint64_t s = 0, t = 0;
+    int32_t gr = 0;
+    if (k < nrows) {
+        if (ORD) row = __ldg(order + k);
+        s = rowptr[row];
+        t = rowptr[row + 1];
+        gr = g[row];
+        acc = lane_dot<V, LPR, U>(idx, val, x, s, t, sub);
+    }
+    acc = group_sum<LPR>(acc);
+    if (k >= nrows) return;
+    if (sub == 0 && fwproj) fwproj[row] = acc;
+    const float r = (acc != 0.0f) ? __fdiv_rn((float)gr, acc) : 0.0f;
+    if (r == 0.0f) return;  // adds of val*0 leave bp unchanged
+    const uint4* idx4 = reinterpret_cast<const uint4*>(idx);
+    const uint64_t v1 = (t + 3) >> 2;
+    for (uint64_t v = (s >> 2) + sub; v < v1; v += LPR) {
+        Vec4<V> p;
+        p.load(idx4, val, v);
+        float prod[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) prod[q] = __fmul_rn(p.a[q], r);
         scatter4(bp, ncols, p.c, prod, v << 2, s, t);
     }
 }
@@ -663,6 +670,46 @@ void launch_fused_fp_scatter(const DevCsr& A, const float* x, const int32_t* g, 
         default:
             launch_ex(k_fused<__nv_bfloat16>, grid, block, 0, s, win, A.rowptr, A.idx,
                       (const __nv_bfloat16*)A.val, x, g, A.nrows, bp, fwproj, A.ncols);
+    }
+}
+
+namespace {
+template <typename V, int LPR, int U>
+void rescan_ord(const DevCsr& A, const float* x, const int32_t* g, float* bp, float* fwproj, bool ordered,
+                L2Window win, cudaStream_t s) {
+    const dim3 grid(ceil_div_u((uint64_t)A.nrows * LPR, 256)), block(256);
+    const V* val = static_cast<const V*>(A.val);
+    if (ordered)
+        launch_ex(k_fused_rescan<V, LPR, U, true>, grid, block, 0, s, win, A.rowptr, A.idx, val, x, A.nrows, g, bp,
+                  fwproj, A.ncols, (const uint32_t*)A.order);
+    else
+        launch_ex(k_fused_rescan<V, LPR, U, false>, grid, block, 0, s, win, A.rowptr, A.idx, val, x, A.nrows, g, bp,
+                  fwproj, A.ncols, (const uint32_t*)nullptr);
+}
+template <typename V>
+void rescan_cfg(const DevCsr& A, const float* x, const int32_t* g, float* bp, float* fwproj, int lanes, int unroll,
+                bool ordered, L2Window win, cudaStream_t s) {
+    if (lanes >= 32) {
+        if (unroll >= 2) rescan_ord<V, 32, 2>(A, x, g, bp, fwproj, ordered, win, s);
+        else rescan_ord<V, 32, 1>(A, x, g, bp, fwproj, ordered, win, s);
+    } else if (lanes >= 16) {
+        if (unroll >= 2) rescan_ord<V, 16, 2>(A, x, g, bp, fwproj, ordered, win, s);
+        else rescan_ord<V, 16, 1>(A, x, g, bp, fwproj, ordered, win, s);
+    } else {
+        if (unroll >= 2) rescan_ord<V, 8, 2>(A, x, g, bp, fwproj, ordered, win, s);
+        else rescan_ord<V, 8, 1>(A, x, g, bp, fwproj, ordered, win, s);
+    }
+}
+}  // namespace
+
+void launch_fused_rescan(const DevCsr& A, const float* x, const int32_t* g, float* bp, float* fwproj, int lanes,
+                         int unroll, bool ordered, L2Window win, cudaStream_t s) {
+    if (A.nrows == 0) return;
+    MLEM_REQUIRE(!ordered || A.order != nullptr, MLEM_EINVAL, "operand has no row order");
+    switch (A.vt) {
+        case MLEM_VAL_F32: rescan_cfg<float>(A, x, g, bp, fwproj, lanes, unroll, ordered, win, s); break;
+        case MLEM_VAL_F16: rescan_cfg<__half>(A, x, g, bp, fwproj, lanes, unroll, ordered, win, s); break;
+        default: rescan_cfg<__nv_bfloat16>(A, x, g, bp, fwproj, lanes, unroll, ordered, win, s);
     }
 }
 

@@ -15,6 +15,7 @@
 // Every mbarrier wait is bounded: on expiry the warp records an error in
 // *err, drains its own copies in flight (again bounded) and returns.
 #include "kernels.cuh"
+#include "tma.cuh"
 
 #include <algorithm>
 #include <map>
@@ -27,60 +28,6 @@ namespace {
 constexpr int kTmaCh = 512;       // elements per chunk
 constexpr int kTmaStages = 4;     // ring depth per warp
 constexpr int kTmaWarps = 4;      // warps per CTA
-constexpr uint32_t kWaitLimit = 1u << 24;
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait; false when the limit expired.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t it = 0; it < kWaitLimit; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-__device__ __forceinline__ uint64_t evict_first_policy() {
-    uint64_t pol;
-    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-    return pol;
-}
-
-// 1-D bulk copy global -> shared, completion counted on bar (bytes % 16 == 0,
-// both addresses 16-byte aligned).
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
-                                         uint64_t pol) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
-            smem_addr(dst)),
-        "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
-        : "memory");
-}
 
 // Staged values are read from shared memory with plain loads (the streaming
 // global loads of Val4 are not valid on a shared-memory address).
@@ -118,7 +65,7 @@ k_csr_tma(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
 
     if (lane == 0)
         for (int s = 0; s < kTmaStages; ++s) mbar_init(&S.bar[s], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    fence_mbar_init();
     __syncwarp();
 
     // row pointers of this warp's rows, 32 at a time: batch kb holds rows
@@ -190,7 +137,7 @@ k_csr_tma(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
     while (true) {
         const ChunkMeta m = S.meta[slot];
         if (m.row == 0xffffffffu) break;
-        if (!mbar_wait(&S.bar[slot], (phase >> slot) & 1u)) {
+        if (!mbar_wait_timed(&S.bar[slot], (phase >> slot) & 1u)) {
             failed = true;
             break;
         }
@@ -243,7 +190,7 @@ k_csr_tma(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx,
         // drain this warp's copies still in flight before leaving
         for (int k = 0; k < kTmaStages; ++k) {
             const int sl = (slot + k) % kTmaStages;
-            if (S.meta[sl].row != 0xffffffffu) mbar_wait(&S.bar[sl], (phase >> sl) & 1u);
+            if (S.meta[sl].row != 0xffffffffu) mbar_wait_timed(&S.bar[sl], (phase >> sl) & 1u);
         }
     }
 }

@@ -36,7 +36,7 @@ typedef enum {
     MLEM_EIO = 2,         /* unreadable / malformed file (reference: runtime_error) */
     MLEM_ENOMEM = 3,      /* device or host allocation failed, or admission refused */
     MLEM_ECUDA = 4,       /* a CUDA runtime call failed */
-    MLEM_ETIMEOUT = 5,    /* a bounded wait expired (server) */
+    MLEM_ETIMEOUT = 5,    /* a bounded wait expired (server, persistent or staged kernels) */
     MLEM_EUNSUPPORTED = 6,/* size or mode outside what the library handles */
     MLEM_EBUSY = 7        /* server queue full / object in use */
 } mlem_status;
@@ -56,7 +56,8 @@ typedef enum { MLEM_VAL_F32 = 0, MLEM_VAL_F16 = 1, MLEM_VAL_BF16 = 2 } mlem_valu
 /* Back-projection form.  MLEM_BP_TRANS and MLEM_BP_SCATTER are argv[7]=0 and
  * argv[7]=1 of the reference; MLEM_BP_FUSED is a single pass over A that does
  * forward projection, correlation and the scatter back projection row by row
- * (reads the matrix once per iteration; same arithmetic as SCATTER). */
+ * (reads the matrix once per iteration; same operations as SCATTER, the
+ * staged form rounds each product before the row sum). */
 typedef enum { MLEM_BP_TRANS = 0, MLEM_BP_SCATTER = 1, MLEM_BP_FUSED = 2 } mlem_bp_mode;
 
 /* ------------------------------------------------------------ host CSR */
@@ -187,7 +188,13 @@ typedef struct {
     uint32_t use_graph;         /* 1: replay the iteration as a CUDA graph */
     uint32_t loglik_every;      /* 0: off; k: FP64 log-likelihood every k-th iteration */
     uint32_t l2_window;         /* 1: keep the image/ratio vector L2-persisting */
-    uint32_t kernel;            /* csr-vector switch only: mlem_kernel variant */
+    uint32_t kernel;            /* csr-vector switch: mlem_kernel variant.  Fused pass
+                                   (bp_mode 2): TMA = chunks staged through shared memory,
+                                   PERSISTENT = one warp per row kept in registers, AUTO =
+                                   the fastest form and configuration (timed once per
+                                   matrix), any other = a group of `lanes` per row that
+                                   re-walks its row from L2 for the scatter (`unroll`,
+                                   ORDERED / row_order as for the projection) */
     uint32_t lanes;             /* DIRECT / PERSISTENT / ORDERED: lanes per row (4, 8, 16, 32;
                                    PERSISTENT 16 or 32); 0 = chosen from the mean row length */
     uint32_t unroll;            /* same kernels: vectors of 4 elements in flight per lane
@@ -255,7 +262,10 @@ mlem_status mlem_run(mlem_matrix* m, const int32_t* g, const float* f0, uint32_t
 
 /* Same loop on device buffers already resident in HBM: g_dev i32[rows],
  * f_dev f32[cols] holds f0 on entry and the image on exit.  Asynchronous on
- * `stream` (a cudaStream_t, NULL = legacy default stream). */
+ * `stream` (a cudaStream_t, NULL = legacy default stream).  A bounded wait
+ * that expired inside a kernel of this call (TMA kernel, staged fused pass)
+ * leaves a flag on the matrix that the next mlem_run reports as
+ * MLEM_ETIMEOUT. */
 mlem_status mlem_run_device(mlem_matrix* m, const int32_t* g_dev, float* f_dev,
                             uint32_t iterations, const mlem_run_opts* opts, void* stream);
 
