@@ -377,11 +377,14 @@ class Matrix:
         return out
 
     def tuning(self, transposed=False) -> dict:
-        """The csr-vector configuration the autotuner chose for A or Aᵀ."""
+        """The csr-vector configuration the autotuner chose for A or Aᵀ
+        (transposed = 2: the form of the fused single pass)."""
         k, ln, u, od, pp, ms = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_float()
         _check(load_library().mlem_matrix_get_tuning(self._h, int(transposed), C.byref(k), C.byref(ln),
                                                      C.byref(u), C.byref(od), C.byref(pp), C.byref(ms)))
         names = {0: "direct", 1: "tma", 2: "persistent", 4: "d16", 5: "ilv", 7: "sym"}
+        if transposed == 2:
+            names = {0: "rescan", 1: "staged", 2: "register"}
         return {"kernel": names.get(k.value, k.value), "lanes_per_row": ln.value, "vectors_in_flight": u.value,
                 "locality_order": bool(od.value), "pipelined": bool(pp.value), "ms": ms.value}
 

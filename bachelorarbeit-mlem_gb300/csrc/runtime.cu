@@ -1162,10 +1162,23 @@ mlem_status mlem_matrix_get_tuning(mlem_matrix* m, uint32_t transposed, int* ker
                                    int* ordered, int* pipelined, float* ms) {
     return guarded([&] {
         MLEM_REQUIRE(m && kernel && lanes && unroll && ordered && pipelined && ms, MLEM_EINVAL, "NULL argument");
-        MLEM_REQUIRE(transposed <= 1, MLEM_EINVAL, "transposed must be 0 or 1");
-        MLEM_REQUIRE(!transposed || m->has_t, MLEM_EINVAL, "matrix has no transpose");
+        MLEM_REQUIRE(transposed <= 2, MLEM_EINVAL, "transposed must be 0, 1 or 2 (fused pass)");
+        MLEM_REQUIRE(transposed != 1 || m->has_t, MLEM_EINVAL, "matrix has no transpose");
         std::lock_guard<std::mutex> lk(m->mu);
         DeviceGuard dg(m->device);
+        if (transposed == 2) {
+            mlem_run_opts o;
+            mlem_run_opts_default(&o);
+            o.bp_mode = MLEM_BP_FUSED;
+            const FusedForm f = fused_form(m, o);
+            *kernel = f.kind == 1 ? MLEM_KERNEL_TMA : f.kind == 0 ? MLEM_KERNEL_PERSISTENT : MLEM_KERNEL_DIRECT;
+            *lanes = f.kind == 1 ? f.threads : f.kind == 2 ? f.lanes : 32;
+            *unroll = f.kind == 2 ? f.unroll : 1;
+            *ordered = f.kind == 2 && f.ordered ? 1 : 0;
+            *pipelined = 0;
+            *ms = f.ms;
+            return;
+        }
         tune_projection(m, transposed != 0);
         const ProjCfg& c = m->proj[transposed];
         *kernel = c.kind;

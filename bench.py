@@ -724,6 +724,10 @@ def run_serving(pkg, torch, n_requests=2000, rate=50.0, serial_every=10):
 def forms_summary(forms, fp32_rate):
     """The headline figure of each form and its ratio to the FP32 plain path."""
     out = {"fp32_plain_iter_s": round(fp32_rate, 2)}
+    fz = forms.get("fused_pass")
+    if fz:
+        out["fused_pass_iter_s"] = round(fz["iterations_per_s"], 2)
+        out["fused_pass_vs_fp32_plain"] = round(fz["vs_fp32_plain"], 3)
 
     def put(key, val, ratio_to=None, nd=2):
         if val is None:
@@ -917,6 +921,25 @@ def main():
                      "autotuned": {"fp": m.tuning(False), "bp": m.tuning(True)}},
         "clocks": clk.summary(),
     }
+    if default_form:
+        # the fused single pass (argv[7]=1 arithmetic: A read once per
+        # iteration, the back projection by atomic vector reductions) on the same matrix
+        def fused_step():
+            f_dev.copy_(f0_dev)
+            m.run_device(g_dev.data_ptr(), f_dev.data_ptr(), iters, stream=s.cuda_stream, bp_mode=2,
+                         kernel=pkg.KERNEL_AUTO)
+
+        for _ in range(max(3, args.warmup)):
+            fused_step()
+        torch.cuda.synchronize()
+        a.record(s)
+        for _ in range(args.steps):
+            fused_step()
+        b.record(s)
+        torch.cuda.synchronize()
+        f_rate = args.steps * iters / (a.elapsed_time(b) * 1e-3)
+        line["fused_pass"] = {"iterations_per_s": f_rate, "vs_fp32_plain": f_rate / (value / world),
+                              "form": m.tuning(2), "matrix_bytes_per_iteration": fp_b}
     m.close()
     if args.forms == "modes":
         line["forms"] = run_modes(pkg, torch, name)
@@ -945,7 +968,7 @@ def main():
             line["forms_detail"] = str(detail.relative_to(ROOT))
         except OSError:
             line["forms"] = forms
-        line["forms_summary"] = forms_summary(forms, value / world)
+        line["forms_summary"] = forms_summary(dict(forms, fused_pass=line.get("fused_pass")), value / world)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -168,7 +168,11 @@ mlem_status mlem_matrix_get_info(const mlem_matrix* m, mlem_matrix_info* info);
  * (transposed = 0) or Aᵀ (1): kernel (mlem_kernel), lanes per row, vectors in
  * flight per lane, whether rows run in locality order, whether the row's
  * vector loads are software-pipelined, and the measured
- * milliseconds of one launch.  Tunes on first call if needed. */
+ * milliseconds of one launch.  Tunes on first call if needed.
+ * transposed = 2: the fused single pass (bp_mode 2) the AUTO switch picks —
+ * kernel = the switch that selects that form (TMA staged, PERSISTENT
+ * register, DIRECT / ordered rescan), lanes = lanes per row (staged: threads
+ * per CTA), unroll and ordered as for the rescan form. */
 mlem_status mlem_matrix_get_tuning(mlem_matrix* m, uint32_t transposed, int* kernel, int* lanes,
                                    int* unroll, int* ordered, int* pipelined, float* ms);
 /* Copies the sensitivity image (f32[cols]) to the host. */

@@ -28,8 +28,10 @@ def test_forms_summary_headlines_and_ratios():
                     "serial_fp32_reconstructions_per_s": 23.5, "vs_serial_fp32": 2.085, "p99_tail_samples": 20,
                     "mix": "not in the summary"},
         "symmetry": {"fp32": {"autotuned": {"iterations_per_s": 1290.0}}},
+        "fused_pass": {"iterations_per_s": 289.0, "vs_fp32_plain": 289.0 / 268.0, "form": {"kernel": "rescan"}},
     }
     s = b.forms_summary(forms, 268.0)
+    assert s["fused_pass_iter_s"] == 289.0 and s["fused_pass_vs_fp32_plain"] == round(289.0 / 268.0, 3)
     assert s["fp32_plain_iter_s"] == 268.0
     assert s["fp16_d16_images_iter_vs_fp32_plain"] == round(480.0 / 268.0, 3)
     assert s["batched_fp16_64_images_iter_vs_fp32_plain"] == round(8600.0 / 1750.0, 3)
