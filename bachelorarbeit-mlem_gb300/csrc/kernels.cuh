@@ -70,6 +70,11 @@ void launch_csrvec_pipe(const DevCsr& op, const float* x, const EpiArgs& epi, in
 void prepare_csr_tma(mlem_value_type vt);
 void launch_csr_tma(const DevCsr& op, const float* x, const EpiArgs& epi, uint32_t* err, L2Window win,
                     cudaStream_t s);
+// The scatter through per-warp shared-memory rings fed by cp.async.bulk
+// (spmv_tma.cu); rows with ratio 0 are not read.  *err is set when a bounded
+// wait expires; prepare_csr_tma settles its attributes outside captures.
+void launch_scatter_tma(const DevCsr& A, const float* ratio, float* bp, uint32_t* err, L2Window win,
+                        cudaStream_t s);
 // bp[idx] += val * ratio[row] over the rows of A (calcBwProj_none_trans, kernel.cu:165-177);
 // lanes per row 8/16/32, unroll = 16-byte vectors per lane in flight (1 or 2).
 void launch_scatter(const DevCsr& A, const float* ratio, float* bp, int lanes, int unroll, L2Window win,

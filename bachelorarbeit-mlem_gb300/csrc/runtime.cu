@@ -163,7 +163,9 @@ static bool permuted(const mlem_matrix* m) { return m->lor_of || m->vox_of; }
 
 // Lanes per row of A (8, 16 or 32) and 16-byte vectors per lane in flight (1
 // or 2) for the scatter back projection, timed once per matrix (ratio 1 into a
-// scratch image).  Returns the lanes; m->scatter_unroll holds the vectors.
+// scratch image), and whether the TMA-ring scatter beats the best of them.
+// Returns the lanes; m->scatter_unroll holds the vectors, m->scatter_tma the
+// choice of the TMA ring inside the MLEM iteration.
 int scatter_lanes(mlem_matrix* m) {
     if (m->scatter_lanes) return m->scatter_lanes;
     const DevCsr& A = m->A;
@@ -195,6 +197,17 @@ int scatter_lanes(mlem_matrix* m) {
                     best_u = u;
                 }
             }
+        ensure_workspace(m);
+        prepare_csr_tma(A.vt);
+        launch_scatter_tma(A, r, bp, m->ws.err, {}, s);
+        MLEM_CUDA(cudaEventRecord(e0, s));
+        for (int q = 0; q < 2; ++q) launch_scatter_tma(A, r, bp, m->ws.err, {}, s);
+        MLEM_CUDA(cudaEventRecord(e1, s));
+        MLEM_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        MLEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        check_device_error(m, s);
+        m->scatter_tma = ms < best;
     } catch (...) {
         cudaStreamSynchronize(s);
         cudaFree(r);
@@ -662,8 +675,12 @@ void enqueue_iteration(mlem_matrix* m, const mlem_run_opts& o, cudaStream_t s, d
             }
             project(m, true, w.ratio, be, o, wr, s);
         } else {
-            const int sl = scatter_lanes(m);  // sets m->scatter_unroll on the first call
-            launch_scatter(A, w.ratio, w.bp, sl, m->scatter_unroll, wr, s);
+            const int sl = scatter_lanes(m);  // sets m->scatter_unroll / scatter_tma on the first call
+            if (o.kernel == MLEM_KERNEL_TMA || (o.kernel == MLEM_KERNEL_AUTO && m->scatter_tma)) {
+                ensure_workspace(m);
+                launch_scatter_tma(A, w.ratio, w.bp, w.err, wr, s);
+            }
+            else launch_scatter(A, w.ratio, w.bp, sl, m->scatter_unroll, wr, s);
             launch_update_zero(w.f, w.bp, m->norm, A.ncols, s);
         }
         if (timer) timer->record(s);

@@ -138,6 +138,7 @@ struct mlem_matrix {
     uint32_t batch_form = 0;          // autotuned batch form: 1 graphs, 2 persistent (0 = not yet)
     int scatter_lanes = 0;            // autotuned lanes per row of the scatter back projection (0 = not yet)
     int scatter_unroll = 1;           // and its 16-byte vectors per lane in flight
+    bool scatter_tma = false;         // the TMA-ring scatter timed faster than those lanes
     mlem::FusedPlan fused;            // chunks of the staged fused pass
     mlem::FusedForm fused_auto;       // fastest form of the fused pass (timed once; ms = 0: not yet)
     bool tuned[2] = {false, false};   // csr-vector configuration of A / Aᵀ measured

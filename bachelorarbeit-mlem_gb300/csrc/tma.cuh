@@ -77,4 +77,22 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
         : "memory");
 }
 
+// Four staged values (entries 4v .. 4v+3) as floats.
+__device__ __forceinline__ void lds_val4(const float* p, uint32_t v, float out[4]) {
+    const float4 t = reinterpret_cast<const float4*>(p)[v];
+    out[0] = t.x; out[1] = t.y; out[2] = t.z; out[3] = t.w;
+}
+__device__ __forceinline__ void lds_val4(const __half* p, uint32_t v, float out[4]) {
+    const uint2 t = reinterpret_cast<const uint2*>(p)[v];
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&t.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&t.y));
+    out[0] = a.x; out[1] = a.y; out[2] = b.x; out[3] = b.y;
+}
+__device__ __forceinline__ void lds_val4(const __nv_bfloat16* p, uint32_t v, float out[4]) {
+    const uint2 t = reinterpret_cast<const uint2*>(p)[v];
+    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&t.x));
+    const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&t.y));
+    out[0] = a.x; out[1] = a.y; out[2] = b.x; out[3] = b.y;
+}
+
 }  // namespace mlem

@@ -192,7 +192,9 @@ typedef struct {
     uint32_t use_graph;         /* 1: replay the iteration as a CUDA graph */
     uint32_t loglik_every;      /* 0: off; k: FP64 log-likelihood every k-th iteration */
     uint32_t l2_window;         /* 1: keep the image/ratio vector L2-persisting */
-    uint32_t kernel;            /* csr-vector switch: mlem_kernel variant.  Fused pass
+    uint32_t kernel;            /* csr-vector switch: mlem_kernel variant (scatter mode: TMA
+                                   also streams the scatter through shared-memory rings,
+                                   AUTO takes it where it timed faster).  Fused pass
                                    (bp_mode 2): TMA = chunks staged through shared memory,
                                    PERSISTENT = one warp per row kept in registers, AUTO =
                                    the fastest form and configuration (timed once per

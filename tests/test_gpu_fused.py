@@ -1,6 +1,7 @@
 """The fused single pass (bp_mode 2: forward projection, correlation and the
 scatter back projection of argv[7]=1, the matrix read once per iteration) in each
-of its forms, against the oracle (GPU, via the C ABI).
+of its forms, and the scatter back projection streamed through shared-memory
+rings (bp_mode 1, kernel TMA), against the oracle (GPU, via the C ABI).
 
 The staged form cuts the rows into chunks of at most 4,096 staged entries and 128
 rows and reads a row longer than a stage from global memory.  The ragged matrix
@@ -121,6 +122,36 @@ def test_staged_low_precision_values(pkg, O, vt):
     m = pkg.Matrix.from_csr(*A, p["cols"], value_type=vt, build_transpose=False)
     ref64 = O.mlem_f64(A, p["g"], O.colsum(*A, p["cols"]), p["f0"], 20)
     got = m.run(p["g"], 20, f0=p["f0"], bp_mode=pkg.BP_FUSED, kernel=FORMS["staged"])
+    tol = TOL_LOWP if vt == 1 else 1e-2
+    assert O.rel_l2(got, ref64) < tol, O.rel_l2(got, ref64)
+    m.close()
+
+
+@pytest.mark.parametrize("kern", [1, 0, 3])
+def test_scatter_forms_on_ragged_rows(pkg, O, kern):
+    """bp_mode 1 (argv[7]=1): TMA rings (rows with ratio 0 and empty rows are not
+    staged, long rows go in pieces of 512), the direct kernel and the tuner's pick."""
+    A, cols, rng, xt = ragged(seed=13)
+    g = sinogram(O, A, xt, rng)
+    norm = O.colsum(*A, cols, f64=True)
+    f0 = np.full(cols, O.initial_value(g, norm), np.float32)
+    m = pkg.Matrix.from_csr(*A, cols, norm=norm, build_transpose=False)
+    iters = 12
+    got = m.run(g, iters, f0=f0, bp_mode=pkg.BP_SCATTER, kernel=kern)
+    ref32 = O.mlem_f32(A, None, g, norm, f0, iters, spmv=1, using_trans=1)
+    assert O.rel_l2(got, ref32) < TOL_F32, O.rel_l2(got, ref32)
+    eager = m.run(g, iters, f0=f0, bp_mode=pkg.BP_SCATTER, kernel=kern, use_graph=False)
+    assert O.rel_l2(eager, got) < TOL_F32
+    m.close()
+
+
+@pytest.mark.parametrize("vt", [1, 2])
+def test_scatter_tma_low_precision_values(pkg, O, vt):
+    p = problem(pkg, O, "cyl3d_tiny_dense")
+    A = (p["rp"], p["col"], p["val"])
+    m = pkg.Matrix.from_csr(*A, p["cols"], value_type=vt, build_transpose=False)
+    ref64 = O.mlem_f64(A, p["g"], O.colsum(*A, p["cols"]), p["f0"], 20)
+    got = m.run(p["g"], 20, f0=p["f0"], bp_mode=pkg.BP_SCATTER, kernel=1)
     tol = TOL_LOWP if vt == 1 else 1e-2
     assert O.rel_l2(got, ref64) < tol, O.rel_l2(got, ref64)
     m.close()
