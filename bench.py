@@ -938,8 +938,11 @@ def main():
         b.record(s)
         torch.cuda.synchronize()
         f_rate = args.steps * iters / (a.elapsed_time(b) * 1e-3)
+        # its algorithmic bytes: one forward-projection stream (A once, the row
+        # pointers, g, f) per iteration; the update's vectors are left out
         line["fused_pass"] = {"iterations_per_s": f_rate, "vs_fp32_plain": f_rate / (value / world),
-                              "form": m.tuning(2), "matrix_bytes_per_iteration": fp_b}
+                              "form": m.tuning(2), "bytes_per_iteration": fp_b,
+                              "achieved_gbs": fp_b * f_rate / 1e9, "frac": fp_b * f_rate / 1e9 / peak}
     m.close()
     if args.forms == "modes":
         line["forms"] = run_modes(pkg, torch, name)
