@@ -34,6 +34,13 @@
 // Every mbarrier wait is bounded (kBarrierWaitNs of %globaltimer): on expiry
 // the CTA sets *err, thread 0 waits (again bounded) for its copies still in
 // flight, and the CTA returns; the host reports MLEM_ETIMEOUT.
+//
+// The other forms of the pass are k_fused_rescan and k_fused (spmv.cu); the
+// run option `kernel` selects one, and AUTO times them all once per matrix
+// (fused_form, runtime.cu).  On the scanners measured the rescan form wins:
+// each CTA here works on one chunk at a time, so its gathers, its slowest
+// warp and its reductions follow one another with 16-24 warps per SM to hide
+// them.
 #include "kernels.cuh"
 #include "scatter.cuh"
 #include "tma.cuh"
