@@ -1,6 +1,7 @@
 """Full-size accuracy: the 3-D mid matrix (208 M nonzeros) and the 12 GB-class
-matrix (1.43 B nonzeros), 100 MLEM iterations, FP32 values and FP16 values
-with 16-bit delta-coded indices (FP32 accumulation), against the FP64 oracle (back projection over Aᵀ, OpenMP)
+matrix (1.43 B nonzeros), 100 MLEM iterations, FP32 values (transposed back
+projection, and the fused single pass) and FP16 values with 16-bit
+delta-coded indices (FP32 accumulation), against the FP64 oracle (back projection over Aᵀ, OpenMP)
 on the FP32 matrix.  Bars: image relative L2 1e-5 (FP32) and 1e-3 (FP16);
 log-likelihood relative error 1e-6 (FP32) and 1e-4 (FP16).  The measured
 errors are printed (run with -s to see them)."""
@@ -32,10 +33,18 @@ def test_full_size_fp32_and_fp16_against_fp64_oracle(pkg, O, cuda, name):
     g = _sinogram(pkg, m, geo, cfg, cuda)
     f0 = np.full(m.cols, m.initial_value(g), np.float32)
     img32, ll32 = m.run(g, iters, f0=f0, loglik=True)
+    # the fused single pass (argv[7]=1 arithmetic, A read once per iteration;
+    # the form the autotuner picks)
+    imgF, llF = m.run(g, iters, f0=f0, loglik=True, bp_mode=pkg.BP_FUSED)
+    formF = m.tuning(2)["kernel"]
     A, AT, norm = m.csr(), m.transpose(), m.norm()
     m.close()
     ref, llref = O.mlem_f64_t(A, AT, g, norm, f0, iters, loglik=True)
     del A, AT
+    eF = O.rel_l2(imgF, ref)
+    lF = float(np.max(np.abs(llF - llref) / np.abs(llref)))
+    print(f"\n{name}: fused pass ({formF}) vs FP64 oracle: image rel L2 {eF:.3e}, log-likelihood {lF:.3e}")
+    assert eF < 1e-5 and lF < 1e-6
     # FP16 values with 16-bit delta-coded indices (the compact precision form;
     # the autotuner picks among the csr-vector, interleaved and D16 kernels)
     m16 = pkg.Matrix.generate(geo, value_type=pkg.VAL_F16, compress=True)
