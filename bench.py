@@ -774,6 +774,8 @@ def main():
                          "the reference's switch combinations, the fused pass and a batched run on --workload; "
                          "symmetry: only the symmetry-compressed operands on --workload")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--detail-dir", default="bench_out",
+                    help="folder (relative to the repository) for the per-variant detail of the forms")
     ap.add_argument("--spmv", default="csr-vector", choices=["csr-vector", "merge"],
                     help="SpMV of the timed reconstruction (the reference's argv[8])")
     ap.add_argument("--values", default="f32", choices=["f32", "f16", "bf16"],
@@ -964,9 +966,9 @@ def main():
     if "forms" in line:
         # the per-variant detail goes to a file; the line ends with the headline of each form
         forms = line.pop("forms")
-        detail = ROOT / "gpurun_out" / f"bench_forms_{name}.json"
+        detail = ROOT / args.detail_dir / f"bench_forms_{name}.json"
         try:
-            detail.parent.mkdir(exist_ok=True)
+            detail.parent.mkdir(parents=True, exist_ok=True)
             detail.write_text(json.dumps(forms, indent=1))
             line["forms_detail"] = str(detail.relative_to(ROOT))
         except OSError:
