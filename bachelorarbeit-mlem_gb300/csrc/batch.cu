@@ -65,7 +65,7 @@ __device__ __forceinline__ void batch_rows(const uint64_t* __restrict__ rowptr, 
             c[i] = 0;
             v[i] = 0.f;
             if (e < t) {
-                c[i] = __ldcs(idx + e);
+                c[i] = ld_stream(idx + e);
                 v[i] = Val4<V>::one(val, e);
             }
         }
@@ -172,7 +172,7 @@ k_batch_scatter(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict_
         uint32_t c = 0;
         float v = 0.f;
         if (e < t) {
-            c = __ldcs(idx + e);
+            c = ld_stream(idx + e);
             v = Val4<V>::one(val, e);
         }
         const int n = (t - base) > 32 ? 32 : (int)(t - base);

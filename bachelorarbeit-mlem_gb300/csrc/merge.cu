@@ -146,7 +146,7 @@ k_merge_tile(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ i
     }
     for (uint32_t u = threadIdx.x; u < nj; u += T) {
         const uint64_t e = J0 + u;
-        s_prod[u] = __fmul_rn(load_val<V>(val, e), __ldg(x + __ldcs(idx + e)));
+        s_prod[u] = __fmul_rn(load_val<V>(val, e), __ldg(x + ld_stream(idx + e)));
     }
     __syncthreads();
 
@@ -276,7 +276,7 @@ __device__ __forceinline__ float group_part_dot(const uint32_t* __restrict__ idx
     uint64_t v = (s >> 2) + sub;
     if constexpr (U == 2)
     for (; v + LPR < v1; v += 2 * LPR) {
-        const uint4 c0 = __ldcs(idx4 + v), c1 = __ldcs(idx4 + v + LPR);
+        const uint4 c0 = ld_stream(idx4 + v), c1 = ld_stream(idx4 + v + LPR);
         float a0[4], a1[4];
         Val4<V>::load(val, v, a0);
         Val4<V>::load(val, v + LPR, a1);
@@ -297,7 +297,7 @@ __device__ __forceinline__ float group_part_dot(const uint32_t* __restrict__ idx
             if (k < (int)hi1) acc = fmaf(a1[k], g1[k], acc);
     }
     for (; v < v1; v += LPR) {
-        const uint4 c = __ldcs(idx4 + v);
+        const uint4 c = ld_stream(idx4 + v);
         float a[4];
         Val4<V>::load(val, v, a);
         const uint32_t cs[4] = {c.x, c.y, c.z, c.w};

@@ -32,8 +32,8 @@ struct Vec4 {
     uint4 c;
     float a[4];
     __device__ __forceinline__ void load(const uint4* idx4, const V* val, uint64_t v) {
-        c = __ldcs(idx4 + v);
-        Val4<V>::load(val, v, a);
+        c = ld_cached(idx4 + v);
+        Val4<V>::load_cached(val, v, a);
     }
 };
 

@@ -35,7 +35,7 @@ template <>
 struct Val8<float> {
     static __device__ __forceinline__ void load(const float* p, uint64_t v, float out[8]) {
         const float4* q = reinterpret_cast<const float4*>(p) + 2 * v;
-        const float4 a = __ldcs(q), b = __ldcs(q + 1);
+        const float4 a = ld_stream(q), b = ld_stream(q + 1);
         out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
         out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
     }
@@ -44,7 +44,7 @@ struct Val8<float> {
 template <>
 struct Val8<__half> {
     static __device__ __forceinline__ void load(const __half* p, uint64_t v, float out[8]) {
-        const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p) + v);
+        const uint4 u = ld_stream(reinterpret_cast<const uint4*>(p) + v);
         const uint32_t w[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -58,7 +58,7 @@ struct Val8<__half> {
 template <>
 struct Val8<__nv_bfloat16> {
     static __device__ __forceinline__ void load(const __nv_bfloat16* p, uint64_t v, float out[8]) {
-        const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p) + v);
+        const uint4 u = ld_stream(reinterpret_cast<const uint4*>(p) + v);
         const uint32_t w[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -100,7 +100,7 @@ k_csr_d16(const uint64_t* __restrict__ dvptr, const uint32_t* __restrict__ dbase
         for (int u = 0; u < U; ++u) {
             if (k + u < nsteps) {
                 const uint64_t v = v0 + (uint64_t)(k + u) * LPR + gl;
-                dw[u] = __ldcs(dv + v);
+                dw[u] = ld_stream(dv + v);
                 Val8<V>::load(dval, v, a[u]);
             } else {
                 dw[u] = make_uint4(0u, 0u, 0u, 0u);

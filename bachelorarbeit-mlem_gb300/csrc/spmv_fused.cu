@@ -89,9 +89,9 @@ __device__ __forceinline__ void wide_row(FusedSmem<V, T>& S, uint32_t row, uint6
     const uint64_t v1 = (t + 3) >> 2;
     float acc = 0.f;
     for (uint64_t v = (s >> 2) + tid; v < v1; v += T) {
-        const uint4 c = __ldcs(idx4 + v);
+        const uint4 c = ld_cached(idx4 + v);
         float a[4];
-        Val4<V>::load(val, v, a);
+        Val4<V>::load_cached(val, v, a);
         const uint32_t cs[4] = {c.x, c.y, c.z, c.w};
         const uint64_t b = v << 2;
 #pragma unroll
@@ -113,9 +113,9 @@ __device__ __forceinline__ void wide_row(FusedSmem<V, T>& S, uint32_t row, uint6
     const float r = S.bcast;
     if (r == 0.0f) return;
     for (uint64_t v = (s >> 2) + tid; v < v1; v += T) {
-        const uint4 c = __ldcs(idx4 + v);
+        const uint4 c = ld_cached(idx4 + v);
         float a[4], pr[4];
-        Val4<V>::load(val, v, a);
+        Val4<V>::load_cached(val, v, a);
         const uint64_t b = v << 2;
         unsigned use = 0;
 #pragma unroll

@@ -51,7 +51,7 @@ k_csr_ilv(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__ idx_
         for (int q = 0; q < U; ++q) {
             if (b + q < b1) {
                 const uint64_t vi = ((b + q) << 5) + lane;
-                c[q] = __ldcs(idx4 + vi);
+                c[q] = ld_stream(idx4 + vi);
                 Val4<V>::load(val_i, vi, a[q]);
             }
         }

@@ -147,7 +147,7 @@ __host__ __device__ __forceinline__ VoxMap vox_map(int s, int32_t n, int32_t nz)
 
 template <typename V>
 __device__ __forceinline__ float ld_val(const V* p, uint64_t e) {
-    return Val4<V>::one(p, e);
+    return Val4<V>::one_cached(p, e);
 }
 
 // cp.async.bulk.prefetch.L2 of [p, p + bytes) widened to 16-byte granules.
@@ -177,7 +177,7 @@ __device__ __forceinline__ void orbit_step(const uint32_t* __restrict__ kp, cons
     for (int u = 0; u < UU; ++u) {
         const uint32_t i = base + slot + 8 * u;
         const bool ok = !PRED || i < n;
-        kk[u] = ok ? __ldcs(kp + i) : 0u;
+        kk[u] = ok ? ld_cached(kp + i) : 0u;
         v[u] = ok ? ld_val<V>(vp, i) : 0.f;
     }
 #pragma unroll
