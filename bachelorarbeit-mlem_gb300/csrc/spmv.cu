@@ -415,14 +415,42 @@ k_fused_rescan(const uint64_t* __restrict__ rowptr, const uint32_t* __restrict__
     }
 }
 
+// calcUpdate (kernel.cu:34-37) for the scatter forms: f * bp / norm, left to right.
+__device__ __forceinline__ float update_one(float f, float b, float nn) {
+    const float t = __fmul_rn(f, b);
+    return (nn == 0.0f) ? t : __fdiv_rn(t, nn);
+}
+
 __global__ void k_update_zero(float* __restrict__ f, float* __restrict__ bp,
                               const float* __restrict__ norm, uint32_t n) {
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         const float b = bp[c];
         bp[c] = 0.0f;
-        const float t = __fmul_rn(f[c], b);
-        const float nn = norm[c];
-        f[c] = (nn == 0.0f) ? t : __fdiv_rn(t, nn);
+        f[c] = update_one(f[c], b, norm[c]);
+    }
+}
+
+// Four columns per thread with 16-byte accesses (16-byte aligned arrays); the
+// n % 4 last columns go to the first threads of block 0.  Same arithmetic.
+__global__ void k_update_zero4(float* __restrict__ f, float* __restrict__ bp, const float* __restrict__ norm,
+                               uint32_t n) {
+    const uint32_t n4 = n >> 2;
+    float4* f4 = reinterpret_cast<float4*>(f);
+    float4* b4 = reinterpret_cast<float4*>(bp);
+    const float4* m4 = reinterpret_cast<const float4*>(norm);
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n4; c += gridDim.x * blockDim.x) {
+        const float4 b = b4[c];
+        const float4 x = f4[c];
+        const float4 nn = __ldg(m4 + c);
+        b4[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        f4[c] = make_float4(update_one(x.x, b.x, nn.x), update_one(x.y, b.y, nn.y), update_one(x.z, b.z, nn.z),
+                            update_one(x.w, b.w, nn.w));
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (n & 3u)) {
+        const uint32_t c = (n4 << 2) + threadIdx.x;
+        const float b = bp[c];
+        bp[c] = 0.0f;
+        f[c] = update_one(f[c], b, norm[c]);
     }
 }
 
@@ -715,8 +743,15 @@ void launch_fused_rescan(const DevCsr& A, const float* x, const int32_t* g, floa
 
 void launch_update_zero(float* f, float* bp, const float* norm, uint32_t n, cudaStream_t s) {
     if (n == 0) return;
-    const unsigned grid = std::min<unsigned>(ceil_div_u(n, 256), 152u * 16u);
-    k_update_zero<<<grid, 256, 0, s>>>(f, bp, norm, n);
+    const bool aligned = ((reinterpret_cast<uintptr_t>(f) | reinterpret_cast<uintptr_t>(bp) |
+                           reinterpret_cast<uintptr_t>(norm)) & 15u) == 0;
+    if (aligned) {
+        const unsigned grid = std::max(1u, std::min<unsigned>(ceil_div_u(n >> 2, 256), 152u * 16u));
+        k_update_zero4<<<grid, 256, 0, s>>>(f, bp, norm, n);
+    } else {
+        const unsigned grid = std::min<unsigned>(ceil_div_u(n, 256), 152u * 16u);
+        k_update_zero<<<grid, 256, 0, s>>>(f, bp, norm, n);
+    }
     MLEM_LAUNCHED();
 }
 
